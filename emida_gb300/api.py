@@ -1,0 +1,265 @@
+"""Python mirror of the reference's driver interface over the C ABI.
+
+`GpuOffset` follows `template<class T, class IN> class gpu_offset`
+(src/gpu_offset.hpp:48-326) member by member; `get_offset` follows the free
+function of src/get_offset.hpp:7-20.  Names, argument meaning and the
+failure behaviour (an exception) are the reference's; the work is done by
+libemida_gb.so.
+"""
+import ctypes
+
+import numpy as np
+
+from . import _lib
+from ._lib import BRUTE, DOUBLE, FFT, FLOAT, IN_F64, IN_U16, MODE_AUTO, MODE_FUSED, MODE_PLAIN
+
+CROSS_POLICY_BRUTE, CROSS_POLICY_FFT = BRUTE, FFT
+
+# data_index<T> of src/common.hpp:152-159 ({T data; uint32 index}, natural alignment)
+DATA_INDEX_F32 = np.dtype([("data", "<f4"), ("index", "<u4")], align=True)
+DATA_INDEX_F64 = np.dtype([("data", "<f8"), ("index", "<u4")], align=True)
+
+
+def _ptr(a):
+    return ctypes.c_void_p(a.ctypes.data)
+
+
+def _dptr(a):
+    return a.ctypes.data_as(ctypes.POINTER(ctypes.c_double))
+
+
+def _precision(p):
+    if p in (DOUBLE, "double", np.float64):
+        return DOUBLE
+    if p in (FLOAT, "float", np.float32):
+        return FLOAT
+    raise ValueError(f"Invalid precision argument: {p!r}")
+
+
+def _policy(p):
+    if p in (BRUTE, "brute"):
+        return BRUTE
+    if p in (FFT, "fft"):
+        return FFT
+    raise ValueError(f"Invalid crosspolicy argument: {p!r}")
+
+
+def _mode(m):
+    return {"auto": MODE_AUTO, "plain": MODE_PLAIN, "fused": MODE_FUSED}.get(m, m)
+
+
+class DeviceBuffer:
+    """A device allocation made through the C ABI (emida_gb_malloc)."""
+
+    def __init__(self, nbytes):
+        self.nbytes = int(nbytes)
+        p = ctypes.c_void_p()
+        _lib.call("emida_gb_malloc", ctypes.byref(p), self.nbytes)
+        self.ptr = p
+
+    @classmethod
+    def from_array(cls, a):
+        a = np.ascontiguousarray(a)
+        b = cls(a.nbytes)
+        b.upload(a)
+        return b
+
+    def upload(self, a):
+        a = np.ascontiguousarray(a)
+        assert a.nbytes <= self.nbytes
+        _lib.call("emida_gb_memcpy_h2d", self.ptr, _ptr(a), a.nbytes)
+
+    def download(self, dtype, shape):
+        out = np.empty(shape, dtype=dtype)
+        _lib.call("emida_gb_memcpy_d2h", _ptr(out), self.ptr, out.nbytes)
+        return out
+
+    def zero(self):
+        _lib.call("emida_gb_memset", self.ptr, 0, self.nbytes)
+
+    def free(self):
+        if self.ptr is not None and self.ptr.value:
+            _lib.lib().emida_gb_free(self.ptr)
+        self.ptr = None
+
+    def __del__(self):
+        try:
+            self.free()
+        except Exception:
+            pass
+
+
+class GpuOffset:
+    """gpu_offset<T, IN> (src/gpu_offset.hpp:48-326).
+
+    src_size, slice_size, cross_size: (x, y) pairs; begins: ROI top-left (x, y)
+    pairs; T is `precision` ("double" | "float"), IN is `in_dtype`
+    (np.uint16 | np.float64).  `mode` selects the staged ("plain") or the fused
+    form; "auto" takes the fused kernel where one covers the shape.
+    """
+
+    def __init__(self, src_size, begins, slice_size, cross_size, batch_size,
+                 policy=CROSS_POLICY_BRUTE, s=3, in_buffers_size=1, precision="double",
+                 in_dtype=np.uint16, mode="auto"):
+        self.src_size = tuple(int(v) for v in src_size)
+        self.begins = np.ascontiguousarray(np.asarray(begins, dtype=np.uint32).reshape(-1, 2))
+        self.slice_size = tuple(int(v) for v in slice_size)
+        self.policy = _policy(policy)
+        if self.policy == FFT:
+            cross_size = (2 * self.slice_size[0] - 1, 2 * self.slice_size[1] - 1)
+        self.cross_size = tuple(int(v) for v in cross_size)
+        self.batch_size = int(batch_size)
+        self.s = int(s)
+        self.precision = _precision(precision)
+        self.T = np.float64 if self.precision == DOUBLE else np.float32
+        self.in_dtype = np.dtype(in_dtype)
+        if self.in_dtype not in (np.dtype(np.uint16), np.dtype(np.float64)):
+            raise ValueError("IN must be uint16 or float64")
+        self.total_slices = len(self.begins) * self.batch_size
+        self.neigh_size = self.s * self.s * self.total_slices
+        self.data_index = DATA_INDEX_F64 if self.precision == DOUBLE else DATA_INDEX_F32
+        p = _lib.Params()
+        p.src_w, p.src_h = self.src_size
+        p.begins = self.begins.ctypes.data_as(ctypes.POINTER(ctypes.c_uint32))
+        p.n_rois = len(self.begins)
+        p.slice_w, p.slice_h = self.slice_size
+        p.cross_w, p.cross_h = self.cross_size
+        p.batch_size = self.batch_size
+        p.policy = self.policy
+        p.precision = self.precision
+        p.fitsize = self.s
+        p.in_type = IN_U16 if self.in_dtype == np.dtype(np.uint16) else IN_F64
+        p.mode = _mode(mode)
+        p.in_buffers = int(in_buffers_size)
+        h = ctypes.c_void_p()
+        _lib.call("emida_gb_create", ctypes.byref(p), ctypes.byref(h))
+        self._h = h
+        self._pinned = []
+
+    @property
+    def handle(self):
+        return self._h
+
+    @property
+    def mode(self):
+        return {MODE_PLAIN: "plain", MODE_FUSED: "fused"}[_lib.lib().emida_gb_resolved_mode(self._h)]
+
+    def allocate_memory(self, temp=None):
+        """src/gpu_offset.hpp:127-211: buffers exist from construction; with a
+        reference pattern, prepares and transforms its ROIs once."""
+        if temp is None:
+            return
+        temp = np.ascontiguousarray(temp, dtype=self.in_dtype)
+        assert temp.size == self.src_size[0] * self.src_size[1]
+        _lib.call("emida_gb_set_reference", self._h, _ptr(temp))
+
+    def transfer_pic_to_device_async(self, pic):
+        """src/gpu_offset.hpp:213-218.  Keeps `pic` alive until the next call on
+        the same buffer; returns the buffer index."""
+        pic = np.ascontiguousarray(pic, dtype=self.in_dtype)
+        idx = ctypes.c_uint32()
+        _lib.call("emida_gb_transfer_async", self._h, _ptr(pic), ctypes.byref(idx))
+        self._pinned.append(pic)
+        if len(self._pinned) > 64:
+            self._pinned.pop(0)
+        return idx.value
+
+    def get_offset_core(self, cu_pic_index=0):
+        """src/gpu_offset.hpp:234-278: returns (maxes_i, neighbors) host arrays,
+        valid after finalize() (which waits for the output stream)."""
+        maxes = np.zeros(self.total_slices, dtype=self.data_index)
+        neigh = np.zeros(self.neigh_size, dtype=self.T)
+        _lib.call("emida_gb_offsets_core", self._h, int(cu_pic_index), _ptr(maxes), _ptr(neigh))
+        self._pinned.append((maxes, neigh))
+        return maxes, neigh
+
+    def finalize(self, maxes_i, neighbors):
+        """src/gpu_offset.hpp:280-301: (offsets [n][2], coefs [n][6])."""
+        offs = np.zeros((self.total_slices, 2))
+        coefs = np.zeros((self.total_slices, 6))
+        _lib.call("emida_gb_finalize", self._h, _ptr(maxes_i), _ptr(neighbors), _dptr(offs),
+                  _dptr(coefs))
+        return offs, coefs
+
+    def get_offset(self, pic, with_peaks=False):
+        """src/gpu_offset.hpp:220-231, with the fit on the device."""
+        pic = np.ascontiguousarray(pic, dtype=self.in_dtype)
+        assert pic.size == self.src_size[0] * self.src_size[1] * self.batch_size
+        offs = np.zeros((self.total_slices, 2))
+        coefs = np.zeros((self.total_slices, 6))
+        peaks = np.zeros(self.total_slices, dtype=np.uint32)
+        _lib.call("emida_gb_get_offset", self._h, _ptr(pic), _dptr(offs), _dptr(coefs),
+                  peaks.ctypes.data_as(ctypes.POINTER(ctypes.c_uint32)))
+        if with_peaks:
+            return offs, coefs, peaks
+        return offs, coefs
+
+    def run_device(self, dev_pics, patterns, dev_offsets, dev_coefs=None, dev_maxes=None,
+                   dev_neigh=None, stream=None):
+        """Device-resident form: any number of patterns, no synchronisation."""
+        def vp(b):
+            return None if b is None else (b.ptr if isinstance(b, DeviceBuffer) else ctypes.c_void_p(b))
+        _lib.call("emida_gb_run_device", self._h, vp(dev_pics), int(patterns), vp(dev_offsets),
+                  vp(dev_coefs), vp(dev_maxes), vp(dev_neigh),
+                  None if stream is None else ctypes.c_void_p(stream))
+
+    def time_device(self, dev_pics, patterns, dev_offsets, repeats):
+        ms = ctypes.c_float()
+        _lib.call("emida_gb_time_device", self._h, dev_pics.ptr, int(patterns), dev_offsets.ptr,
+                  int(repeats), ctypes.byref(ms))
+        return ms.value
+
+    def stream(self):
+        return _lib.lib().emida_gb_stream(self._h)
+
+    def launches_per_run(self):
+        return _lib.lib().emida_gb_launches_per_run(self._h)
+
+    def close(self):
+        if getattr(self, "_h", None) is not None and self._h.value:
+            _lib.lib().emida_gb_destroy(self._h)
+        self._h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+
+def get_offset(pic, temp, size, cross_size=None, c_policy=CROSS_POLICY_BRUTE, precision="double"):
+    """src/get_offset.hpp:7-20: offsets of one ROI pair (the whole of `pic`
+    against the whole of `temp`, both `size`), as gpu_offset<T, T> does."""
+    pic = np.ascontiguousarray(pic, dtype=np.float64)
+    temp = np.ascontiguousarray(temp, dtype=np.float64)
+    size = tuple(int(v) for v in size)
+    if cross_size is None:
+        cross_size = (2 * size[0] - 1, 2 * size[1] - 1)
+    g = GpuOffset(size, [(0, 0)], size, cross_size, 1, c_policy, 3, 1, precision, np.float64)
+    try:
+        g.allocate_memory(temp)
+        offs, _ = g.get_offset(pic)
+    finally:
+        g.close()
+    return offs
+
+
+def lstsq_matrix(s):
+    out = np.zeros(6 * s * s)
+    _lib.call("emida_gb_lstsq_matrix", int(s), _dptr(out))
+    return out.reshape(6, s * s)
+
+
+def subpixel_max(neigh, s):
+    """subpixel_max_serial (src/subpixel_max.hpp:76-97) on the host."""
+    neigh = np.ascontiguousarray(neigh, dtype=np.float64).reshape(-1, s * s)
+    sub = np.zeros((len(neigh), 2))
+    coefs = np.zeros((len(neigh), 6))
+    _lib.call("emida_gb_subpixel_max", _dptr(neigh), int(s), len(neigh), _dptr(sub), _dptr(coefs))
+    return sub, coefs
+
+
+def device_count():
+    n = ctypes.c_int()
+    st = _lib.lib().emida_gb_device_count(ctypes.byref(n))
+    return n.value if st == 0 else 0

@@ -1,0 +1,828 @@
+// capi.cu -- the C ABI (include/emida_gb.h): a handle that owns the device
+// buffers, streams and resident reference spectra of one ROI layout, the
+// host-side pieces of the reference's gpu_offset (src/gpu_offset.hpp:48-326),
+// and the per-stage launch exports.
+#include <cuda.h>
+
+#include <atomic>
+#include <cmath>
+#include <cstdarg>
+#include <cstring>
+#include <mutex>
+#include <string>
+#include <vector>
+
+#include "../../include/emida_gb.h"
+#include "fft.cuh"
+#include "fused.cuh"
+#include "staged.cuh"
+
+using namespace emida_gb;
+
+namespace {
+
+thread_local std::string g_last_error;
+
+int fail(int code, const char *fmt, ...)
+{
+    char buf[512];
+    va_list ap;
+    va_start(ap, fmt);
+    vsnprintf(buf, sizeof buf, fmt, ap);
+    va_end(ap);
+    g_last_error = buf;
+    return code;
+}
+
+#define CK(expr)                                                                            \
+    do {                                                                                    \
+        cudaError_t e_ = (expr);                                                            \
+        if (e_ != cudaSuccess)                                                              \
+            return fail(e_ == cudaErrorMemoryAllocation ? EMIDA_GB_OUT_OF_MEMORY             \
+                                                        : EMIDA_GB_CUDA_ERROR,               \
+                        "CUDA error %d (%s) at %s:%d: %s", (int)e_, cudaGetErrorString(e_),  \
+                        __FILE__, __LINE__, #expr);                                         \
+    } while (0)
+
+#define CKS(expr)                                                                           \
+    do {                                                                                    \
+        int s_ = (expr);                                                                    \
+        if (s_ != EMIDA_GB_OK) return s_;                                                   \
+    } while (0)
+
+// ---- exact least-squares matrix ---------------------------------------------
+// (A^T A)^-1 A^T for A rows (1, x, y, x^2, xy, y^2), x fastest
+// (src/subpixel_max.hpp:42-67): Gauss-Jordan over exact rationals, one
+// rounding per entry, which gives the same doubles as the reference's
+// tables of src/subpixel_max.cpp:22-58.
+struct q128 {
+    __int128 n, d;
+};
+__int128 gcd_i(__int128 a, __int128 b)
+{
+    if (a < 0) a = -a;
+    if (b < 0) b = -b;
+    while (b != 0) {
+        __int128 r = a % b;
+        a = b;
+        b = r;
+    }
+    return a;
+}
+q128 q_make(__int128 n, __int128 d)
+{
+    if (d < 0) {
+        n = -n;
+        d = -d;
+    }
+    __int128 g = gcd_i(n, d);
+    if (g > 1) {
+        n /= g;
+        d /= g;
+    }
+    return q128{n, d};
+}
+q128 q_mul(q128 a, q128 b)
+{
+    q128 x = q_make(a.n, b.d), y = q_make(b.n, a.d);
+    return q_make(x.n * y.n, x.d * y.d);
+}
+q128 q_sub(q128 a, q128 b) { return q_make(a.n * b.d - b.n * a.d, a.d * b.d); }
+q128 q_div(q128 a, q128 b) { return q_mul(a, q_make(b.d, b.n)); }
+
+int lstsq_matrix(int s, double *out)
+{
+    if (s != 3 && s != 5 && s != 7 && s != 9) return -1;
+    const int np = s * s, cols = 6 + np;
+    std::vector<q128> M(6 * cols);
+    auto at = [&](int r, int c) -> q128 & { return M[r * cols + c]; };
+    auto feat = [&](int k, int f) -> long long {
+        const long long x = k % s, y = k / s;
+        const long long v[6] = {1, x, y, x * x, x * y, y * y};
+        return v[f];
+    };
+    for (int i = 0; i < 6; ++i) {
+        for (int j = 0; j < 6; ++j) {
+            long long acc = 0;
+            for (int k = 0; k < np; ++k) acc += feat(k, i) * feat(k, j);
+            at(i, j) = q_make(acc, 1);
+        }
+        for (int k = 0; k < np; ++k) at(i, 6 + k) = q_make(feat(k, i), 1);
+    }
+    for (int c = 0; c < 6; ++c) {
+        int piv = c;
+        while (piv < 6 && at(piv, c).n == 0) ++piv;
+        if (piv == 6) return -1;
+        if (piv != c)
+            for (int j = 0; j < cols; ++j) std::swap(at(c, j), at(piv, j));
+        const q128 p = at(c, c);
+        for (int j = 0; j < cols; ++j) at(c, j) = q_div(at(c, j), p);
+        for (int i = 0; i < 6; ++i) {
+            if (i == c || at(i, c).n == 0) continue;
+            const q128 f = at(i, c);
+            for (int j = 0; j < cols; ++j) at(i, j) = q_sub(at(i, j), q_mul(f, at(c, j)));
+        }
+    }
+    for (int i = 0; i < 6; ++i)
+        for (int k = 0; k < np; ++k) out[i * np + k] = (double)at(i, 6 + k).n / (double)at(i, 6 + k).d;
+    return 0;
+}
+
+// Host fit in the reference's operation order (src/subpixel_max.hpp:14-29, :76-97).
+// This file is built with -ffp-contract=off, so each product and sum rounds once.
+void host_fit(const double *mat, const double *v, int s, double *coef, double &x, double &y)
+{
+    const int np = s * s;
+    for (int j = 0; j < 6; ++j) {
+        double acc = 0;
+        for (int k = 0; k < np; ++k) acc += mat[j * np + k] * v[k];
+        coef[j] = acc;
+    }
+    const double b = coef[1], c = coef[2], d = coef[3], e = coef[4], f = coef[5];
+    y = (b * e - 2 * c * d) / (4 * f * d - e * e);
+    x = (-e * y - b) / (2 * d);
+}
+
+// cuTensorMapEncodeTiled through the runtime's driver entry point (no libcuda link).
+using encode_fn = CUresult (*)(CUtensorMap *, CUtensorMapDataType, cuuint32_t, void *,
+                               const cuuint64_t *, const cuuint64_t *, const cuuint32_t *,
+                               const cuuint32_t *, CUtensorMapInterleave, CUtensorMapSwizzle,
+                               CUtensorMapL2promotion, CUtensorMapFloatOOBfill);
+encode_fn get_encoder()
+{
+    static encode_fn fn = nullptr;
+    static std::once_flag once;
+    std::call_once(once, [] {
+        void *p = nullptr;
+        cudaDriverEntryPointQueryResult q;
+        if (cudaGetDriverEntryPointByVersion("cuTensorMapEncodeTiled", &p, 12000, cudaEnableDefault,
+                                             &q) == cudaSuccess &&
+            q == cudaDriverEntryPointSuccess)
+            fn = reinterpret_cast<encode_fn>(p);
+    });
+    return fn;
+}
+
+}  // namespace
+
+struct emida_gb_handle {
+    emida_gb_params p{};
+    std::vector<uint32_t> begins;
+    int device = 0;
+    bool dbl = false, in_f64 = false, fft = false;
+    int mode = EMIDA_GB_MODE_PLAIN;
+    size2 src{}, slice{}, cross{};
+    uint32_t S = 0, B = 0, N = 0;
+    uint32_t w2 = 0, h2 = 0, half = 0;
+    size_t in_elem = 2, t_elem = 4, c_elem = 8, di_elem = 8;
+    cudaStream_t in_stream = nullptr, out_stream = nullptr, comp = nullptr;
+    std::vector<cudaEvent_t> in_done;
+    cudaEvent_t comp_done = nullptr;
+    std::vector<void *> d_in;
+    std::atomic<uint32_t> in_next{0};
+    void *d_ref_in = nullptr;
+    uint2 *d_begins = nullptr;
+    void *d_hann = nullptr, *d_hann_fused = nullptr;
+    void *d_sums_ref = nullptr, *d_sums = nullptr;
+    void *d_ref_prep = nullptr, *d_prep = nullptr;
+    void *d_ref_spec = nullptr, *d_ref_spec_cm = nullptr, *d_spec = nullptr;
+    void *d_map = nullptr, *d_maxes = nullptr, *d_neigh = nullptr;
+    double *d_offsets = nullptr, *d_coefs = nullptr, *d_lstsq = nullptr;
+    void *d_tw_row = nullptr, *d_tw_col = nullptr;
+    uint32_t *d_err = nullptr;
+    std::vector<double> lstsq;
+    bool ref_set = false;
+    std::mutex mu;
+    std::vector<void *> allocs;
+
+    int alloc(void **ptr, size_t bytes, bool zero = false)
+    {
+        if (bytes == 0) bytes = 16;
+        CK(cudaMalloc(ptr, bytes));
+        allocs.push_back(*ptr);
+        if (zero) CK(cudaMemset(*ptr, 0, bytes));
+        return EMIDA_GB_OK;
+    }
+    uint32_t map_size() const { return fft ? w2 * h2 : cross.x * cross.y; }
+    size2 prep_size() const { return fft ? size2{w2, h2} : slice; }
+};
+
+namespace {
+
+template <typename T> std::vector<T> hann_host(uint32_t n)
+{
+    // src/host_helpers.hpp:29-37: FP64 formula, cast to T
+    const double PI = 3.14159265358979323846;
+    std::vector<T> v(n);
+    for (uint32_t i = 0; i < n; ++i) v[i] = (T)(0.5 * (1 - std::cos(2 * PI * i / (double)(n - 1))));
+    return v;
+}
+
+int upload_hann(emida_gb_handle *h, void **dst, uint32_t nx, uint32_t ny)
+{
+    if (h->dbl) {
+        auto x = hann_host<double>(nx), y = hann_host<double>(ny);
+        x.insert(x.end(), y.begin(), y.end());
+        CKS(h->alloc(dst, x.size() * sizeof(double)));
+        CK(cudaMemcpy(*dst, x.data(), x.size() * sizeof(double), cudaMemcpyHostToDevice));
+    } else {
+        auto x = hann_host<float>(nx), y = hann_host<float>(ny);
+        x.insert(x.end(), y.begin(), y.end());
+        CKS(h->alloc(dst, x.size() * sizeof(float)));
+        CK(cudaMemcpy(*dst, x.data(), x.size() * sizeof(float), cudaMemcpyHostToDevice));
+    }
+    return EMIDA_GB_OK;
+}
+
+int upload_twiddles(emida_gb_handle *h, void **dst, uint32_t n)
+{
+    const double PI = 3.14159265358979323846;
+    if (h->dbl) {
+        std::vector<double2> w(n);
+        for (uint32_t j = 0; j < n; ++j)
+            w[j] = make_double2(std::cos(2 * PI * j / n), -std::sin(2 * PI * j / n));
+        CKS(h->alloc(dst, n * sizeof(double2)));
+        CK(cudaMemcpy(*dst, w.data(), n * sizeof(double2), cudaMemcpyHostToDevice));
+    } else {
+        std::vector<float2> w(n);
+        for (uint32_t j = 0; j < n; ++j)
+            w[j] = make_float2((float)std::cos(2 * PI * j / n), (float)-std::sin(2 * PI * j / n));
+        CKS(h->alloc(dst, n * sizeof(float2)));
+        CK(cudaMemcpy(*dst, w.data(), n * sizeof(float2), cudaMemcpyHostToDevice));
+    }
+    return EMIDA_GB_OK;
+}
+
+fft_tables tables(const emida_gb_handle *h) { return fft_tables{h->d_tw_row, h->d_tw_col, h->w2, h->h2}; }
+
+// The staged pipeline for `pats` patterns from `pics` (<= B patterns):
+// src/gpu_offset.hpp:234-278 stage by stage.
+int run_plain_chunk(emida_gb_handle *h, const void *pics, uint32_t pats, void *maxes, void *neigh,
+                    double *offsets, double *coefs, cudaStream_t st)
+{
+    const uint32_t n = pats * h->S;
+    const int pol = h->fft ? POLICY_FFT : POLICY_BRUTE;
+    CK(run_sums(pics, h->in_f64 ? IN_F64 : IN_U16, h->src, h->d_begins, h->S, h->slice, pats,
+                h->d_sums, st));
+    CK(run_prepare(pics, h->in_f64 ? IN_F64 : IN_U16, h->dbl, h->d_prep, h->d_hann, h->d_sums,
+                   h->d_begins, h->src, h->slice, h->prep_size(), h->S, pats, st));
+    if (h->fft) {
+        CK(run_fft_r2c(h->d_prep, h->d_spec, n, tables(h), h->dbl, st));
+        CK(run_hadamard(h->d_spec, h->d_ref_spec, h->h2 * h->half, h->S, pats, h->dbl, st));
+        CK(run_fft_c2r(h->d_spec, h->d_map, n, tables(h), h->dbl, st));
+    } else {
+        CK(run_cross_corr(h->d_prep, h->d_ref_prep, h->d_map, h->dbl, h->slice, h->cross, h->S,
+                          pats, st));
+    }
+    void *mx = maxes ? maxes : h->d_maxes;
+    void *nb = neigh ? neigh : h->d_neigh;
+    CK(run_maxarg(h->d_map, h->map_size(), n, mx, h->dbl, st));
+    CK(run_extract_neighbors(h->d_map, mx, nb, h->p.fitsize, h->cross, n, pol, h->dbl, st));
+    if (offsets)
+        CK(run_fit(nb, mx, n, h->p.fitsize, h->cross, pol, h->d_lstsq, h->dbl, offsets, coefs, st));
+    return EMIDA_GB_OK;
+}
+
+int run_fused(emida_gb_handle *h, const void *pics, uint32_t pats, void *maxes, void *neigh,
+              double *offsets, double *coefs, cudaStream_t st)
+{
+    fused_args a{};
+    a.pics = pics;
+    a.src_w = h->src.x;
+    a.src_h = h->src.y;
+    a.begins = h->d_begins;
+    a.n_rois = h->S;
+    a.n_pairs = pats * h->S;
+    a.ref_spec = h->d_ref_spec_cm;
+    a.hann = h->d_hann_fused;
+    a.twiddles = h->d_tw_row;
+    a.lstsq = h->d_lstsq;
+    a.fitsize = h->p.fitsize;
+    a.offsets = offsets;
+    a.coefs = coefs;
+    a.maxes = maxes;
+    a.neigh = neigh;
+    a.err = h->d_err;
+    CUtensorMap map;
+    std::memset(&map, 0, sizeof map);
+    a.use_tma = 0;
+    if (!h->in_f64 && (h->src.x % 8) == 0 && ((uintptr_t)pics % 16) == 0) {
+        if (encode_fn enc = get_encoder()) {
+            const cuuint64_t dims[3] = {h->src.x, h->src.y, pats};
+            const cuuint64_t strides[2] = {(cuuint64_t)h->src.x * 2,
+                                           (cuuint64_t)h->src.x * h->src.y * 2};
+            const cuuint32_t box[3] = {h->slice.x + 8, h->slice.y, 1};
+            const cuuint32_t estr[3] = {1, 1, 1};
+            if (enc(&map, CU_TENSOR_MAP_DATA_TYPE_UINT16, 3, const_cast<void *>(pics), dims,
+                    strides, box, estr, CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_NONE,
+                    CU_TENSOR_MAP_L2_PROMOTION_L2_128B,
+                    CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE) == CUDA_SUCCESS)
+                a.use_tma = 1;
+        }
+    }
+    CK(launch_fused(h->w2, h->dbl, h->in_f64, a, &map, 0, st));
+    return EMIDA_GB_OK;
+}
+
+int run_any(emida_gb_handle *h, const void *pics, uint32_t pats, void *maxes, void *neigh,
+            double *offsets, double *coefs, cudaStream_t st)
+{
+    if (h->mode == EMIDA_GB_MODE_FUSED) return run_fused(h, pics, pats, maxes, neigh, offsets, coefs, st);
+    const size_t pat_bytes = (size_t)h->src.x * h->src.y * h->in_elem;
+    const size_t s2 = (size_t)h->p.fitsize * h->p.fitsize;
+    for (uint32_t done = 0; done < pats; done += h->B) {
+        const uint32_t c = pats - done < h->B ? pats - done : h->B;
+        const size_t r0 = (size_t)done * h->S;
+        CKS(run_plain_chunk(h, (const char *)pics + done * pat_bytes, c,
+                            maxes ? (char *)maxes + r0 * h->di_elem : nullptr,
+                            neigh ? (char *)neigh + r0 * s2 * h->t_elem : nullptr,
+                            offsets ? offsets + 2 * r0 : nullptr, coefs ? coefs + 6 * r0 : nullptr,
+                            st));
+    }
+    return EMIDA_GB_OK;
+}
+
+int check_device_error(emida_gb_handle *h)
+{
+    uint32_t err = 0;
+    CK(cudaMemcpy(&err, h->d_err, sizeof err, cudaMemcpyDeviceToHost));
+    if (err) {
+        CK(cudaMemset(h->d_err, 0, sizeof err));
+        return fail(EMIDA_GB_DEVICE_CHECK, "device check failed (flags 0x%x%s)", err,
+                    (err & DEV_ERR_TMA_TIMEOUT) ? ": TMA wait ran out" : "");
+    }
+    return EMIDA_GB_OK;
+}
+
+int validate(const emida_gb_params *p)
+{
+    if (!p) return fail(EMIDA_GB_INVALID_ARGUMENT, "null parameters");
+    if (p->src_w == 0 || p->src_h == 0) return fail(EMIDA_GB_INVALID_ARGUMENT, "empty pattern size");
+    if (p->n_rois == 0 || !p->begins) return fail(EMIDA_GB_INVALID_ARGUMENT, "no ROIs");
+    if (p->slice_w < 2 || p->slice_h < 2) return fail(EMIDA_GB_INVALID_ARGUMENT, "ROI smaller than 2x2");
+    if (p->batch_size == 0) return fail(EMIDA_GB_INVALID_ARGUMENT, "batchsize must be greater than 0");
+    if (p->policy != EMIDA_GB_BRUTE && p->policy != EMIDA_GB_FFT)
+        return fail(EMIDA_GB_INVALID_ARGUMENT, "invalid cross policy %d", p->policy);
+    if (p->precision != EMIDA_GB_DOUBLE && p->precision != EMIDA_GB_FLOAT)
+        return fail(EMIDA_GB_INVALID_ARGUMENT, "invalid precision %d", p->precision);
+    if (p->fitsize != 3 && p->fitsize != 5 && p->fitsize != 7 && p->fitsize != 9)
+        return fail(EMIDA_GB_INVALID_ARGUMENT, "Wrong fitting size.");
+    if (p->in_type != EMIDA_GB_IN_U16 && p->in_type != EMIDA_GB_IN_F64)
+        return fail(EMIDA_GB_INVALID_ARGUMENT, "invalid input type %d", p->in_type);
+    for (uint32_t r = 0; r < p->n_rois; ++r)
+        if ((uint64_t)p->begins[2 * r] + p->slice_w > p->src_w ||
+            (uint64_t)p->begins[2 * r + 1] + p->slice_h > p->src_h)
+            return fail(EMIDA_GB_INVALID_ARGUMENT, "A slice out of bounds (ROI %u)", r);
+    if (p->policy == EMIDA_GB_BRUTE) {
+        if (p->cross_w == 0 || p->cross_h == 0 || p->cross_w > 2 * p->slice_w - 1 ||
+            p->cross_h > 2 * p->slice_h - 1)
+            return fail(EMIDA_GB_INVALID_ARGUMENT,
+                        "cross size must be lesser or equal to slice_size * 2 - 1");
+    } else if (p->slice_w != p->slice_h) {
+        return fail(EMIDA_GB_UNSUPPORTED, "the FFT policy needs square ROIs");
+    }
+    return EMIDA_GB_OK;
+}
+
+}  // namespace
+
+extern "C" {
+
+const char *emida_gb_last_error(void) { return g_last_error.c_str(); }
+const char *emida_gb_version(void) { return "emida-gb300 0.1 (sm_103a)"; }
+
+int emida_gb_lstsq_matrix(int s, double *out)
+{
+    if (!out || lstsq_matrix(s, out) != 0) return fail(EMIDA_GB_INVALID_ARGUMENT, "Wrong fitting size.");
+    return EMIDA_GB_OK;
+}
+
+int emida_gb_subpixel_max(const double *neigh, int s, uint32_t n, double *sub, double *coefs)
+{
+    double mat[6 * 81];
+    if (lstsq_matrix(s, mat) != 0) return fail(EMIDA_GB_INVALID_ARGUMENT, "Wrong fitting size.");
+    for (uint32_t i = 0; i < n; ++i) {
+        double c[6], x, y;
+        host_fit(mat, neigh + (size_t)i * s * s, s, c, x, y);
+        sub[2 * i] = x;
+        sub[2 * i + 1] = y;
+        if (coefs) std::memcpy(coefs + 6 * (size_t)i, c, sizeof c);
+    }
+    return EMIDA_GB_OK;
+}
+
+int emida_gb_create(const emida_gb_params *p, emida_gb_handle **out)
+{
+    if (!out) return fail(EMIDA_GB_INVALID_ARGUMENT, "null output handle");
+    *out = nullptr;
+    CKS(validate(p));
+    auto *h = new emida_gb_handle();
+    h->p = *p;
+    h->begins.assign(p->begins, p->begins + 2 * (size_t)p->n_rois);
+    h->p.begins = h->begins.data();
+    if (h->p.in_buffers == 0) h->p.in_buffers = 1;
+    h->dbl = p->precision == EMIDA_GB_DOUBLE;
+    h->in_f64 = p->in_type == EMIDA_GB_IN_F64;
+    h->fft = p->policy == EMIDA_GB_FFT;
+    h->src = size2{p->src_w, p->src_h};
+    h->slice = size2{p->slice_w, p->slice_h};
+    h->S = p->n_rois;
+    h->B = p->batch_size;
+    h->N = h->S * h->B;
+    h->in_elem = h->in_f64 ? 8 : 2;
+    h->t_elem = h->dbl ? 8 : 4;
+    h->c_elem = 2 * h->t_elem;
+    h->di_elem = h->dbl ? sizeof(data_index<double>) : sizeof(data_index<float>);
+    if (h->fft) {
+        h->w2 = 2 * p->slice_w;
+        h->h2 = 2 * p->slice_h;
+        h->half = h->w2 / 2 + 1;
+        h->cross = size2{2 * p->slice_w - 1, 2 * p->slice_h - 1};
+    } else {
+        h->cross = size2{p->cross_w, p->cross_h};
+    }
+    const bool fusable = h->fft && fused_supported(h->w2);
+    if (p->mode == EMIDA_GB_MODE_FUSED && !fusable) {
+        delete h;
+        return fail(EMIDA_GB_UNSUPPORTED, "no fused kernel for this shape (FFT policy, 32x32 or 64x64 ROIs)");
+    }
+    h->mode = (p->mode == EMIDA_GB_MODE_PLAIN || !fusable) ? EMIDA_GB_MODE_PLAIN : EMIDA_GB_MODE_FUSED;
+
+    auto bail = [&](int st) {
+        emida_gb_destroy(h);
+        return st;
+    };
+    int st;
+#define TRY(expr)                                                                           \
+    if ((st = (expr)) != EMIDA_GB_OK) return bail(st);
+    TRY([&]() -> int { CK(cudaGetDevice(&h->device)); return EMIDA_GB_OK; }());
+    TRY([&]() -> int {
+        CK(cudaStreamCreateWithFlags(&h->in_stream, cudaStreamNonBlocking));
+        CK(cudaStreamCreateWithFlags(&h->out_stream, cudaStreamNonBlocking));
+        CK(cudaStreamCreateWithFlags(&h->comp, cudaStreamNonBlocking));
+        CK(cudaEventCreateWithFlags(&h->comp_done, cudaEventDisableTiming));
+        h->in_done.resize(h->p.in_buffers);
+        for (auto &e : h->in_done) CK(cudaEventCreateWithFlags(&e, cudaEventDisableTiming));
+        return EMIDA_GB_OK;
+    }());
+    const size_t pat_bytes = (size_t)h->src.x * h->src.y * h->in_elem;
+    h->d_in.resize(h->p.in_buffers);
+    for (auto &b : h->d_in) TRY(h->alloc(&b, pat_bytes * h->B));
+    TRY(h->alloc(&h->d_ref_in, pat_bytes));
+    TRY(h->alloc((void **)&h->d_begins, sizeof(uint2) * h->S));
+    TRY([&]() -> int {
+        CK(cudaMemcpy(h->d_begins, h->begins.data(), sizeof(uint2) * h->S, cudaMemcpyHostToDevice));
+        return EMIDA_GB_OK;
+    }());
+    TRY(upload_hann(h, &h->d_hann, h->slice.x, h->slice.y));
+    const size_t sum_elem = h->in_f64 ? 8 : 4;
+    TRY(h->alloc(&h->d_sums_ref, sum_elem * h->S));
+    TRY(h->alloc((void **)&h->d_err, sizeof(uint32_t), true));
+    h->lstsq.resize(6 * (size_t)p->fitsize * p->fitsize);
+    lstsq_matrix(p->fitsize, h->lstsq.data());
+    TRY(h->alloc((void **)&h->d_lstsq, h->lstsq.size() * sizeof(double)));
+    TRY([&]() -> int {
+        CK(cudaMemcpy(h->d_lstsq, h->lstsq.data(), h->lstsq.size() * sizeof(double),
+                      cudaMemcpyHostToDevice));
+        return EMIDA_GB_OK;
+    }());
+    const size2 ps = h->prep_size();
+    TRY(h->alloc(&h->d_ref_prep, (size_t)ps.x * ps.y * h->S * h->t_elem, true));
+    if (h->fft) {
+        TRY(upload_twiddles(h, &h->d_tw_row, h->w2));
+        TRY(upload_twiddles(h, &h->d_tw_col, h->h2));
+        TRY(h->alloc(&h->d_ref_spec, (size_t)h->h2 * h->half * h->S * h->c_elem));
+    }
+    const size_t s2 = (size_t)p->fitsize * p->fitsize;
+    if (h->mode == EMIDA_GB_MODE_FUSED) {
+        TRY(upload_hann(h, &h->d_hann_fused, h->slice.x, h->slice.y));
+        TRY(h->alloc(&h->d_ref_spec_cm, (size_t)h->h2 * h->half * h->S * h->c_elem));
+    } else {
+        TRY(h->alloc(&h->d_sums, sum_elem * h->N));
+        TRY(h->alloc(&h->d_prep, (size_t)ps.x * ps.y * h->N * h->t_elem, true));
+        TRY(h->alloc(&h->d_map, (size_t)h->map_size() * h->N * h->t_elem));
+        if (h->fft) TRY(h->alloc(&h->d_spec, (size_t)h->h2 * h->half * h->N * h->c_elem));
+    }
+    TRY(h->alloc(&h->d_maxes, h->di_elem * h->N));
+    TRY(h->alloc(&h->d_neigh, s2 * h->N * h->t_elem));
+    TRY(h->alloc((void **)&h->d_offsets, 2 * sizeof(double) * h->N));
+    TRY(h->alloc((void **)&h->d_coefs, 6 * sizeof(double) * h->N));
+#undef TRY
+    *out = h;
+    return EMIDA_GB_OK;
+}
+
+int emida_gb_set_reference(emida_gb_handle *h, const void *ref)
+{
+    if (!h || !ref) return fail(EMIDA_GB_INVALID_ARGUMENT, "null argument");
+    std::lock_guard<std::mutex> lk(h->mu);
+    const size_t pat_bytes = (size_t)h->src.x * h->src.y * h->in_elem;
+    CK(cudaMemcpyAsync(h->d_ref_in, ref, pat_bytes, cudaMemcpyHostToDevice, h->comp));
+    const int in_type = h->in_f64 ? IN_F64 : IN_U16;
+    CK(run_sums(h->d_ref_in, in_type, h->src, h->d_begins, h->S, h->slice, 1, h->d_sums_ref, h->comp));
+    CK(run_prepare(h->d_ref_in, in_type, h->dbl, h->d_ref_prep, h->d_hann, h->d_sums_ref,
+                   h->d_begins, h->src, h->slice, h->prep_size(), h->S, 1, h->comp));
+    if (h->fft) {
+        CK(run_fft_r2c(h->d_ref_prep, h->d_ref_spec, h->S, tables(h), h->dbl, h->comp));
+        if (h->d_ref_spec_cm)
+            CK(run_spec_to_colmajor(h->d_ref_spec, h->d_ref_spec_cm, h->S, h->w2, h->h2, h->dbl,
+                                    h->comp));
+    }
+    CK(cudaStreamSynchronize(h->comp));
+    h->ref_set = true;
+    return EMIDA_GB_OK;
+}
+
+int emida_gb_transfer_async(emida_gb_handle *h, const void *batch, uint32_t *buffer_index)
+{
+    if (!h || !batch) return fail(EMIDA_GB_INVALID_ARGUMENT, "null argument");
+    const uint32_t i = h->in_next.fetch_add(1) % (uint32_t)h->d_in.size();
+    const size_t bytes = (size_t)h->src.x * h->src.y * h->in_elem * h->B;
+    CK(cudaMemcpyAsync(h->d_in[i], batch, bytes, cudaMemcpyHostToDevice, h->in_stream));
+    CK(cudaEventRecord(h->in_done[i], h->in_stream));
+    if (buffer_index) *buffer_index = i;
+    return EMIDA_GB_OK;
+}
+
+int emida_gb_offsets_core(emida_gb_handle *h, uint32_t buffer_index, void *maxes_out,
+                          void *neigh_out)
+{
+    if (!h) return fail(EMIDA_GB_INVALID_ARGUMENT, "null handle");
+    if (buffer_index >= h->d_in.size()) return fail(EMIDA_GB_INVALID_ARGUMENT, "bad buffer index");
+    if (!h->ref_set) return fail(EMIDA_GB_INVALID_ARGUMENT, "reference pattern not set");
+    std::lock_guard<std::mutex> lk(h->mu);
+    CK(cudaStreamWaitEvent(h->comp, h->in_done[buffer_index], 0));
+    CKS(run_any(h, h->d_in[buffer_index], h->B, h->d_maxes, h->d_neigh, nullptr, nullptr, h->comp));
+    CK(cudaEventRecord(h->comp_done, h->comp));
+    CK(cudaStreamWaitEvent(h->out_stream, h->comp_done, 0));
+    const size_t s2 = (size_t)h->p.fitsize * h->p.fitsize;
+    if (maxes_out)
+        CK(cudaMemcpyAsync(maxes_out, h->d_maxes, h->di_elem * h->N, cudaMemcpyDeviceToHost, h->out_stream));
+    if (neigh_out)
+        CK(cudaMemcpyAsync(neigh_out, h->d_neigh, s2 * h->t_elem * h->N, cudaMemcpyDeviceToHost,
+                           h->out_stream));
+    return EMIDA_GB_OK;
+}
+
+int emida_gb_finalize(emida_gb_handle *h, const void *maxes, const void *neigh, double *offsets,
+                      double *coefs)
+{
+    if (!h || !maxes || !neigh || !offsets) return fail(EMIDA_GB_INVALID_ARGUMENT, "null argument");
+    CK(cudaStreamSynchronize(h->out_stream));
+    CKS(check_device_error(h));
+    const int s = h->p.fitsize, s2 = s * s, r = (s - 1) / 2;
+    std::vector<double> v(s2);
+    for (uint32_t i = 0; i < h->N; ++i) {
+        uint32_t index;
+        if (h->dbl) {
+            index = reinterpret_cast<const data_index<double> *>(maxes)[i].index;
+            for (int k = 0; k < s2; ++k) v[k] = reinterpret_cast<const double *>(neigh)[(size_t)i * s2 + k];
+        } else {
+            index = reinterpret_cast<const data_index<float> *>(maxes)[i].index;
+            for (int k = 0; k < s2; ++k) v[k] = (double)reinterpret_cast<const float *>(neigh)[(size_t)i * s2 + k];
+        }
+        double c[6], sx, sy;
+        host_fit(h->lstsq.data(), v.data(), s, c, sx, sy);
+        uint32_t mx, my;
+        if (h->fft) {
+            const uint32_t iw = h->cross.x + 1, ih = h->cross.y + 1;
+            mx = (index % iw + (iw - 1) / 2) % iw;
+            my = (index / iw + (ih - 1) / 2) % ih;
+        } else {
+            mx = index % h->cross.x;
+            my = index / h->cross.x;
+        }
+        offsets[2 * (size_t)i] = -((int)mx - ((int)h->cross.x / 2) - r + sx);
+        offsets[2 * (size_t)i + 1] = -((int)my - ((int)h->cross.y / 2) - r + sy);
+        if (coefs) std::memcpy(coefs + 6 * (size_t)i, c, sizeof c);
+    }
+    return EMIDA_GB_OK;
+}
+
+int emida_gb_get_offset(emida_gb_handle *h, const void *batch, double *offsets, double *coefs,
+                        uint32_t *peaks)
+{
+    if (!h || !batch || !offsets) return fail(EMIDA_GB_INVALID_ARGUMENT, "null argument");
+    if (!h->ref_set) return fail(EMIDA_GB_INVALID_ARGUMENT, "reference pattern not set");
+    std::lock_guard<std::mutex> lk(h->mu);
+    const size_t bytes = (size_t)h->src.x * h->src.y * h->in_elem * h->B;
+    CK(cudaMemcpyAsync(h->d_in[0], batch, bytes, cudaMemcpyHostToDevice, h->comp));
+    CKS(run_any(h, h->d_in[0], h->B, h->d_maxes, h->d_neigh, h->d_offsets, h->d_coefs, h->comp));
+    CK(cudaMemcpyAsync(offsets, h->d_offsets, 2 * sizeof(double) * h->N, cudaMemcpyDeviceToHost, h->comp));
+    if (coefs)
+        CK(cudaMemcpyAsync(coefs, h->d_coefs, 6 * sizeof(double) * h->N, cudaMemcpyDeviceToHost, h->comp));
+    std::vector<unsigned char> mx;
+    if (peaks) {
+        mx.resize(h->di_elem * h->N);
+        CK(cudaMemcpyAsync(mx.data(), h->d_maxes, mx.size(), cudaMemcpyDeviceToHost, h->comp));
+    }
+    CK(cudaStreamSynchronize(h->comp));
+    CKS(check_device_error(h));
+    if (peaks)
+        for (uint32_t i = 0; i < h->N; ++i)
+            peaks[i] = h->dbl ? reinterpret_cast<const data_index<double> *>(mx.data())[i].index
+                              : reinterpret_cast<const data_index<float> *>(mx.data())[i].index;
+    return EMIDA_GB_OK;
+}
+
+int emida_gb_run_device(emida_gb_handle *h, const void *dev_patterns, uint32_t patterns,
+                        double *dev_offsets, double *dev_coefs, void *dev_maxes, void *dev_neigh,
+                        void *stream)
+{
+    if (!h || !dev_patterns || !dev_offsets) return fail(EMIDA_GB_INVALID_ARGUMENT, "null argument");
+    if (!h->ref_set) return fail(EMIDA_GB_INVALID_ARGUMENT, "reference pattern not set");
+    cudaStream_t st = stream ? (cudaStream_t)stream : h->comp;
+    std::lock_guard<std::mutex> lk(h->mu);
+    return run_any(h, dev_patterns, patterns, dev_maxes, dev_neigh, dev_offsets, dev_coefs, st);
+}
+
+int emida_gb_time_device(emida_gb_handle *h, const void *dev_patterns, uint32_t patterns,
+                         double *dev_offsets, int repeats, float *ms)
+{
+    if (!h || !ms || repeats < 1) return fail(EMIDA_GB_INVALID_ARGUMENT, "bad argument");
+    cudaEvent_t a, b;
+    CK(cudaEventCreate(&a));
+    CK(cudaEventCreate(&b));
+    CK(cudaEventRecord(a, h->comp));
+    for (int i = 0; i < repeats; ++i)
+        CKS(emida_gb_run_device(h, dev_patterns, patterns, dev_offsets, nullptr, nullptr, nullptr, nullptr));
+    CK(cudaEventRecord(b, h->comp));
+    CK(cudaEventSynchronize(b));
+    CK(cudaEventElapsedTime(ms, a, b));
+    cudaEventDestroy(a);
+    cudaEventDestroy(b);
+    return check_device_error(h);
+}
+
+int emida_gb_resolved_mode(const emida_gb_handle *h) { return h ? h->mode : -1; }
+void *emida_gb_stream(emida_gb_handle *h) { return h ? (void *)h->comp : nullptr; }
+int emida_gb_launches_per_run(const emida_gb_handle *h)
+{
+    if (!h) return -1;
+    if (h->mode == EMIDA_GB_MODE_FUSED) return 1;
+    return h->fft ? 10 : 6;
+}
+
+void emida_gb_destroy(emida_gb_handle *h)
+{
+    if (!h) return;
+    if (h->comp) cudaStreamSynchronize(h->comp);
+    if (h->in_stream) cudaStreamSynchronize(h->in_stream);
+    if (h->out_stream) cudaStreamSynchronize(h->out_stream);
+    for (void *p : h->allocs) cudaFree(p);
+    for (auto e : h->in_done)
+        if (e) cudaEventDestroy(e);
+    if (h->comp_done) cudaEventDestroy(h->comp_done);
+    if (h->comp) cudaStreamDestroy(h->comp);
+    if (h->in_stream) cudaStreamDestroy(h->in_stream);
+    if (h->out_stream) cudaStreamDestroy(h->out_stream);
+    delete h;
+}
+
+// ---- memory helpers -----------------------------------------------------------
+int emida_gb_device_count(int *count)
+{
+    CK(cudaGetDeviceCount(count));
+    return EMIDA_GB_OK;
+}
+int emida_gb_malloc(void **p, size_t bytes)
+{
+    CK(cudaMalloc(p, bytes ? bytes : 16));
+    return EMIDA_GB_OK;
+}
+int emida_gb_free(void *p)
+{
+    CK(cudaFree(p));
+    return EMIDA_GB_OK;
+}
+int emida_gb_memset(void *p, int v, size_t bytes)
+{
+    CK(cudaMemset(p, v, bytes));
+    return EMIDA_GB_OK;
+}
+int emida_gb_memcpy_h2d(void *d, const void *s, size_t bytes)
+{
+    CK(cudaMemcpy(d, s, bytes, cudaMemcpyHostToDevice));
+    return EMIDA_GB_OK;
+}
+int emida_gb_memcpy_d2h(void *d, const void *s, size_t bytes)
+{
+    CK(cudaMemcpy(d, s, bytes, cudaMemcpyDeviceToHost));
+    return EMIDA_GB_OK;
+}
+int emida_gb_malloc_host(void **p, size_t bytes)
+{
+    CK(cudaMallocHost(p, bytes ? bytes : 16));
+    return EMIDA_GB_OK;
+}
+int emida_gb_free_host(void *p)
+{
+    CK(cudaFreeHost(p));
+    return EMIDA_GB_OK;
+}
+int emida_gb_synchronize(void)
+{
+    CK(cudaDeviceSynchronize());
+    return EMIDA_GB_OK;
+}
+
+// ---- per-stage launchers --------------------------------------------------------
+int emida_gb_run_sum(const void *pics, int in_type, uint32_t src_w, uint32_t src_h,
+                     const uint32_t *dev_begins, uint32_t n_rois, uint32_t slice_w,
+                     uint32_t slice_h, uint32_t batch, void *sums)
+{
+    CK(run_sums(pics, in_type, size2{src_w, src_h}, reinterpret_cast<const uint2 *>(dev_begins),
+                n_rois, size2{slice_w, slice_h}, batch, sums, 0));
+    CK(cudaDeviceSynchronize());
+    return EMIDA_GB_OK;
+}
+
+int emida_gb_run_prepare(const void *pics, int in_type, int precision, void *slices,
+                         const void *hann, const void *sums, const uint32_t *dev_begins,
+                         uint32_t src_w, uint32_t src_h, uint32_t slice_w, uint32_t slice_h,
+                         uint32_t out_w, uint32_t out_h, uint32_t n_rois, uint32_t batch)
+{
+    CK(run_prepare(pics, in_type, precision == EMIDA_GB_DOUBLE, slices, hann, sums,
+                   reinterpret_cast<const uint2 *>(dev_begins), size2{src_w, src_h},
+                   size2{slice_w, slice_h}, size2{out_w, out_h}, n_rois, batch, 0));
+    CK(cudaDeviceSynchronize());
+    return EMIDA_GB_OK;
+}
+
+int emida_gb_run_cross_corr(const void *pics, const void *ref, void *res, int precision,
+                            uint32_t w, uint32_t h, uint32_t res_w, uint32_t res_h,
+                            uint32_t ref_slices, uint32_t batch)
+{
+    CK(run_cross_corr(pics, ref, res, precision == EMIDA_GB_DOUBLE, size2{w, h},
+                      size2{res_w, res_h}, ref_slices, batch, 0));
+    CK(cudaDeviceSynchronize());
+    return EMIDA_GB_OK;
+}
+
+static int stage_tables(int precision, uint32_t w2, uint32_t h2, emida_gb_handle &tmp, fft_tables &t)
+{
+    tmp.dbl = precision == EMIDA_GB_DOUBLE;
+    CKS(upload_twiddles(&tmp, &tmp.d_tw_row, w2));
+    CKS(upload_twiddles(&tmp, &tmp.d_tw_col, h2));
+    t = fft_tables{tmp.d_tw_row, tmp.d_tw_col, w2, h2};
+    return EMIDA_GB_OK;
+}
+
+int emida_gb_run_fft_r2c(const void *real_in, void *spec, uint32_t maps, uint32_t w2,
+                         uint32_t h2, int precision)
+{
+    emida_gb_handle tmp;
+    fft_tables t;
+    int st = stage_tables(precision, w2, h2, tmp, t);
+    if (st == EMIDA_GB_OK) {
+        cudaError_t e = run_fft_r2c(real_in, spec, maps, t, precision == EMIDA_GB_DOUBLE, 0);
+        if (e == cudaSuccess) e = cudaDeviceSynchronize();
+        if (e != cudaSuccess) st = fail(EMIDA_GB_CUDA_ERROR, "fft r2c: %s", cudaGetErrorString(e));
+    }
+    for (void *p : tmp.allocs) cudaFree(p);
+    tmp.allocs.clear();
+    return st;
+}
+
+int emida_gb_run_fft_c2r(void *spec, void *real_out, uint32_t maps, uint32_t w2, uint32_t h2,
+                         int precision)
+{
+    emida_gb_handle tmp;
+    fft_tables t;
+    int st = stage_tables(precision, w2, h2, tmp, t);
+    if (st == EMIDA_GB_OK) {
+        cudaError_t e = run_fft_c2r(spec, real_out, maps, t, precision == EMIDA_GB_DOUBLE, 0);
+        if (e == cudaSuccess) e = cudaDeviceSynchronize();
+        if (e != cudaSuccess) st = fail(EMIDA_GB_CUDA_ERROR, "fft c2r: %s", cudaGetErrorString(e));
+    }
+    for (void *p : tmp.allocs) cudaFree(p);
+    tmp.allocs.clear();
+    return st;
+}
+
+int emida_gb_run_hadamard(void *pics, const void *ref, uint32_t one_area, uint32_t ref_slices,
+                          uint32_t batch, int precision)
+{
+    CK(run_hadamard(pics, ref, one_area, ref_slices, batch, precision == EMIDA_GB_DOUBLE, 0));
+    CK(cudaDeviceSynchronize());
+    return EMIDA_GB_OK;
+}
+
+int emida_gb_run_maxarg(const void *maps, uint32_t map_size, uint32_t n, void *maxes, int precision)
+{
+    CK(run_maxarg(maps, map_size, n, maxes, precision == EMIDA_GB_DOUBLE, 0));
+    CK(cudaDeviceSynchronize());
+    return EMIDA_GB_OK;
+}
+
+int emida_gb_run_extract_neighbors(const void *maps, const void *maxes, void *neigh, int s,
+                                   uint32_t cross_w, uint32_t cross_h, uint32_t n, int policy,
+                                   int precision)
+{
+    CK(run_extract_neighbors(maps, maxes, neigh, s, size2{cross_w, cross_h}, n, policy,
+                             precision == EMIDA_GB_DOUBLE, 0));
+    CK(cudaDeviceSynchronize());
+    return EMIDA_GB_OK;
+}
+
+}  // extern "C"

@@ -1,0 +1,441 @@
+// fused.cu -- the fused FFT-policy kernel: one CTA carries one (pattern, ROI)
+// pair at a time through the whole path of src/gpu_offset.hpp:234-301 --
+//   ROI gather (TMA) -> sum -> mean/Hann (prepare_pics.cu:34-41)
+//   -> 2N x 2N R2C in shared memory -> conj product with the resident reference
+//   spectrum (hadamard.cu:39-40) -> C2R -> argmax (maxarg.cu, first maximum)
+//   -> s x s neighbourhood (extract_neighbors.cu, FFT index policy)
+//   -> FP64 fit and offset (subpixel_max.hpp:76-97, gpu_offset.hpp:289-298).
+// Nothing but the ROI pixels is read from HBM per pair and nothing but the
+// results is written back; the reference spectra (66.5 KB per ROI at N=128)
+// stay L2-resident across the batch.
+//
+// Shared-memory spectrum: N rows (ky) x N/2 complex slots (kx), slot 0 packs
+// the real DC and Nyquist columns as (X[.][0], X[.][N/2]).  Slots are XOR
+// swizzled by row so that column and row accesses of the 8-lane FFT groups
+// spread over all banks.  The uint16 ROI tile is staged by TMA into the
+// spectrum's upper half, which is unused until the column pass.
+#include <cuda.h>
+
+#include "device_fit.cuh"
+#include "fft.cuh"
+#include "fused.cuh"
+
+namespace emida_gb {
+
+namespace {
+
+template <int N, typename C>
+__device__ __forceinline__ C *sp(C *S, int row, int slot)
+{
+    return S + row * (N / 2) + (slot ^ (((row >> 1) & 3) << 2));
+}
+
+template <int N, typename C> struct col_line {
+    C *S;
+    int c;
+    __device__ __forceinline__ C *operator()(int q) const { return sp<N>(S, q, c); }
+};
+template <int N, typename C> struct row_line {
+    C *S;
+    int a;
+    __device__ __forceinline__ C *operator()(int q) const
+    {
+        return sp<N>(S, a + (q >= N / 2 ? 1 : 0), q & (N / 2 - 1));
+    }
+};
+
+__device__ __forceinline__ uint32_t smem_u32(const void *p)
+{
+    return (uint32_t)__cvta_generic_to_shared(p);
+}
+
+__device__ __forceinline__ void mbar_init(uint64_t *bar, uint32_t count)
+{
+    asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;" ::"r"(smem_u32(bar)), "r"(count));
+}
+__device__ __forceinline__ void fence_proxy_async()
+{
+    asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
+}
+__device__ __forceinline__ void mbar_expect_tx(uint64_t *bar, uint32_t bytes)
+{
+    asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(smem_u32(bar)),
+                 "r"(bytes)
+                 : "memory");
+}
+__device__ __forceinline__ void tma_load_3d(void *dst, const CUtensorMap *map, int x, int y, int z,
+                                            uint64_t *bar)
+{
+    asm volatile(
+        "cp.async.bulk.tensor.3d.shared::cluster.global.tile.mbarrier::complete_tx::bytes"
+        " [%0], [%1, {%2, %3, %4}], [%5];" ::"r"(smem_u32(dst)),
+        "l"((uint64_t)map), "r"(x), "r"(y), "r"(z), "r"(smem_u32(bar))
+        : "memory");
+}
+// Bounded wait on an mbarrier phase: returns false when the budget ran out.
+__device__ __forceinline__ bool mbar_wait(uint64_t *bar, uint32_t parity)
+{
+    const long long budget = 4000000000LL; /* ~2 s at 2 GHz */
+    long long start = clock64();
+    while (true) {
+        uint32_t done;
+        asm volatile(
+            "{ .reg .pred p; mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;"
+            " selp.u32 %0, 1, 0, p; }"
+            : "=r"(done)
+            : "r"(smem_u32(bar)), "r"(parity)
+            : "memory");
+        if (done) return true;
+        if (clock64() - start > budget) return false;
+    }
+}
+
+template <typename T> __device__ __forceinline__ T neg_inf();
+template <> __device__ __forceinline__ float neg_inf<float>() { return -__int_as_float(0x7f800000); }
+template <> __device__ __forceinline__ double neg_inf<double>()
+{
+    return -__longlong_as_double(0x7ff0000000000000LL);
+}
+
+template <typename T>
+__device__ __forceinline__ void better(T &bv, uint32_t &bi, T v, uint32_t i)
+{
+    if (v > bv || (v == bv && i < bi)) {
+        bv = v;
+        bi = i;
+    }
+}
+
+}  // namespace
+
+template <int N, typename T, typename IN>
+__global__ void __launch_bounds__(2 * N, sizeof(T) == 4 ? 2 : 1) fused_fft_kernel(const fused_args a,
+                                                          const __grid_constant__ CUtensorMap tmap)
+{
+    using C = cplx<T>;
+    constexpr int H = N / 2;           // ROI side
+    constexpr int SL = N / 2;          // slots per spectrum row
+    constexpr int E = N / 8;           // elements per lane
+    constexpr int THREADS = 2 * N;
+    constexpr int GROUPS = THREADS / 8;
+    constexpr int WARPS = THREADS / 32;
+    constexpr int TW = H + 8;          // uint16 tile row (TMA box width)
+
+    extern __shared__ __align__(1024) unsigned char smem[];
+    C *S = reinterpret_cast<C *>(smem);
+    C *tw = S + N * SL;
+    T *hx = reinterpret_cast<T *>(tw + N);
+    T *hy = hx + H;
+    T *red_v = hy + H;
+    uint32_t *red_i = reinterpret_cast<uint32_t *>(red_v + 32);
+    double *red_s = reinterpret_cast<double *>(red_i + 32);  // 8-aligned: counts are even
+    double *nb = red_s + 32;                                 // 81 neighbours
+    double *cf = nb + 81;                                    // 6 coefficients (+1 pad)
+    uint64_t *bar = reinterpret_cast<uint64_t *>(cf + 8);
+    unsigned char *tile = reinterpret_cast<unsigned char *>(S + H * SL);
+
+    const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
+    const int t = lane & 7, g = tid >> 3;
+
+    const C *gtw = reinterpret_cast<const C *>(a.twiddles);
+    for (int i = tid; i < N; i += THREADS) tw[i] = gtw[i];
+    const T *ghann = reinterpret_cast<const T *>(a.hann);
+    for (int i = tid; i < 2 * H; i += THREADS) hx[i] = ghann[i];  // hx then hy
+    if (tid == 0) {
+        mbar_init(bar, 1);
+        fence_proxy_async();
+    }
+    __syncthreads();
+
+    const int s = a.fitsize, s2 = s * s;
+    uint32_t iter = 0;
+    for (uint32_t pair = blockIdx.x; pair < a.n_pairs; pair += gridDim.x, ++iter) {
+        const uint32_t pic = pair / a.n_rois, roi = pair % a.n_rois;
+        const uint2 beg = a.begins[roi];
+
+        // ---- gather the ROI and sum it (sum.cu:109-158) -------------------
+        T mean;
+        int xo = 0;
+        if constexpr (sizeof(IN) == 2) {
+            const int x0 = (int)(beg.x & ~7u);
+            xo = (int)beg.x - x0;
+            uint16_t *t16 = reinterpret_cast<uint16_t *>(tile);
+            if (a.use_tma) {
+                if (tid == 0) {
+                    fence_proxy_async();
+                    mbar_expect_tx(bar, TW * H * 2);
+                    tma_load_3d(tile, &tmap, x0, (int)beg.y, (int)pic, bar);
+                }
+                if (!mbar_wait(bar, iter & 1)) {
+                    if (tid == 0) atomicOr(a.err, DEV_ERR_TMA_TIMEOUT);
+                    return;
+                }
+            } else {
+                const uint16_t *src = reinterpret_cast<const uint16_t *>(a.pics) +
+                                      (size_t)pic * a.src_w * a.src_h +
+                                      (size_t)beg.y * a.src_w + beg.x;
+                for (int i = tid; i < H * H; i += THREADS)
+                    t16[(i / H) * TW + xo + (i % H)] = src[(size_t)(i / H) * a.src_w + (i % H)];
+                __syncthreads();
+            }
+            uint32_t acc = 0;
+            for (int i = tid; i < H * H; i += THREADS) acc += t16[(i / H) * TW + xo + (i % H)];
+#pragma unroll
+            for (int o = 16; o; o >>= 1) acc += __shfl_xor_sync(0xffffffffu, acc, o);
+            if (lane == 0) red_i[warp] = acc;
+            __syncthreads();
+            uint32_t total = 0;
+#pragma unroll
+            for (int w = 0; w < WARPS; ++w) total += red_i[w];
+            mean = (T)total / (T)(H * H);
+        } else {
+            double *t64 = reinterpret_cast<double *>(tile);
+            const double *src = reinterpret_cast<const double *>(a.pics) +
+                                (size_t)pic * a.src_w * a.src_h + (size_t)beg.y * a.src_w + beg.x;
+            double acc = 0;
+            for (int i = tid; i < H * H; i += THREADS) {
+                double v = src[(size_t)(i / H) * a.src_w + (i % H)];
+                t64[i] = v;
+                acc += v;
+            }
+#pragma unroll
+            for (int o = 16; o; o >>= 1) acc += __shfl_xor_sync(0xffffffffu, acc, o);
+            if (lane == 0) red_s[warp] = acc;
+            __syncthreads();
+            double total = 0;
+#pragma unroll
+            for (int w = 0; w < WARPS; ++w) total += red_s[w];
+            mean = (T)total / (T)(H * H);
+        }
+
+        // ---- forward rows: pairs of real rows as one complex FFT ----------
+        {
+            const int ra = 2 * g, rb = ra + 1;
+            C v[E];
+#pragma unroll
+            for (int m = 0; m < E / 2; ++m) {
+                const int x = t + 8 * m;
+                T pa, pb;
+                if constexpr (sizeof(IN) == 2) {
+                    const uint16_t *t16 = reinterpret_cast<const uint16_t *>(tile);
+                    pa = (T)t16[ra * TW + xo + x];
+                    pb = (T)t16[rb * TW + xo + x];
+                } else {
+                    const double *t64 = reinterpret_cast<const double *>(tile);
+                    pa = (T)t64[ra * H + x];
+                    pb = (T)t64[rb * H + x];
+                }
+                pa -= mean;
+                pb -= mean;
+                pa = pa * hx[x] * hy[ra];
+                pb = pb * hx[x] * hy[rb];
+                v[m] = cmake<C>(pa, pb);
+            }
+            row_line<N, C> line{S, ra};
+            group_fft<N, -1, true, T>(v, t, line, tw);
+            const int partner = (lane & ~7) | ((8 - t) & 7);
+#pragma unroll
+            for (int j = 0; j < E / 2; ++j) {
+                C send = (t == 0) ? v[(E - j) & (E - 1)] : v[E - 1 - j];
+                C zm = cmake<C>(__shfl_sync(0xffffffffu, send.x, partner),
+                                __shfl_sync(0xffffffffu, send.y, partner));
+                C z = v[j];
+                const int k = t + 8 * j;
+                if (k == 0) {
+                    C zh = v[E / 2];
+                    *sp<N>(S, ra, 0) = cmake<C>(z.x, zh.x);
+                    *sp<N>(S, rb, 0) = cmake<C>(z.y, zh.y);
+                } else {
+                    *sp<N>(S, ra, k) = cmake<C>((z.x + zm.x) * (T)0.5, (z.y - zm.y) * (T)0.5);
+                    *sp<N>(S, rb, k) = cmake<C>((z.y + zm.y) * (T)0.5, (zm.x - z.x) * (T)0.5);
+                }
+            }
+        }
+        __syncthreads();
+
+        // ---- columns: forward FFT, conj product, inverse FFT --------------
+        const C *R = reinterpret_cast<const C *>(a.ref_spec) + (size_t)roi * (SL + 1) * N;
+#pragma unroll 1
+        for (int rnd = 0; rnd < SL / GROUPS; ++rnd) {
+            const int c = g + rnd * GROUPS;
+            C v[E];
+#pragma unroll
+            for (int m = 0; m < E / 2; ++m) v[m] = *sp<N>(S, t + 8 * m, c);
+            col_line<N, C> line{S, c};
+            group_fft<N, -1, true, T>(v, t, line, tw);
+            const C *Rc = R + (size_t)c * N;
+            if (warp == 0 && rnd == 0) {
+                // This warp holds column 0, whose slot packs the DC and Nyquist
+                // columns: unpack X[ky] with its mirror X[N-ky], multiply each
+                // half by its own reference column, repack.  The exchange goes
+                // through the warp's columns with full-warp syncs.
+#pragma unroll
+                for (int j = 0; j < E; ++j) *sp<N>(S, t + 8 * j, c) = v[j];
+                __syncwarp();
+#pragma unroll
+                for (int j = 0; j < E; ++j) {
+                    const int ky = t + 8 * j;
+                    if (c == 0) {
+                        C x = v[j];
+                        C xm = *sp<N>(S, (N - ky) & (N - 1), 0);
+                        C p0 = cmake<C>((x.x + xm.x) * (T)0.5, (x.y - xm.y) * (T)0.5);
+                        C p64 = cmake<C>((x.y + xm.y) * (T)0.5, (xm.x - x.x) * (T)0.5);
+                        C q0 = cmulc(p0, __ldg(R + ky));
+                        C q64 = cmulc(p64, __ldg(R + (size_t)SL * N + ky));
+                        v[j] = cmake<C>(q0.x - q64.y, q0.y + q64.x);
+                    } else {
+                        v[j] = cmulc(v[j], __ldg(Rc + ky));
+                    }
+                }
+                __syncwarp();
+            } else {
+#pragma unroll
+                for (int j = 0; j < E; ++j) v[j] = cmulc(v[j], __ldg(Rc + t + 8 * j));
+            }
+            group_fft<N, +1, false, T>(v, t, line, tw);
+#pragma unroll
+            for (int j = 0; j < E; ++j) *sp<N>(S, t + 8 * j, c) = v[j];
+        }
+        __syncthreads();
+
+        // ---- inverse rows: pairs of half spectra -> two real rows ---------
+        T bv = neg_inf<T>();
+        uint32_t bi = 0xffffffffu;
+#pragma unroll 1
+        for (int rnd = 0; rnd < (N / 2) / GROUPS; ++rnd) {
+            const int ra = 2 * (g + rnd * GROUPS), rb = ra + 1;
+            C v[E];
+#pragma unroll
+            for (int j = 0; j < E; ++j) {
+                const int n = t + 8 * j;
+                if (j < E / 2) {
+                    C ga = *sp<N>(S, ra, n), gb = *sp<N>(S, rb, n);
+                    v[j] = (n == 0) ? cmake<C>(ga.x, gb.x) : cmake<C>(ga.x - gb.y, ga.y + gb.x);
+                } else {
+                    const int k = (n == H) ? 0 : N - n;
+                    C ga = *sp<N>(S, ra, k), gb = *sp<N>(S, rb, k);
+                    v[j] = (n == H) ? cmake<C>(ga.y, gb.y) : cmake<C>(ga.x + gb.y, gb.x - ga.y);
+                }
+            }
+            row_line<N, C> line{S, ra};
+            group_fft<N, +1, false, T>(v, t, line, tw);
+#pragma unroll
+            for (int j = 0; j < E; ++j) {
+                const int x = t + 8 * j;
+                reinterpret_cast<T *>(sp<N>(S, ra, x >> 1))[x & 1] = v[j].x;
+                reinterpret_cast<T *>(sp<N>(S, rb, x >> 1))[x & 1] = v[j].y;
+                better(bv, bi, v[j].x, (uint32_t)(ra * N + x));
+                better(bv, bi, v[j].y, (uint32_t)(rb * N + x));
+            }
+        }
+
+        // ---- argmax over the N x N map (maxarg.cu, first maximum) ---------
+#pragma unroll
+        for (int o = 16; o; o >>= 1) {
+            T ov = __shfl_xor_sync(0xffffffffu, bv, o);
+            uint32_t oi = __shfl_xor_sync(0xffffffffu, bi, o);
+            better(bv, bi, ov, oi);
+        }
+        if (lane == 0) {
+            red_v[warp] = bv;
+            red_i[warp] = bi;
+        }
+        __syncthreads();
+
+        // ---- neighbourhood, FP64 fit, offsets (warp 0) --------------------
+        if (warp == 0) {
+            T pv = red_v[0];
+            uint32_t pk = red_i[0];
+            for (int w = 1; w < WARPS; ++w) better(pv, pk, red_v[w], red_i[w]);
+            if (pk >= (uint32_t)(N * N)) pk = 0;
+            uint32_t mx, my;
+            shift_pos(pk, POLICY_FFT, N - 1, N - 1, mx, my);
+            for (int l = lane; l < s2; l += 32) {
+                uint32_t x, y;
+                neighbour_pos(mx, my, l % s, l / s, s, N - 1, N - 1, x, y);
+                const uint32_t q = (uint32_t)policy_index(POLICY_FFT, x, y, N - 1, N - 1);
+                const uint32_t qy = q / N, qx = q % N;
+                T val = reinterpret_cast<T *>(sp<N>(S, qy, qx >> 1))[qx & 1];
+                nb[l] = (double)val;
+                if (a.neigh) reinterpret_cast<T *>(a.neigh)[(size_t)pair * s2 + l] = val;
+            }
+            __syncwarp();
+            if (lane < 6) cf[lane] = fit_coef(a.lstsq, nb, s, lane);
+            __syncwarp();
+            if (lane < 6 && a.coefs) a.coefs[(size_t)pair * 6 + lane] = cf[lane];
+            if (lane == 0) {
+                double ox, oy;
+                fit_offsets(cf, mx, my, N - 1, N - 1, s, ox, oy);
+                a.offsets[2 * (size_t)pair] = ox;
+                a.offsets[2 * (size_t)pair + 1] = oy;
+                if (a.maxes) {
+                    data_index<T> *mi = reinterpret_cast<data_index<T> *>(a.maxes) + pair;
+                    mi->data = pv;
+                    mi->index = pk;
+                }
+            }
+        }
+        __syncthreads();
+    }
+}
+
+template <int N, typename T>
+size_t fused_smem_bytes()
+{
+    using C = cplx<T>;
+    size_t b = (size_t)N * (N / 2) * sizeof(C);  // spectrum
+    b += N * sizeof(C);                          // twiddles
+    b += N * sizeof(T);                          // hx, hy
+    b += 32 * sizeof(T) + 32 * sizeof(uint32_t); // argmax scratch
+    b = (b + 7) & ~(size_t)7;
+    b += (32 + 81 + 8) * sizeof(double);         // sums, neighbours, coefs
+    b += 16;                                     // mbarrier
+    return b;
+}
+
+template <int N, typename T, typename IN>
+static cudaError_t launch_one(const fused_args &a, const CUtensorMap *tmap, int grid,
+                              cudaStream_t st)
+{
+    auto k = fused_fft_kernel<N, T, IN>;
+    const size_t smem = fused_smem_bytes<N, T>();
+    cudaError_t e = cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+    if (e != cudaSuccess) return e;
+    if (grid <= 0) {
+        int per_sm = 0, dev = 0, sms = 0;
+        cudaGetDevice(&dev);
+        cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+        e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k, 2 * N, smem);
+        if (e != cudaSuccess) return e;
+        if (per_sm < 1) per_sm = 1;
+        grid = per_sm * sms;
+    }
+    if ((uint32_t)grid > a.n_pairs) grid = (int)a.n_pairs;
+    if (grid < 1) return cudaSuccess;
+    k<<<grid, 2 * N, smem, st>>>(a, *tmap);
+    return cudaGetLastError();
+}
+
+bool fused_supported(uint32_t fft_n) { return fft_n == 64 || fft_n == 128; }
+
+cudaError_t launch_fused(uint32_t fft_n, bool dbl, bool in_f64, const fused_args &a,
+                         const CUtensorMap *tmap, int grid, cudaStream_t st)
+{
+    if (fft_n == 128) {
+        if (dbl)
+            return in_f64 ? launch_one<128, double, double>(a, tmap, grid, st)
+                          : launch_one<128, double, uint16_t>(a, tmap, grid, st);
+        return in_f64 ? launch_one<128, float, double>(a, tmap, grid, st)
+                      : launch_one<128, float, uint16_t>(a, tmap, grid, st);
+    }
+    if (fft_n == 64) {
+        if (dbl)
+            return in_f64 ? launch_one<64, double, double>(a, tmap, grid, st)
+                          : launch_one<64, double, uint16_t>(a, tmap, grid, st);
+        return in_f64 ? launch_one<64, float, double>(a, tmap, grid, st)
+                      : launch_one<64, float, uint16_t>(a, tmap, grid, st);
+    }
+    return cudaErrorInvalidValue;
+}
+
+}  // namespace emida_gb

@@ -1,0 +1,35 @@
+// fused.cuh -- launcher interface of the fused FFT-policy kernel (fused.cu).
+#pragma once
+
+#include <cuda.h>
+
+#include "common.cuh"
+
+namespace emida_gb {
+
+struct fused_args {
+    const void *pics;       // [batch][src_h][src_w] uint16 or double
+    uint32_t src_w, src_h;
+    const uint2 *begins;    // [n_rois] ROI top-left (x, y)
+    uint32_t n_rois;
+    uint32_t n_pairs;       // batch * n_rois
+    const void *ref_spec;   // [n_rois][N/2 + 1][N] complex: column kx holds X[0..N-1][kx]
+    const void *hann;       // [2 * (N/2)]: x window then y window, element type T
+    const void *twiddles;   // [N] complex T: exp(-2 pi i j / N)
+    const double *lstsq;    // (A^T A)^-1 A^T, 6 x s*s
+    int fitsize;
+    int use_tma;            // stage the uint16 ROI through a TMA tensor map
+    double *offsets;        // [n_pairs][2]
+    double *coefs;          // [n_pairs][6] or null
+    void *maxes;            // data_index<T>[n_pairs] or null
+    void *neigh;            // T[n_pairs][s*s] or null
+    uint32_t *err;          // device error word (dev_err_t bits)
+};
+
+bool fused_supported(uint32_t fft_n);
+
+// grid <= 0: one wave of resident CTAs (occupancy x SM count).
+cudaError_t launch_fused(uint32_t fft_n, bool dbl, bool in_f64, const fused_args &a,
+                         const CUtensorMap *tmap, int grid, cudaStream_t st);
+
+}  // namespace emida_gb

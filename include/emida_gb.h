@@ -1,0 +1,169 @@
+/*
+ * emida_gb.h -- C ABI of the GB300-native emida ROI cross-correlation path.
+ *
+ * The entry points replace, one for one, the members of the reference's
+ * driver class  template<class T, class IN> class gpu_offset
+ * (src/gpu_offset.hpp:48-326) and its kernel launchers (src/kernels.cuh:56-125).
+ * All functions return EMIDA_GB_OK (0) or a negative status; the message of the
+ * last failure on the calling thread is returned by emida_gb_last_error().
+ * The reference throws std::runtime_error instead (src/host_helpers.hpp:14-25);
+ * the C++ shim include/emida_gb/gpu_offset.hpp turns statuses back into throws.
+ *
+ * Layouts (src/gpu_offset.hpp:41-45): a batch is [batch][src_h][src_w]
+ * row-major pixels; results are pattern-major then ROI-major
+ * (i = pattern * n_rois + roi).  Offsets are (x, y) doubles, coefficients the
+ * six (a, b, c, d, e, f) of a + bx + cy + dx^2 + exy + fy^2.
+ */
+#ifndef EMIDA_GB_H
+#define EMIDA_GB_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+enum {
+    EMIDA_GB_OK = 0,
+    EMIDA_GB_INVALID_ARGUMENT = -1,
+    EMIDA_GB_CUDA_ERROR = -2,
+    EMIDA_GB_UNSUPPORTED = -3,
+    EMIDA_GB_DEVICE_CHECK = -4,
+    EMIDA_GB_OUT_OF_MEMORY = -5
+};
+
+/* src/common.hpp:269-273 cross_policy */
+enum { EMIDA_GB_BRUTE = 0, EMIDA_GB_FFT = 1 };
+/* src/args_parser.hpp:14-18 precision_type (value order of this ABI) */
+enum { EMIDA_GB_DOUBLE = 0, EMIDA_GB_FLOAT = 1 };
+/* the IN template parameter of gpu_offset<T, IN> */
+enum { EMIDA_GB_IN_U16 = 0, EMIDA_GB_IN_F64 = 1 };
+/* execution form: AUTO picks FUSED where a fused kernel covers the shape */
+enum { EMIDA_GB_MODE_AUTO = 0, EMIDA_GB_MODE_PLAIN = 1, EMIDA_GB_MODE_FUSED = 2 };
+
+typedef struct emida_gb_handle emida_gb_handle;
+
+/* Constructor arguments of gpu_offset (src/gpu_offset.hpp:100-125). */
+typedef struct emida_gb_params {
+    uint32_t src_w, src_h;     /* pattern size (src_size) */
+    const uint32_t *begins;    /* [n_rois][2] ROI top-left (x, y); copied */
+    uint32_t n_rois;
+    uint32_t slice_w, slice_h; /* ROI size (slice_size) */
+    uint32_t cross_w, cross_h; /* brute lag window (odd); FFT forces 2*slice-1 */
+    uint32_t batch_size;       /* patterns per batch */
+    int32_t policy;            /* EMIDA_GB_BRUTE | EMIDA_GB_FFT */
+    int32_t precision;         /* EMIDA_GB_DOUBLE | EMIDA_GB_FLOAT (the T parameter) */
+    int32_t fitsize;           /* s = 3, 5, 7, 9 */
+    int32_t in_type;           /* EMIDA_GB_IN_U16 | EMIDA_GB_IN_F64 (the IN parameter) */
+    int32_t mode;              /* EMIDA_GB_MODE_* */
+    uint32_t in_buffers;       /* device input buffers (in_buffers_size) */
+} emida_gb_params;
+
+/* gpu_offset ctor + the allocating half of allocate_memory
+ * (src/gpu_offset.hpp:100-183).  Creates the streams and every device buffer. */
+int emida_gb_create(const emida_gb_params *p, emida_gb_handle **out);
+
+/* Reference half of allocate_memory (src/gpu_offset.hpp:185-210): sums,
+ * prepare and forward FFT of the reference ROIs, kept resident.
+ * ref: host pointer to one pattern of in_type pixels. */
+int emida_gb_set_reference(emida_gb_handle *h, const void *ref);
+
+/* transfer_pic_to_device_async (src/gpu_offset.hpp:213-218): asynchronous copy
+ * of one batch from (pinned) host memory into the next input buffer on the
+ * input stream; thread-safe; returns the buffer index. */
+int emida_gb_transfer_async(emida_gb_handle *h, const void *batch, uint32_t *buffer_index);
+
+/* get_offset_core (src/gpu_offset.hpp:234-278): runs the path on input buffer
+ * `buffer_index` (after the input stream) and copies the per-ROI maxima
+ * (data_index<T> {T value; uint32 index}) and s*s neighbourhoods (T) to the
+ * host buffers, asynchronously on the output stream.  Either may be NULL. */
+int emida_gb_offsets_core(emida_gb_handle *h, uint32_t buffer_index, void *maxes_out,
+                          void *neigh_out);
+
+/* finalize (src/gpu_offset.hpp:280-301): waits for the output stream and fits
+ * the neighbourhoods on the host.  offsets [n][2]; coefs [n][6] or NULL. */
+int emida_gb_finalize(emida_gb_handle *h, const void *maxes, const void *neigh,
+                      double *offsets, double *coefs);
+
+/* get_offset (src/gpu_offset.hpp:220-231): synchronous copy of one batch,
+ * the whole path on the device including the FP64 fit, and the results.
+ * coefs and peaks (uint32 argmax index per ROI) may be NULL. */
+int emida_gb_get_offset(emida_gb_handle *h, const void *batch, double *offsets, double *coefs,
+                        uint32_t *peaks);
+
+/* Device-resident form for pipelines and benchmarks: `patterns` whole
+ * patterns (any count, not limited to batch_size) already in device memory,
+ * results to device memory, all on `stream` (NULL: the handle's compute
+ * stream), no synchronisation.  coefs, maxes, neigh may be NULL. */
+int emida_gb_run_device(emida_gb_handle *h, const void *dev_patterns, uint32_t patterns,
+                        double *dev_offsets, double *dev_coefs, void *dev_maxes,
+                        void *dev_neigh, void *stream);
+
+/* Which form the handle runs: EMIDA_GB_MODE_PLAIN or EMIDA_GB_MODE_FUSED. */
+int emida_gb_resolved_mode(const emida_gb_handle *h);
+/* The handle's compute stream (a cudaStream_t). */
+void *emida_gb_stream(emida_gb_handle *h);
+/* Number of kernel launches one emida_gb_run_device call makes. */
+int emida_gb_launches_per_run(const emida_gb_handle *h);
+void emida_gb_destroy(emida_gb_handle *h);
+
+const char *emida_gb_last_error(void);
+const char *emida_gb_version(void);
+
+/* Host fit of s*s neighbourhoods (src/subpixel_max.hpp:76-97); values are
+ * doubles.  sub [n][2] (x, y) inside the window, coefs [n][6] or NULL. */
+int emida_gb_subpixel_max(const double *neigh, int s, uint32_t n, double *sub, double *coefs);
+/* (A^T A)^-1 A^T used by the fit, 6 x s*s (src/subpixel_max.cpp:5-58). */
+int emida_gb_lstsq_matrix(int s, double *out);
+
+/* ---- device memory helpers (for callers without a CUDA runtime binding) --- */
+int emida_gb_device_count(int *count);
+int emida_gb_malloc(void **dev_ptr, size_t bytes);
+int emida_gb_free(void *dev_ptr);
+int emida_gb_memset(void *dev_ptr, int value, size_t bytes);
+int emida_gb_memcpy_h2d(void *dev_dst, const void *host_src, size_t bytes);
+int emida_gb_memcpy_d2h(void *host_dst, const void *dev_src, size_t bytes);
+int emida_gb_malloc_host(void **host_ptr, size_t bytes);
+int emida_gb_free_host(void *host_ptr);
+int emida_gb_synchronize(void);
+/* CUDA-event timing on a stream: elapsed ms of `repeats` runs of the handle's
+ * device form over the same inputs, measured on the launching stream. */
+int emida_gb_time_device(emida_gb_handle *h, const void *dev_patterns, uint32_t patterns,
+                         double *dev_offsets, int repeats, float *ms);
+
+/* ---- per-stage launchers (src/kernels.cuh:56-125), device pointers -------- */
+/* run_sum: sums[pair] over each ROI; u16 -> uint32, f64 -> double. */
+int emida_gb_run_sum(const void *pics, int in_type, uint32_t src_w, uint32_t src_h,
+                     const uint32_t *dev_begins, uint32_t n_rois, uint32_t slice_w,
+                     uint32_t slice_h, uint32_t batch, void *sums);
+/* run_prepare_pics: hann = slice_w x-window values then slice_h y-window values (T). */
+int emida_gb_run_prepare(const void *pics, int in_type, int precision, void *slices,
+                         const void *hann, const void *sums, const uint32_t *dev_begins,
+                         uint32_t src_w, uint32_t src_h, uint32_t slice_w, uint32_t slice_h,
+                         uint32_t out_w, uint32_t out_h, uint32_t n_rois, uint32_t batch);
+/* run_cross_corr (brute): res [ref_slices*batch][res_h][res_w]. */
+int emida_gb_run_cross_corr(const void *pics, const void *ref, void *res, int precision,
+                            uint32_t w, uint32_t h, uint32_t res_w, uint32_t res_h,
+                            uint32_t ref_slices, uint32_t batch);
+/* forward R2C of [maps][h2][w2] real into [maps][h2][w2/2+1] complex (cuFFT layout). */
+int emida_gb_run_fft_r2c(const void *real_in, void *spec, uint32_t maps, uint32_t w2,
+                         uint32_t h2, int precision);
+/* unnormalised C2R of [maps][h2][w2/2+1] (overwritten) into [maps][h2][w2] real. */
+int emida_gb_run_fft_c2r(void *spec, void *real_out, uint32_t maps, uint32_t w2, uint32_t h2,
+                         int precision);
+/* run_hadamard: pics[i] *= conj(ref[i mod (one_area*ref_slices)]) (complex T). */
+int emida_gb_run_hadamard(void *pics, const void *ref, uint32_t one_area, uint32_t ref_slices,
+                          uint32_t batch, int precision);
+/* run_maxarg_reduce: maxes[i] = {max, first index} of map i. */
+int emida_gb_run_maxarg(const void *maps, uint32_t map_size, uint32_t n, void *maxes,
+                        int precision);
+/* run_extract_neighbors with the policy's index map. */
+int emida_gb_run_extract_neighbors(const void *maps, const void *maxes, void *neigh, int s,
+                                   uint32_t cross_w, uint32_t cross_h, uint32_t n, int policy,
+                                   int precision);
+
+#ifdef __cplusplus
+}
+#endif
+#endif

@@ -1,0 +1,90 @@
+"""The C ABI library loads and exports every entry point include/emida_gb.h
+declares; host-side logic that needs no GPU (parameter validation, the exact
+least-squares tables, the host fit).  CPU only."""
+import os
+import re
+
+import numpy as np
+import pytest
+
+from tests.conftest import GOLDEN, ROOT
+
+REF_OUT = np.load(os.path.join(GOLDEN, "ref_cpu_outputs.npz"))
+
+
+def header_symbols():
+    text = open(os.path.join(ROOT, "include", "emida_gb.h")).read()
+    return sorted(set(re.findall(r"\b(emida_gb_[a-z0-9_]+)\s*\(", text)))
+
+
+@pytest.fixture(scope="module")
+def lib():
+    import __graft_entry__
+    __graft_entry__.build_library()
+    from emida_gb300 import _lib
+    return _lib.lib()
+
+
+def test_every_declared_symbol_is_exported(lib):
+    syms = header_symbols()
+    assert len(syms) >= 30
+    for s in syms:
+        assert hasattr(lib, s), s
+
+
+def test_binding_covers_header(lib):
+    from emida_gb300 import _lib
+    assert set(header_symbols()) == set(_lib.SIGNATURES)
+
+
+@pytest.mark.parametrize("s", [3, 5, 7, 9])
+def test_library_lstsq_tables_are_the_references(lib, s):
+    from emida_gb300 import lstsq_matrix
+    assert np.array_equal(lstsq_matrix(s).ravel(), REF_OUT[f"lstsq_{s}"])
+
+
+@pytest.mark.parametrize("s", [3, 5, 7, 9])
+def test_library_host_fit_is_the_references(lib, s):
+    from emida_gb300 import subpixel_max
+    sub, co = subpixel_max(REF_OUT[f"fit_{s}_neigh"], s)
+    assert np.array_equal(sub, REF_OUT[f"fit_{s}_sub"])
+    assert np.array_equal(co, REF_OUT[f"fit_{s}_coefs"])
+
+
+def test_fitsize_rejected(lib):
+    from emida_gb300 import EmidaError, subpixel_max, lstsq_matrix
+    with pytest.raises(EmidaError, match="Wrong fitting size"):
+        lstsq_matrix(4)
+    with pytest.raises(EmidaError):
+        subpixel_max(np.zeros(16), 4)
+
+
+@pytest.mark.parametrize("kw,msg", [
+    (dict(s=4), "Wrong fitting size"),
+    (dict(batch_size=0), "batchsize"),
+    (dict(begins=[(200, 0)]), "out of bounds"),
+    (dict(cross_size=(200, 3)), "cross size"),
+    (dict(policy="sideways"), "crosspolicy"),
+    (dict(precision="half"), "precision"),
+])
+def test_parameter_validation(lib, kw, msg):
+    from emida_gb300 import EmidaError, GpuOffset
+    args = dict(src_size=(256, 256), begins=[(0, 0)], slice_size=(64, 64), cross_size=(127, 127),
+                batch_size=1, policy="brute", s=3)
+    args.update(kw)
+    with pytest.raises((EmidaError, ValueError), match=msg):
+        GpuOffset(**args)
+
+
+def test_fft_needs_square_rois(lib):
+    from emida_gb300 import EmidaError, GpuOffset
+    with pytest.raises(EmidaError, match="square"):
+        GpuOffset((256, 256), [(0, 0)], (64, 32), (127, 63), 1, "fft", 3)
+
+
+def test_no_cpu_fallback_when_library_missing(tmp_path, monkeypatch):
+    from emida_gb300 import _lib
+    monkeypatch.setattr(_lib, "_lib", None)
+    monkeypatch.setattr(_lib, "LIB_PATH", str(tmp_path / "missing.so"))
+    with pytest.raises(ImportError, match="no CPU fallback"):
+        _lib.lib()

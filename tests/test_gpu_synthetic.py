@@ -1,0 +1,137 @@
+"""Synthetic EBSD patterns (uint16) through the C ABI against the FP64 oracle:
+integer peaks identical, offsets within the precision's tolerance."""
+import numpy as np
+import pytest
+
+pytestmark = pytest.mark.gpu
+
+
+@pytest.fixture(scope="module", autouse=True)
+def built():
+    import __graft_entry__
+    __graft_entry__.build_library()
+
+
+@pytest.fixture(scope="module")
+def data512():
+    from emida_gb300 import synth
+    ref = synth.reference_pattern(512, seed=11)
+    pics, _ = synth.deformed_patterns(512, 11, 3, sigma_eps=2e-3)
+    return ref, pics
+
+
+def run(ref, pics, begins, slice_, policy, s, precision, mode, cross=None):
+    from emida_gb300 import GpuOffset
+    h, w = ref.shape
+    cross = cross or (2 * slice_ - 1, 2 * slice_ - 1)
+    g = GpuOffset((w, h), begins, (slice_, slice_), cross, len(pics), policy, s, 1, precision,
+                  np.uint16, mode)
+    g.allocate_memory(ref)
+    out = g.get_offset(pics, with_peaks=True)
+    assert g.mode == mode
+    g.close()
+    return out
+
+
+def oracle(ref, pics, begins, slice_, policy, s, cross=None):
+    from oracle import oracle as eo
+    cross = cross or (2 * slice_ - 1, 2 * slice_ - 1)
+    pol = eo.POLICY_FFT if policy == "fft" else eo.POLICY_BRUTE
+    return eo.get_offsets(ref, pics, begins, slice_, slice_, pol, s, cross[0], cross[1])
+
+
+def test_brute_double_bit_exact(data512):
+    # the brute stages use the oracle's operation order: same bits
+    from emida_gb300 import synth
+    ref, pics = data512
+    _, begins = synth.roi_grid(512, 5, 32, margin=40)
+    offs, coefs, peaks = run(ref, pics[:2], begins, 64, "brute", 3, "double", "plain")
+    o_offs, o_coefs, o_peaks = oracle(ref, pics[:2], begins, 64, "brute", 3)
+    assert np.array_equal(peaks, o_peaks)
+    assert np.array_equal(offs, o_offs)
+    assert np.array_equal(coefs, o_coefs)
+
+
+@pytest.mark.parametrize("mode", ["plain", "fused"])
+@pytest.mark.parametrize("precision,tol", [("double", 1e-9), ("float", 1e-3)])
+@pytest.mark.parametrize("s", [3, 5, 7, 9])
+def test_fft_vs_oracle(data512, mode, precision, tol, s):
+    from emida_gb300 import synth
+    ref, pics = data512
+    _, begins = synth.roi_grid(512, 4, 32, margin=40)
+    offs, coefs, peaks = run(ref, pics, begins, 64, "fft", s, precision, mode)
+    o_offs, o_coefs, o_peaks = oracle(ref, pics, begins, 64, "fft", s)
+    assert np.array_equal(peaks, o_peaks)
+    assert np.abs(offs - o_offs).max() <= tol
+    assert np.allclose(coefs, o_coefs, rtol=1e-5 if precision == "float" else 1e-11,
+                       atol=1e-6 * np.abs(o_coefs).max())
+
+
+@pytest.mark.parametrize("precision,tol", [("double", 1e-9), ("float", 1e-3)])
+def test_fused_radius16(data512, precision, tol):
+    # 32 x 32 ROIs: 64-point transforms
+    from emida_gb300 import synth
+    ref, pics = data512
+    _, begins = synth.roi_grid(512, 6, 16, margin=30)
+    offs, _, peaks = run(ref, pics, begins, 32, "fft", 3, precision, "fused")
+    o_offs, _, o_peaks = oracle(ref, pics, begins, 32, "fft", 3)
+    assert np.array_equal(peaks, o_peaks)
+    assert np.abs(offs - o_offs).max() <= tol
+
+
+def test_fused_equals_plain_peaks_and_border_rois(data512):
+    # ROIs touching every border and with x not a multiple of 8 (TMA x rounding)
+    ref, pics = data512
+    begins = np.array([(0, 0), (448, 0), (0, 448), (448, 448), (3, 5), (101, 77), (447, 13)],
+                      dtype=np.uint32)
+    for precision in ("float", "double"):
+        f = run(ref, pics, begins, 64, "fft", 3, precision, "fused")
+        p = run(ref, pics, begins, 64, "fft", 3, precision, "plain")
+        o = oracle(ref, pics, begins, 64, "fft", 3)
+        assert np.array_equal(f[2], o[2]) and np.array_equal(p[2], o[2])
+        tol = 1e-3 if precision == "float" else 1e-9
+        assert np.abs(f[0] - o[0]).max() <= tol and np.abs(p[0] - o[0]).max() <= tol
+
+
+def test_width_not_multiple_of_8_uses_plain_loads():
+    from emida_gb300 import synth
+    ref = synth.reference_pattern((300, 260), seed=5)
+    pics, _ = synth.deformed_patterns((300, 260), 5, 2)
+    begins = np.array([(0, 0), (236, 196), (117, 61)], dtype=np.uint32)
+    f = run(ref, pics, begins, 64, "fft", 5, "float", "fused")
+    o = oracle(ref, pics, begins, 64, "fft", 5)
+    assert np.array_equal(f[2], o[2])
+    assert np.abs(f[0] - o[0]).max() <= 1e-3
+
+
+def test_constant_roi_gives_nan_like_reference():
+    # A flat ROI: zero map, peak at index 0, singular fit -> NaN offsets
+    # (the reference prints them normalised, src/process_files.hpp:249-253)
+    ref = np.full((256, 256), 1000, dtype=np.uint16)
+    pics = np.full((1, 256, 256), 1000, dtype=np.uint16)
+    begins = np.array([(10, 10)], dtype=np.uint32)
+    for mode in ("plain", "fused"):
+        offs, _, peaks = run(ref, pics, begins, 64, "fft", 3, "float", mode)
+        assert peaks[0] == 0
+        assert np.isnan(offs).all()
+
+
+def test_brute_small_cross_window(data512):
+    # --crosssize smaller than 2*slice-1 (src/args_parser.cpp:192-201)
+    from emida_gb300 import synth
+    ref, pics = data512
+    _, begins = synth.roi_grid(512, 3, 32, margin=40)
+    for cross in ((15, 15), (9, 13)):
+        offs, _, peaks = run(ref, pics[:1], begins, 64, "brute", 3, "double", "plain", cross)
+        o_offs, _, o_peaks = oracle(ref, pics[:1], begins, 64, "brute", 3, cross)
+        assert np.array_equal(peaks, o_peaks)
+        assert np.array_equal(offs, o_offs)
+
+
+def test_repeatable(data512):
+    from emida_gb300 import synth
+    ref, pics = data512
+    _, begins = synth.roi_grid(512, 4, 32, margin=40)
+    a = run(ref, pics, begins, 64, "fft", 5, "float", "fused")
+    b = run(ref, pics, begins, 64, "fft", 5, "float", "fused")
+    assert all(np.array_equal(x, y) for x, y in zip(a, b))
