@@ -13,6 +13,7 @@ REPO = os.path.dirname(HERE)
 CSRC = os.path.join(HERE, "csrc")
 OBJ = os.path.join(HERE, "_build")
 LIB = os.path.join(HERE, "libemida_gb.so")
+CLI = os.path.join(HERE, "bin", "emida")
 SOURCES = ["fused.cu", "staged.cu", "capi.cu"]
 HEADERS = ["common.cuh", "fft.cuh", "device_fit.cuh", "fused.cuh", "staged.cuh"]
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
@@ -56,9 +57,27 @@ def build(verbose=False, extra=()):
         r = subprocess.run(cmd, capture_output=True, text=True)
         if r.returncode != 0:
             raise RuntimeError(f"link failed:\n{r.stdout}\n{r.stderr}")
+    build_cli()
     if verbose:
-        print("built", LIB)
+        print("built", LIB, "and", CLI)
     return LIB
+
+
+def build_cli():
+    """The `emida` command line (emida_gb300/cli), linked against the library."""
+    src = os.path.join(HERE, "cli", "main.cpp")
+    deps = [src, os.path.join(HERE, "cli", "tiff.hpp"), LIB,
+            os.path.join(REPO, "include", "emida_gb", "gpu_offset.hpp")]
+    if not _stale(CLI, deps):
+        return CLI
+    os.makedirs(os.path.dirname(CLI), exist_ok=True)
+    cxx = shutil.which("g++") or "c++"
+    cmd = [cxx, "-O2", "-std=c++17", "-pthread", "-I" + os.path.join(REPO, "include"), src, "-o", CLI,
+           "-L" + HERE, "-lemida_gb", "-Wl,-rpath,$ORIGIN/.."]
+    r = subprocess.run(cmd, capture_output=True, text=True)
+    if r.returncode != 0:
+        raise RuntimeError(f"CLI build failed:\n{r.stdout}\n{r.stderr}")
+    return CLI
 
 
 if __name__ == "__main__":

@@ -298,7 +298,8 @@ int run_fused(emida_gb_handle *h, const void *pics, uint32_t pats, void *maxes, 
     a.twiddles = h->d_tw_row;
     a.lstsq = h->d_lstsq;
     a.fitsize = h->p.fitsize;
-    a.offsets = offsets;
+    // the fused kernel always writes offsets; offsets_core passes none
+    a.offsets = offsets ? offsets : h->d_offsets;
     a.coefs = coefs;
     a.maxes = maxes;
     a.neigh = neigh;

@@ -125,9 +125,12 @@ template <int DIR, typename C> struct rdft<1, DIR, C> {
 // Exchange position of A'[t][k1]: 8*k1 + ((t + k1) & 7), chosen so that both
 // the writes (fixed k1) and the reads (fixed t) of the eight lanes fall in
 // eight different rows / slots.
+// tw: the inter-pass twiddles of this direction laid out [k1][lane]:
+// tw[8*k1 + t] = W_N^{t*k1} (exp(-2 pi i t k1 / N) forward, its conjugate
+// inverse), so the eight lanes of a group read eight consecutive slots.
 template <int N, int DIR, bool HALF_INPUT, typename T, typename Line>
 __device__ __forceinline__ void group_fft(cplx<T> *v, int t, const Line &line,
-                                          const cplx<T> *__restrict__ tw /* W_N^j, forward */)
+                                          const cplx<T> *__restrict__ tw)
 {
     using C = cplx<T>;
     constexpr int E = N / 8;
@@ -136,13 +139,8 @@ __device__ __forceinline__ void group_fft(cplx<T> *v, int t, const Line &line,
         rdft<E, DIR, C>::run_half(v);
     else
         rdft<E, DIR, C>::run(v);
-    // twiddle W_N^{t*k1}
 #pragma unroll
-    for (int k1 = 1; k1 < E; ++k1) {
-        C w = tw[t * k1];
-        if (DIR > 0) w = cconj(w);
-        v[k1] = (t == 0) ? v[k1] : cmul(v[k1], w);
-    }
+    for (int k1 = 1; k1 < E; ++k1) v[k1] = cmul(v[k1], tw[8 * k1 + t]);
     __syncwarp();
 #pragma unroll
     for (int k1 = 0; k1 < E; ++k1) *line(8 * k1 + ((t + k1) & 7)) = v[k1];

@@ -109,8 +109,8 @@ __device__ __forceinline__ void better(T &bv, uint32_t &bi, T v, uint32_t i)
 }  // namespace
 
 template <int N, typename T, typename IN>
-__global__ void __launch_bounds__(2 * N, sizeof(T) == 4 ? 2 : 1) fused_fft_kernel(const fused_args a,
-                                                          const __grid_constant__ CUtensorMap tmap)
+__global__ void __launch_bounds__(2 * N, sizeof(T) == 4 ? 2 : 1)
+    fused_fft_kernel(const fused_args a, const __grid_constant__ CUtensorMap tmap)
 {
     using C = cplx<T>;
     constexpr int H = N / 2;           // ROI side
@@ -120,32 +120,53 @@ __global__ void __launch_bounds__(2 * N, sizeof(T) == 4 ? 2 : 1) fused_fft_kerne
     constexpr int GROUPS = THREADS / 8;
     constexpr int WARPS = THREADS / 32;
     constexpr int TW = H + 8;          // uint16 tile row (TMA box width)
+    constexpr bool U16 = sizeof(IN) == 2;
 
     extern __shared__ __align__(1024) unsigned char smem[];
     C *S = reinterpret_cast<C *>(smem);
-    C *tw = S + N * SL;
-    T *hx = reinterpret_cast<T *>(tw + N);
+    C *twf = S + N * SL;               // [E][8] forward inter-pass twiddles
+    C *twi = twf + 8 * E;              // [E][8] inverse
+    T *hx = reinterpret_cast<T *>(twi + 8 * E);
     T *hy = hx + H;
     T *red_v = hy + H;
     uint32_t *red_i = reinterpret_cast<uint32_t *>(red_v + 32);
     double *red_s = reinterpret_cast<double *>(red_i + 32);  // 8-aligned: counts are even
     double *nb = red_s + 32;                                 // 81 neighbours
-    double *cf = nb + 81;                                    // 6 coefficients (+1 pad)
+    double *cf = nb + 81;                                    // 6 coefficients (+pad)
     uint64_t *bar = reinterpret_cast<uint64_t *>(cf + 8);
-    unsigned char *tile = reinterpret_cast<unsigned char *>(S + H * SL);
+    // uint16 ROIs: a tile of their own (128-byte aligned), refilled by TMA for
+    // the next pair while this pair is in its column and inverse passes.
+    // FP64 ROIs: staged in the spectrum's upper half, unused until the columns.
+    uint16_t *t16 = reinterpret_cast<uint16_t *>(
+        (reinterpret_cast<uintptr_t>(bar + 2) + 127) & ~(uintptr_t)127);
+    double *t64 = reinterpret_cast<double *>(S + H * SL);
 
     const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
     const int t = lane & 7, g = tid >> 3;
 
     const C *gtw = reinterpret_cast<const C *>(a.twiddles);
-    for (int i = tid; i < N; i += THREADS) tw[i] = gtw[i];
+    for (int i = tid; i < 8 * E; i += THREADS) {
+        const C w = gtw[(i & 7) * (i >> 3)];  // W_N^{t k1}, t = i & 7, k1 = i >> 3
+        twf[i] = w;
+        twi[i] = cconj(w);
+    }
     const T *ghann = reinterpret_cast<const T *>(a.hann);
     for (int i = tid; i < 2 * H; i += THREADS) hx[i] = ghann[i];  // hx then hy
+    const bool tma = U16 && a.use_tma;
     if (tid == 0) {
         mbar_init(bar, 1);
         fence_proxy_async();
     }
     __syncthreads();
+
+    auto issue_tile = [&](uint32_t pair) {
+        const uint32_t pic = pair / a.n_rois;
+        const uint2 b = a.begins[pair % a.n_rois];
+        fence_proxy_async();
+        mbar_expect_tx(bar, TW * H * 2);
+        tma_load_3d(t16, &tmap, (int)(b.x & ~7u), (int)b.y, (int)pic, bar);
+    };
+    if (tma && tid == 0 && blockIdx.x < a.n_pairs) issue_tile(blockIdx.x);
 
     const int s = a.fitsize, s2 = s * s;
     uint32_t iter = 0;
@@ -155,17 +176,9 @@ __global__ void __launch_bounds__(2 * N, sizeof(T) == 4 ? 2 : 1) fused_fft_kerne
 
         // ---- gather the ROI and sum it (sum.cu:109-158) -------------------
         T mean;
-        int xo = 0;
-        if constexpr (sizeof(IN) == 2) {
-            const int x0 = (int)(beg.x & ~7u);
-            xo = (int)beg.x - x0;
-            uint16_t *t16 = reinterpret_cast<uint16_t *>(tile);
-            if (a.use_tma) {
-                if (tid == 0) {
-                    fence_proxy_async();
-                    mbar_expect_tx(bar, TW * H * 2);
-                    tma_load_3d(tile, &tmap, x0, (int)beg.y, (int)pic, bar);
-                }
+        const int xo = U16 ? (int)(beg.x & 7u) : 0;
+        if constexpr (U16) {
+            if (tma) {
                 if (!mbar_wait(bar, iter & 1)) {
                     if (tid == 0) atomicOr(a.err, DEV_ERR_TMA_TIMEOUT);
                     return;
@@ -189,7 +202,6 @@ __global__ void __launch_bounds__(2 * N, sizeof(T) == 4 ? 2 : 1) fused_fft_kerne
             for (int w = 0; w < WARPS; ++w) total += red_i[w];
             mean = (T)total / (T)(H * H);
         } else {
-            double *t64 = reinterpret_cast<double *>(tile);
             const double *src = reinterpret_cast<const double *>(a.pics) +
                                 (size_t)pic * a.src_w * a.src_h + (size_t)beg.y * a.src_w + beg.x;
             double acc = 0;
@@ -216,12 +228,10 @@ __global__ void __launch_bounds__(2 * N, sizeof(T) == 4 ? 2 : 1) fused_fft_kerne
             for (int m = 0; m < E / 2; ++m) {
                 const int x = t + 8 * m;
                 T pa, pb;
-                if constexpr (sizeof(IN) == 2) {
-                    const uint16_t *t16 = reinterpret_cast<const uint16_t *>(tile);
+                if constexpr (U16) {
                     pa = (T)t16[ra * TW + xo + x];
                     pb = (T)t16[rb * TW + xo + x];
                 } else {
-                    const double *t64 = reinterpret_cast<const double *>(tile);
                     pa = (T)t64[ra * H + x];
                     pb = (T)t64[rb * H + x];
                 }
@@ -232,7 +242,7 @@ __global__ void __launch_bounds__(2 * N, sizeof(T) == 4 ? 2 : 1) fused_fft_kerne
                 v[m] = cmake<C>(pa, pb);
             }
             row_line<N, C> line{S, ra};
-            group_fft<N, -1, true, T>(v, t, line, tw);
+            group_fft<N, -1, true, T>(v, t, line, twf);
             const int partner = (lane & ~7) | ((8 - t) & 7);
 #pragma unroll
             for (int j = 0; j < E / 2; ++j) {
@@ -252,6 +262,8 @@ __global__ void __launch_bounds__(2 * N, sizeof(T) == 4 ? 2 : 1) fused_fft_kerne
             }
         }
         __syncthreads();
+        // the tile is free: fetch the next pair's ROI behind the remaining passes
+        if (tma && tid == 0 && pair + gridDim.x < a.n_pairs) issue_tile(pair + gridDim.x);
 
         // ---- columns: forward FFT, conj product, inverse FFT --------------
         const C *R = reinterpret_cast<const C *>(a.ref_spec) + (size_t)roi * (SL + 1) * N;
@@ -262,7 +274,7 @@ __global__ void __launch_bounds__(2 * N, sizeof(T) == 4 ? 2 : 1) fused_fft_kerne
 #pragma unroll
             for (int m = 0; m < E / 2; ++m) v[m] = *sp<N>(S, t + 8 * m, c);
             col_line<N, C> line{S, c};
-            group_fft<N, -1, true, T>(v, t, line, tw);
+            group_fft<N, -1, true, T>(v, t, line, twf);
             const C *Rc = R + (size_t)c * N;
             if (warp == 0 && rnd == 0) {
                 // This warp holds column 0, whose slot packs the DC and Nyquist
@@ -292,13 +304,15 @@ __global__ void __launch_bounds__(2 * N, sizeof(T) == 4 ? 2 : 1) fused_fft_kerne
 #pragma unroll
                 for (int j = 0; j < E; ++j) v[j] = cmulc(v[j], __ldg(Rc + t + 8 * j));
             }
-            group_fft<N, +1, false, T>(v, t, line, tw);
+            group_fft<N, +1, false, T>(v, t, line, twi);
 #pragma unroll
             for (int j = 0; j < E; ++j) *sp<N>(S, t + 8 * j, c) = v[j];
         }
         __syncthreads();
 
         // ---- inverse rows: pairs of half spectra -> two real rows ---------
+        // Each lane scans its values in increasing map index, so a strict '>'
+        // keeps the first maximum; lanes merge with the index tie-break.
         T bv = neg_inf<T>();
         uint32_t bi = 0xffffffffu;
 #pragma unroll 1
@@ -318,14 +332,24 @@ __global__ void __launch_bounds__(2 * N, sizeof(T) == 4 ? 2 : 1) fused_fft_kerne
                 }
             }
             row_line<N, C> line{S, ra};
-            group_fft<N, +1, false, T>(v, t, line, tw);
+            group_fft<N, +1, false, T>(v, t, line, twi);
 #pragma unroll
             for (int j = 0; j < E; ++j) {
                 const int x = t + 8 * j;
                 reinterpret_cast<T *>(sp<N>(S, ra, x >> 1))[x & 1] = v[j].x;
+                if (v[j].x > bv) {
+                    bv = v[j].x;
+                    bi = (uint32_t)(ra * N + x);
+                }
+            }
+#pragma unroll
+            for (int j = 0; j < E; ++j) {
+                const int x = t + 8 * j;
                 reinterpret_cast<T *>(sp<N>(S, rb, x >> 1))[x & 1] = v[j].y;
-                better(bv, bi, v[j].x, (uint32_t)(ra * N + x));
-                better(bv, bi, v[j].y, (uint32_t)(rb * N + x));
+                if (v[j].y > bv) {
+                    bv = v[j].y;
+                    bi = (uint32_t)(rb * N + x);
+                }
             }
         }
 
@@ -384,12 +408,14 @@ size_t fused_smem_bytes()
 {
     using C = cplx<T>;
     size_t b = (size_t)N * (N / 2) * sizeof(C);  // spectrum
-    b += N * sizeof(C);                          // twiddles
+    b += 2 * (size_t)N * sizeof(C);              // forward and inverse twiddles
     b += N * sizeof(T);                          // hx, hy
     b += 32 * sizeof(T) + 32 * sizeof(uint32_t); // argmax scratch
     b = (b + 7) & ~(size_t)7;
     b += (32 + 81 + 8) * sizeof(double);         // sums, neighbours, coefs
     b += 16;                                     // mbarrier
+    b = (b + 127) & ~(size_t)127;
+    b += (size_t)(N / 2) * (N / 2 + 8) * 2;      // uint16 ROI tile
     return b;
 }
 

@@ -195,8 +195,55 @@ static void fft_rec(const double *x, size_t xs, double *X, uint32_t n, int sign,
     }
 }
 
+/* Iterative radix-2 decimation in time for power-of-two n, twiddles computed
+ * with cos/sin per length and cached per thread. */
+static _Thread_local double *tw_cache = NULL;
+static _Thread_local uint32_t tw_n = 0;
+
+static void fft_pow2(double *a, uint32_t n, int sign)
+{
+    if (tw_n != n) {
+        free(tw_cache);
+        tw_cache = (double *)malloc(sizeof(double) * n);
+        for (uint32_t k = 0; k < n / 2; ++k) {
+            tw_cache[2 * k] = cos(2 * EO_PI * (double)k / (double)n);
+            tw_cache[2 * k + 1] = sin(2 * EO_PI * (double)k / (double)n);
+        }
+        tw_n = n;
+    }
+    for (uint32_t i = 1, j = 0; i < n; ++i) {
+        uint32_t bit = n >> 1;
+        for (; j & bit; bit >>= 1) j ^= bit;
+        j ^= bit;
+        if (i < j) {
+            double t0 = a[2 * i], t1 = a[2 * i + 1];
+            a[2 * i] = a[2 * j];
+            a[2 * i + 1] = a[2 * j + 1];
+            a[2 * j] = t0;
+            a[2 * j + 1] = t1;
+        }
+    }
+    for (uint32_t len = 2; len <= n; len <<= 1) {
+        const uint32_t half = len / 2, step = n / len;
+        for (uint32_t i = 0; i < n; i += len)
+            for (uint32_t k = 0; k < half; ++k) {
+                const double c = tw_cache[2 * (k * step)], s = sign * tw_cache[2 * (k * step) + 1];
+                double *u = a + 2 * (i + k), *v = a + 2 * (i + k + half);
+                const double vr = v[0] * c - v[1] * s, vi = v[0] * s + v[1] * c;
+                v[0] = u[0] - vr;
+                v[1] = u[1] - vi;
+                u[0] += vr;
+                u[1] += vi;
+            }
+    }
+}
+
 void eo_fft_c2c(double *data, uint32_t n, int inverse)
 {
+    if (n >= 2 && (n & (n - 1)) == 0) {
+        fft_pow2(data, n, inverse ? 1 : -1);
+        return;
+    }
     /* scratch: each recursion level needs n complex values; depth <= log2(n)+1 */
     size_t levels = 1;
     for (uint32_t t = n; t > 1; t /= 2) ++levels;
