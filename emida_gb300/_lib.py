@@ -57,6 +57,8 @@ SIGNATURES = {
     "emida_gb_offsets_core": [_VP, _U32, _VP, _VP],
     "emida_gb_finalize": [_VP, _VP, _VP, _DP, _DP],
     "emida_gb_get_offset": [_VP, _VP, _DP, _DP, _U32P],
+    "emida_gb_submit": [_VP, _VP, _U32, ctypes.POINTER(ctypes.c_uint64)],
+    "emida_gb_wait": [_VP, ctypes.c_uint64, _DP, _DP, _U32P],
     "emida_gb_run_device": [_VP, _VP, _U32, _VP, _VP, _VP, _VP, _VP],
     "emida_gb_resolved_mode": [_VP],
     "emida_gb_stream": [_VP],

@@ -194,6 +194,25 @@ class GpuOffset:
             return offs, coefs, peaks
         return offs, coefs
 
+    def submit(self, pic, patterns=None):
+        """Queue one batch (host memory, pinned for overlap) and return a ticket.
+        `pic` must stay alive and unchanged until wait(ticket)."""
+        patterns = self.batch_size if patterns is None else int(patterns)
+        t = ctypes.c_uint64()
+        ptr = pic if isinstance(pic, int) else pic.ctypes.data
+        _lib.call("emida_gb_submit", self._h, ctypes.c_void_p(ptr), patterns, ctypes.byref(t))
+        return t.value
+
+    def wait(self, ticket, patterns=None, with_peaks=False):
+        """Results of a submitted batch: (offsets, coefs[, peaks])."""
+        n = (self.batch_size if patterns is None else int(patterns)) * len(self.begins)
+        offs = np.zeros((n, 2))
+        coefs = np.zeros((n, 6))
+        peaks = np.zeros(n, dtype=np.uint32)
+        _lib.call("emida_gb_wait", self._h, ctypes.c_uint64(ticket), _dptr(offs), _dptr(coefs),
+                  peaks.ctypes.data_as(ctypes.POINTER(ctypes.c_uint32)))
+        return (offs, coefs, peaks) if with_peaks else (offs, coefs)
+
     def run_device(self, dev_pics, patterns, dev_offsets, dev_coefs=None, dev_maxes=None,
                    dev_neigh=None, stream=None):
         """Device-resident form: any number of patterns, no synchronisation."""

@@ -194,6 +194,19 @@ struct emida_gb_handle {
     bool ref_set = false;
     std::mutex mu;
     std::vector<void *> allocs;
+    // submit/wait ring: one slot per input buffer
+    struct slot {
+        double *d_offsets = nullptr, *d_coefs = nullptr;
+        void *d_maxes = nullptr;
+        double *h_offsets = nullptr, *h_coefs = nullptr;
+        void *h_maxes = nullptr;
+        cudaEvent_t h2d = nullptr, comp = nullptr, done = nullptr;
+        uint64_t ticket = 0;
+        uint32_t patterns = 0;
+        bool busy = false;
+    };
+    std::vector<slot> ring;
+    uint64_t next_ticket = 1;
 
     int alloc(void **ptr, size_t bytes, bool zero = false)
     {
@@ -626,6 +639,87 @@ int emida_gb_get_offset(emida_gb_handle *h, const void *batch, double *offsets, 
     return EMIDA_GB_OK;
 }
 
+static int ring_init(emida_gb_handle *h)
+{
+    if (!h->ring.empty()) return EMIDA_GB_OK;
+    std::vector<emida_gb_handle::slot> ring(h->d_in.size());
+    for (auto &r : ring) {
+        CKS(h->alloc((void **)&r.d_offsets, 2 * sizeof(double) * h->N));
+        CKS(h->alloc((void **)&r.d_coefs, 6 * sizeof(double) * h->N));
+        CKS(h->alloc(&r.d_maxes, h->di_elem * h->N));
+        CK(cudaMallocHost((void **)&r.h_offsets, 2 * sizeof(double) * h->N));
+        CK(cudaMallocHost((void **)&r.h_coefs, 6 * sizeof(double) * h->N));
+        CK(cudaMallocHost(&r.h_maxes, h->di_elem * h->N));
+        CK(cudaEventCreateWithFlags(&r.h2d, cudaEventDisableTiming));
+        CK(cudaEventCreateWithFlags(&r.comp, cudaEventDisableTiming));
+        CK(cudaEventCreateWithFlags(&r.done, cudaEventDisableTiming));
+    }
+    h->ring = std::move(ring);
+    return EMIDA_GB_OK;
+}
+
+int emida_gb_submit(emida_gb_handle *h, const void *batch, uint32_t patterns, uint64_t *ticket)
+{
+    if (!h || !batch || !ticket) return fail(EMIDA_GB_INVALID_ARGUMENT, "null argument");
+    if (patterns == 0 || patterns > h->B)
+        return fail(EMIDA_GB_INVALID_ARGUMENT, "patterns must be in [1, batch_size]");
+    if (!h->ref_set) return fail(EMIDA_GB_INVALID_ARGUMENT, "reference pattern not set");
+    std::lock_guard<std::mutex> lk(h->mu);
+    CKS(ring_init(h));
+    const uint64_t t = h->next_ticket;
+    const size_t si = t % h->ring.size();
+    auto &r = h->ring[si];
+    if (r.busy)
+        return fail(EMIDA_GB_INVALID_ARGUMENT, "all %zu slots in flight: wait for ticket %llu first",
+                    h->ring.size(), (unsigned long long)r.ticket);
+    const size_t bytes = (size_t)h->src.x * h->src.y * h->in_elem * patterns;
+    // the input buffer is free once the slot's previous computation ran
+    CK(cudaStreamWaitEvent(h->in_stream, r.comp, 0));
+    CK(cudaMemcpyAsync(h->d_in[si], batch, bytes, cudaMemcpyHostToDevice, h->in_stream));
+    CK(cudaEventRecord(r.h2d, h->in_stream));
+    CK(cudaStreamWaitEvent(h->comp, r.h2d, 0));
+    CKS(run_any(h, h->d_in[si], patterns, r.d_maxes, h->d_neigh, r.d_offsets, r.d_coefs, h->comp));
+    CK(cudaEventRecord(r.comp, h->comp));
+    CK(cudaStreamWaitEvent(h->out_stream, r.comp, 0));
+    const size_t n = (size_t)patterns * h->S;
+    CK(cudaMemcpyAsync(r.h_offsets, r.d_offsets, 2 * sizeof(double) * n, cudaMemcpyDeviceToHost, h->out_stream));
+    CK(cudaMemcpyAsync(r.h_coefs, r.d_coefs, 6 * sizeof(double) * n, cudaMemcpyDeviceToHost, h->out_stream));
+    CK(cudaMemcpyAsync(r.h_maxes, r.d_maxes, h->di_elem * n, cudaMemcpyDeviceToHost, h->out_stream));
+    CK(cudaEventRecord(r.done, h->out_stream));
+    r.busy = true;
+    r.ticket = t;
+    r.patterns = patterns;
+    h->next_ticket = t + 1;
+    *ticket = t;
+    return EMIDA_GB_OK;
+}
+
+int emida_gb_wait(emida_gb_handle *h, uint64_t ticket, double *offsets, double *coefs,
+                  uint32_t *peaks)
+{
+    if (!h || !offsets) return fail(EMIDA_GB_INVALID_ARGUMENT, "null argument");
+    emida_gb_handle::slot *r = nullptr;
+    {
+        std::lock_guard<std::mutex> lk(h->mu);
+        if (h->ring.empty()) return fail(EMIDA_GB_INVALID_ARGUMENT, "nothing submitted");
+        r = &h->ring[ticket % h->ring.size()];
+        if (!r->busy || r->ticket != ticket)
+            return fail(EMIDA_GB_INVALID_ARGUMENT, "unknown ticket %llu", (unsigned long long)ticket);
+    }
+    CK(cudaEventSynchronize(r->done));
+    CKS(check_device_error(h));
+    const size_t n = (size_t)r->patterns * h->S;
+    std::memcpy(offsets, r->h_offsets, 2 * sizeof(double) * n);
+    if (coefs) std::memcpy(coefs, r->h_coefs, 6 * sizeof(double) * n);
+    if (peaks)
+        for (size_t i = 0; i < n; ++i)
+            peaks[i] = h->dbl ? reinterpret_cast<const data_index<double> *>(r->h_maxes)[i].index
+                              : reinterpret_cast<const data_index<float> *>(r->h_maxes)[i].index;
+    std::lock_guard<std::mutex> lk(h->mu);
+    r->busy = false;
+    return EMIDA_GB_OK;
+}
+
 int emida_gb_run_device(emida_gb_handle *h, const void *dev_patterns, uint32_t patterns,
                         double *dev_offsets, double *dev_coefs, void *dev_maxes, void *dev_neigh,
                         void *stream)
@@ -670,6 +764,13 @@ void emida_gb_destroy(emida_gb_handle *h)
     if (h->comp) cudaStreamSynchronize(h->comp);
     if (h->in_stream) cudaStreamSynchronize(h->in_stream);
     if (h->out_stream) cudaStreamSynchronize(h->out_stream);
+    for (auto &r : h->ring) {
+        if (r.h_offsets) cudaFreeHost(r.h_offsets);
+        if (r.h_coefs) cudaFreeHost(r.h_coefs);
+        if (r.h_maxes) cudaFreeHost(r.h_maxes);
+        for (cudaEvent_t e : {r.h2d, r.comp, r.done})
+            if (e) cudaEventDestroy(e);
+    }
     for (void *p : h->allocs) cudaFree(p);
     for (auto e : h->in_done)
         if (e) cudaEventDestroy(e);

@@ -3,17 +3,12 @@
 // These replace the cuFFT R2C/C2R calls of the reference
 // (src/gpu_offset.hpp:171-183, :303-316, src/cufft_helpers.hpp:105-155).
 //
-// One 1-D transform of length N = 8*E is carried by a group of 8 consecutive
-// lanes of one warp ("fft group"); each lane holds E complex values.  Lane t of
-// the group holds element n = t + 8*j in register j, both before and after the
-// transform (the scheme is self-sorting), so transforms chain without
-// permutations.  The only exchange goes through shared memory inside the
-// group's own 128-slot line and needs __syncwarp only.
-//
-//   n = t + 8m, k = k1 + E*k2:
-//   X[k1 + E k2] = sum_t W8^{t k2} * W_N^{t k1} * sum_m x[t + 8m] W_E^{m k1}
-//   pass 1: E-point DFT over m in registers; twiddle W_N^{t k1};
-//   exchange; pass 2: E/8 8-point DFTs over t.
+// One 1-D transform of length N = G*E is carried by a group of G = 4 or 8
+// consecutive lanes of one warp ("fft group"); each lane holds E complex
+// values.  Lane t of the group holds element n = t + G*j in register j, both
+// before and after the transform (the scheme is self-sorting), so transforms
+// chain without permutations.  The only exchange goes through shared memory
+// inside the group's own line of N slots and needs __syncwarp only.
 #pragma once
 
 #include "common.cuh"
@@ -46,40 +41,54 @@ template <typename C> __device__ __forceinline__ C cmulc(C a, C b)
 }
 template <typename C> __device__ __forceinline__ C cconj(C a) { return cmake<C>(a.x, -a.y); }
 
-// cos/sin(2*pi*k/16), k = 0..7, correctly rounded decimal expansions.
-__device__ __forceinline__ double c16(int k)
+// cos(2*pi*k/48) for k = 0..12 (first quadrant), 25 significant digits; the
+// other quadrants follow by symmetry.  Every register DFT length used here
+// (2, 3, 4, 6, 8, 12, 16, 24) divides 48.
+__device__ __forceinline__ double c48(int k)
 {
-    switch (k & 15) {
-    case 0: return 1.0;
-    case 1: return 0.92387953251128675613;
-    case 2: return 0.70710678118654752440;
-    case 3: return 0.38268343236508977173;
-    case 4: return 0.0;
-    case 5: return -0.38268343236508977173;
-    case 6: return -0.70710678118654752440;
-    case 7: return -0.92387953251128675613;
-    default: return -c16(k - 8);
+    k %= 48;
+    if (k < 0) k += 48;
+    if (k > 24) k = 48 - k;            // cos(-x) = cos(x)
+    const bool neg = k > 12;
+    if (neg) k = 24 - k;               // cos(pi - x) = -cos(x)
+    double v;
+    switch (k) {
+    case 0: v = 1.0; break;
+    case 1: v = 0.9914448613738104111445575; break;
+    case 2: v = 0.9659258262890682867497432; break;
+    case 3: v = 0.9238795325112867561281832; break;
+    case 4: v = 0.8660254037844386467637232; break;
+    case 5: v = 0.7933533402912351645797770; break;
+    case 6: v = 0.7071067811865475244008444; break;
+    case 7: v = 0.6087614290087206394160975; break;
+    case 8: v = 0.5; break;
+    case 9: v = 0.3826834323650897717284600; break;
+    case 10: v = 0.2588190451025207623488988; break;
+    case 11: v = 0.1305261922200515915484062; break;
+    default: v = 0.0; break;
     }
+    return neg ? -v : v;
 }
-__device__ __forceinline__ double s16(int k) { return c16(k - 4); }
+__device__ __forceinline__ double s48(int k) { return c48(k - 12); }
 
-// Multiply a by W_16^k, W = exp(DIR * 2 pi i / 16), DIR = -1 forward, +1 inverse.
-// k is a compile-time constant after unrolling; exact cases are special-cased.
-template <int DIR, typename C> __device__ __forceinline__ C tw16(C a, int k)
+// Multiply a by W_L^n, W = exp(DIR * 2 pi i / L), DIR = -1 forward, +1 inverse,
+// L dividing 48.  n and L are compile-time constants after unrolling; the
+// quarter turns are exact.
+template <int DIR, typename C> __device__ __forceinline__ C twl(C a, int n, int L)
 {
     using T = decltype(C::x);
-    k &= 15;
+    int k = (n * (48 / L)) % 48;
     if (k == 0) return a;
-    if (k == 8) return cmake<C>(-a.x, -a.y);
-    if (k == 4) return DIR < 0 ? cmake<C>(a.y, -a.x) : cmake<C>(-a.y, a.x);
-    if (k == 12) return DIR < 0 ? cmake<C>(-a.y, a.x) : cmake<C>(a.y, -a.x);
-    T c = (T)c16(k);
-    T s = (T)(DIR * s16(k));
+    if (k == 24) return cmake<C>(-a.x, -a.y);
+    if (k == 12) return DIR < 0 ? cmake<C>(a.y, -a.x) : cmake<C>(-a.y, a.x);
+    if (k == 36) return DIR < 0 ? cmake<C>(-a.y, a.x) : cmake<C>(a.y, -a.x);
+    T c = (T)c48(k);
+    T s = (T)(DIR * s48(k));
     return cmake<C>(a.x * c - a.y * s, a.x * s + a.y * c);
 }
 
-// In-register DFT of length L (power of two <= 16), natural order in and out.
-// Radix-2 decimation in frequency, recursively.
+// In-register DFT of length L (2^a * 3^b <= 24), natural order in and out:
+// radix-2 decimation in frequency down to length 3 or 1.
 template <int L, int DIR, typename C> struct rdft {
     static __device__ __forceinline__ void run(C *a)
     {
@@ -87,7 +96,7 @@ template <int L, int DIR, typename C> struct rdft {
 #pragma unroll
         for (int n = 0; n < L / 2; ++n) {
             e[n] = cadd(a[n], a[n + L / 2]);
-            o[n] = tw16<DIR>(csub(a[n], a[n + L / 2]), n * (16 / L));
+            o[n] = twl<DIR>(csub(a[n], a[n + L / 2]), n, L);
         }
         rdft<L / 2, DIR, C>::run(e);
         rdft<L / 2, DIR, C>::run(o);
@@ -104,7 +113,7 @@ template <int L, int DIR, typename C> struct rdft {
 #pragma unroll
         for (int n = 0; n < L / 2; ++n) {
             e[n] = a[n];
-            o[n] = tw16<DIR>(a[n], n * (16 / L));
+            o[n] = twl<DIR>(a[n], n, L);
         }
         rdft<L / 2, DIR, C>::run(e);
         rdft<L / 2, DIR, C>::run(o);
@@ -119,41 +128,59 @@ template <int DIR, typename C> struct rdft<1, DIR, C> {
     static __device__ __forceinline__ void run(C *) {}
     static __device__ __forceinline__ void run_half(C *) {}
 };
+// Length 3: X0 = a0 + s, X1,2 = a0 - s/2 +- DIR i (sqrt(3)/2) d, s = a1 + a2, d = a1 - a2.
+template <int DIR, typename C> struct rdft<3, DIR, C> {
+    static __device__ __forceinline__ void run(C *a)
+    {
+        using T = decltype(C::x);
+        const T h = (T)0.8660254037844386467637232;  // sqrt(3)/2
+        C s = cadd(a[1], a[2]), d = csub(a[1], a[2]);
+        C t = cmake<C>(a[0].x - (T)0.5 * s.x, a[0].y - (T)0.5 * s.y);
+        // DIR * i * h * d
+        C r = cmake<C>(-(T)DIR * h * d.y, (T)DIR * h * d.x);
+        a[0] = cadd(a[0], s);
+        a[1] = cadd(t, r);
+        a[2] = csub(t, r);
+    }
+};
 
-// Shared-memory view of one transform line of N complex slots.  The group
-// passes an accessor that maps a line position (0..N-1) to a slot pointer.
-// Exchange position of A'[t][k1]: 8*k1 + ((t + k1) & 7), chosen so that both
-// the writes (fixed k1) and the reads (fixed t) of the eight lanes fall in
-// eight different rows / slots.
-// tw: the inter-pass twiddles of this direction laid out [k1][lane]:
-// tw[8*k1 + t] = W_N^{t*k1} (exp(-2 pi i t k1 / N) forward, its conjugate
-// inverse), so the eight lanes of a group read eight consecutive slots.
-template <int N, int DIR, bool HALF_INPUT, typename T, typename Line>
+// One 1-D transform of length N = G * E carried by G consecutive lanes
+// (G = 4 or 8), E values per lane; lane t holds element n = t + G*j in
+// register j before and after (self-sorting):
+//   n = t + G m, k = k1 + E k2:
+//   X[k1 + E k2] = sum_t W_G^{t k2} W_N^{t k1} sum_m x[t + G m] W_E^{m k1}.
+// Pass 1 is an E-point DFT over m in registers, then the twiddle, then an
+// exchange through the group's own line of N slots (shared memory, reached
+// through `line`), then pass 2: E/G G-point DFTs over t.  The exchange slot of
+// A'[t][k1] is G*k1 + ((t + k1) mod G): the G lanes' writes (fixed k1) and reads
+// (fixed t) fall in G different rows or slots.
+// tw: this direction's inter-pass twiddles laid out [k1][lane],
+// tw[G*k1 + t] = W_N^{t*k1}.
+template <int N, int DIR, bool HALF_INPUT, typename T, int G, typename Line>
 __device__ __forceinline__ void group_fft(cplx<T> *v, int t, const Line &line,
                                           const cplx<T> *__restrict__ tw)
 {
     using C = cplx<T>;
-    constexpr int E = N / 8;
-    static_assert(E == 8 || E == 16, "group_fft supports N = 64 and N = 128");
+    constexpr int E = N / G;
+    static_assert(E % G == 0, "pass 2 needs a whole number of G-point DFTs per lane");
     if (HALF_INPUT)
         rdft<E, DIR, C>::run_half(v);
     else
         rdft<E, DIR, C>::run(v);
 #pragma unroll
-    for (int k1 = 1; k1 < E; ++k1) v[k1] = cmul(v[k1], tw[8 * k1 + t]);
+    for (int k1 = 1; k1 < E; ++k1) v[k1] = cmul(v[k1], tw[G * k1 + t]);
     __syncwarp();
 #pragma unroll
-    for (int k1 = 0; k1 < E; ++k1) *line(8 * k1 + ((t + k1) & 7)) = v[k1];
+    for (int k1 = 0; k1 < E; ++k1) *line(G * k1 + ((t + k1) & (G - 1))) = v[k1];
     __syncwarp();
-    // pass 2: for i in [0, E/8): k1 = t + 8 i, DFT over the 8 lanes' values
 #pragma unroll
-    for (int i = 0; i < E / 8; ++i) {
-        C a[8];
+    for (int i = 0; i < E / G; ++i) {
+        C a[G];
 #pragma unroll
-        for (int s = 0; s < 8; ++s) a[s] = *line(8 * t + 64 * i + ((s + t) & 7));
-        rdft<8, DIR, C>::run(a);
+        for (int s = 0; s < G; ++s) a[s] = *line(G * t + G * G * i + ((s + t) & (G - 1)));
+        rdft<G, DIR, C>::run(a);
 #pragma unroll
-        for (int k2 = 0; k2 < 8; ++k2) v[i + (E / 8) * k2] = a[k2];
+        for (int k2 = 0; k2 < G; ++k2) v[i + (E / G) * k2] = a[k2];
     }
     __syncwarp();
 }

@@ -24,10 +24,17 @@ namespace emida_gb {
 
 namespace {
 
+// Slot swizzle: XOR the slot with f(row & 7), f = 2 * (row bits 0, 2, 1 as bits
+// 0, 1, 2).  64-bit accesses are served per half-warp (two 8-lane groups).
+// A group's column access (8 rows t + 8m of one column) gets 8 distinct even
+// slot offsets, and its neighbour group's column (c + 1) the odd ones.  Two
+// groups' row accesses (rows 8w + 2g' + e) land in different 8-slot halves.
+// So every half-warp access covers 16 distinct 8-byte slots.
 template <int N, typename C>
 __device__ __forceinline__ C *sp(C *S, int row, int slot)
 {
-    return S + row * (N / 2) + (slot ^ (((row >> 1) & 3) << 2));
+    const int f = ((row & 1) << 1) | (row & 4) | ((row & 2) << 2);
+    return S + row * (N / 2) + (slot ^ f);
 }
 
 template <int N, typename C> struct col_line {
@@ -108,6 +115,36 @@ __device__ __forceinline__ void better(T &bv, uint32_t &bi, T v, uint32_t i)
 
 }  // namespace
 
+// Lane l fits buffered pair l: coefficients as sequential FP64 dot products
+// and the closed-form extremum (src/subpixel_max.hpp:14-29, :76-97), offset
+// (src/gpu_offset.hpp:296-297).  One warp instruction serves up to 32 pairs,
+// which matters on a part whose FP64 pipe is narrow.
+template <typename T>
+__device__ __forceinline__ void fit_batch(const fused_args &a, const T *fbuf, const uint32_t *fmeta,
+                                          const T *fval, int count, int lane, uint32_t cross)
+{
+    if (lane < count) {
+        const int s = a.fitsize, s2 = s * s;
+        double v[81];
+        for (int k = 0; k < s2; ++k) v[k] = (double)fbuf[lane * 81 + k];
+        double c[6];
+        for (int j = 0; j < 6; ++j) c[j] = fit_coef(a.lstsq, v, s, j);
+        const uint32_t pair = fmeta[4 * lane], mx = fmeta[4 * lane + 1], my = fmeta[4 * lane + 2];
+        double ox, oy;
+        fit_offsets(c, mx, my, cross, cross, s, ox, oy);
+        a.offsets[2 * (size_t)pair] = ox;
+        a.offsets[2 * (size_t)pair + 1] = oy;
+        if (a.coefs)
+            for (int j = 0; j < 6; ++j) a.coefs[(size_t)pair * 6 + j] = c[j];
+        if (a.maxes) {
+            data_index<T> *mi = reinterpret_cast<data_index<T> *>(a.maxes) + pair;
+            mi->data = fval[lane];
+            mi->index = fmeta[4 * lane + 3];
+        }
+    }
+    __syncwarp();
+}
+
 template <int N, typename T, typename IN>
 __global__ void __launch_bounds__(2 * N, sizeof(T) == 4 ? 2 : 1)
     fused_fft_kernel(const fused_args a, const __grid_constant__ CUtensorMap tmap)
@@ -132,13 +169,17 @@ __global__ void __launch_bounds__(2 * N, sizeof(T) == 4 ? 2 : 1)
     uint32_t *red_i = reinterpret_cast<uint32_t *>(red_v + 32);
     double *red_s = reinterpret_cast<double *>(red_i + 32);  // 8-aligned: counts are even
     double *nb = red_s + 32;                                 // 81 neighbours
-    double *cf = nb + 81;                                    // 6 coefficients (+pad)
+    double *cf = nb + 81;                                    // (spare)
     uint64_t *bar = reinterpret_cast<uint64_t *>(cf + 8);
+    // neighbourhoods of up to 32 pairs wait here for one lane-per-pair fit
+    T *fbuf = reinterpret_cast<T *>(bar + 2);                // [32][81]
+    uint32_t *fmeta = reinterpret_cast<uint32_t *>(fbuf + 32 * 81);  // [32][4]
+    T *fval = reinterpret_cast<T *>(fmeta + 32 * 4);         // [32]
     // uint16 ROIs: a tile of their own (128-byte aligned), refilled by TMA for
     // the next pair while this pair is in its column and inverse passes.
     // FP64 ROIs: staged in the spectrum's upper half, unused until the columns.
     uint16_t *t16 = reinterpret_cast<uint16_t *>(
-        (reinterpret_cast<uintptr_t>(bar + 2) + 127) & ~(uintptr_t)127);
+        (reinterpret_cast<uintptr_t>(fval + 32) + 127) & ~(uintptr_t)127);
     double *t64 = reinterpret_cast<double *>(S + H * SL);
 
     const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
@@ -366,7 +407,7 @@ __global__ void __launch_bounds__(2 * N, sizeof(T) == 4 ? 2 : 1)
         }
         __syncthreads();
 
-        // ---- neighbourhood, FP64 fit, offsets (warp 0) --------------------
+        // ---- neighbourhood (warp 0); the FP64 fit runs every 32 pairs ----
         if (warp == 0) {
             T pv = red_v[0];
             uint32_t pk = red_i[0];
@@ -374,30 +415,26 @@ __global__ void __launch_bounds__(2 * N, sizeof(T) == 4 ? 2 : 1)
             if (pk >= (uint32_t)(N * N)) pk = 0;
             uint32_t mx, my;
             shift_pos(pk, POLICY_FFT, N - 1, N - 1, mx, my);
+            const uint32_t slot = iter & 31;
             for (int l = lane; l < s2; l += 32) {
                 uint32_t x, y;
                 neighbour_pos(mx, my, l % s, l / s, s, N - 1, N - 1, x, y);
                 const uint32_t q = (uint32_t)policy_index(POLICY_FFT, x, y, N - 1, N - 1);
                 const uint32_t qy = q / N, qx = q % N;
                 T val = reinterpret_cast<T *>(sp<N>(S, qy, qx >> 1))[qx & 1];
-                nb[l] = (double)val;
+                fbuf[slot * 81 + l] = val;
                 if (a.neigh) reinterpret_cast<T *>(a.neigh)[(size_t)pair * s2 + l] = val;
             }
-            __syncwarp();
-            if (lane < 6) cf[lane] = fit_coef(a.lstsq, nb, s, lane);
-            __syncwarp();
-            if (lane < 6 && a.coefs) a.coefs[(size_t)pair * 6 + lane] = cf[lane];
             if (lane == 0) {
-                double ox, oy;
-                fit_offsets(cf, mx, my, N - 1, N - 1, s, ox, oy);
-                a.offsets[2 * (size_t)pair] = ox;
-                a.offsets[2 * (size_t)pair + 1] = oy;
-                if (a.maxes) {
-                    data_index<T> *mi = reinterpret_cast<data_index<T> *>(a.maxes) + pair;
-                    mi->data = pv;
-                    mi->index = pk;
-                }
+                fmeta[4 * slot] = pair;
+                fmeta[4 * slot + 1] = mx;
+                fmeta[4 * slot + 2] = my;
+                fmeta[4 * slot + 3] = pk;
+                fval[slot] = pv;
             }
+            __syncwarp();
+            const bool last = pair + gridDim.x >= a.n_pairs;
+            if (slot == 31 || last) fit_batch<T>(a, fbuf, fmeta, fval, (int)slot + 1, lane, N - 1);
         }
         __syncthreads();
     }
@@ -412,8 +449,9 @@ size_t fused_smem_bytes()
     b += N * sizeof(T);                          // hx, hy
     b += 32 * sizeof(T) + 32 * sizeof(uint32_t); // argmax scratch
     b = (b + 7) & ~(size_t)7;
-    b += (32 + 81 + 8) * sizeof(double);         // sums, neighbours, coefs
+    b += (32 + 81 + 8) * sizeof(double);         // sums, neighbours, spare
     b += 16;                                     // mbarrier
+    b += 32 * 81 * sizeof(T) + 32 * 4 * 4 + 32 * sizeof(T);  // fit buffer
     b = (b + 127) & ~(size_t)127;
     b += (size_t)(N / 2) * (N / 2 + 8) * 2;      // uint16 ROI tile
     return b;

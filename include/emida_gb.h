@@ -92,6 +92,20 @@ int emida_gb_finalize(emida_gb_handle *h, const void *maxes, const void *neigh,
 int emida_gb_get_offset(emida_gb_handle *h, const void *batch, double *offsets, double *coefs,
                         uint32_t *peaks);
 
+/* Pipelined form of get_offset for a stream of batches: queues the copy of
+ * `patterns` (<= batch_size) patterns from host memory (pinned for overlap) on
+ * the input stream, the path on the compute stream and the copy of the results
+ * on the output stream, and returns a ticket at once.  Up to in_buffers batches
+ * may be in flight; a ticket must be waited for before its slot is reused
+ * (EMIDA_GB_INVALID_ARGUMENT otherwise).  The host batch must stay untouched
+ * until its ticket is waited for.  The process_files pipeline of the reference
+ * (src/process_files.hpp:98-233) does the same with threads and two streams. */
+int emida_gb_submit(emida_gb_handle *h, const void *batch, uint32_t patterns, uint64_t *ticket);
+/* Waits for a ticket and copies its offsets [patterns*n_rois][2], coefficients
+ * [..][6] and argmax indices [..] to the host (coefs, peaks may be NULL). */
+int emida_gb_wait(emida_gb_handle *h, uint64_t ticket, double *offsets, double *coefs,
+                  uint32_t *peaks);
+
 /* Device-resident form for pipelines and benchmarks: `patterns` whole
  * patterns (any count, not limited to batch_size) already in device memory,
  * results to device memory, all on `stream` (NULL: the handle's compute

@@ -86,3 +86,29 @@ def test_pipeline_api_matches_get_offset():
             assert np.array_equal(offs, ref_offs)
             assert np.array_equal(coefs, ref_coefs)
         go.close()
+
+
+def test_submit_wait_pipeline_matches_get_offset():
+    # several batches in flight on the three streams; partial last batch
+    from emida_gb300 import EmidaError, GpuOffset
+    pic, temp = golden_pair()
+    begins = slice_begins(256, 64, 32)
+    batches = [np.stack([pic, pic[::-1, ::-1].copy(), pic[:, ::-1].copy()]) for _ in range(4)]
+    for mode in ("plain", "fused"):
+        go = GpuOffset((256, 256), begins, (64, 64), (127, 127), 3, "fft", 5, 3, "float",
+                       np.float64, mode)
+        go.allocate_memory(temp)
+        ref_offs, ref_coefs, ref_peaks = go.get_offset(batches[0], with_peaks=True)
+        tickets = [go.submit(b) for b in batches[:3]]
+        with pytest.raises(EmidaError, match="in flight"):
+            go.submit(batches[3])
+        for t in tickets:
+            offs, coefs, peaks = go.wait(t, with_peaks=True)
+            assert np.array_equal(offs, ref_offs) and np.array_equal(coefs, ref_coefs)
+            assert np.array_equal(peaks, ref_peaks)
+        with pytest.raises(EmidaError, match="unknown ticket"):
+            go.wait(tickets[0])
+        t = go.submit(batches[3], patterns=2)
+        offs, _ = go.wait(t, patterns=2)
+        assert np.array_equal(offs, ref_offs[:2 * len(begins)])
+        go.close()

@@ -44,13 +44,18 @@ def well_posed(coefs, s):
     return (x >= 0) & (x <= s - 1) & (y >= 0) & (y <= s - 1)
 
 
-def assert_offsets(offs, o_offs, o_coefs, s, tol):
+def assert_offsets(offs, coefs, o_offs, o_coefs, s, tol):
+    """Offsets within `tol` for well-posed fits.  For extrapolated fits the
+    closed-form extremum amplifies rounding without bound, so there the fitted
+    coefficients are compared instead, at the precision's relative level."""
     ok = well_posed(o_coefs, s)
     assert ok.mean() > 0.5  # the tolerance check below must not be vacuous
     err = np.abs(offs - o_offs).max(axis=1)
     assert err[ok].max() <= tol, err[ok].max()
-    if (~ok).any():  # extrapolated fits: loose relative bound only
-        assert (err[~ok] <= np.maximum(0.1, 1e-2 * np.abs(o_offs[~ok]).max(axis=1))).all()
+    if (~ok).any():
+        rel = 1e-5 if tol >= 1e-6 else 1e-11
+        scale = np.abs(o_coefs[~ok]).max(axis=1, keepdims=True)
+        assert (np.abs(coefs[~ok] - o_coefs[~ok]) <= rel * scale).all()
 
 
 def oracle(ref, pics, begins, slice_, policy, s, cross=None):
@@ -82,7 +87,7 @@ def test_fft_vs_oracle(data512, mode, precision, tol, s):
     offs, coefs, peaks = run(ref, pics, begins, 64, "fft", s, precision, mode)
     o_offs, o_coefs, o_peaks = oracle(ref, pics, begins, 64, "fft", s)
     assert np.array_equal(peaks, o_peaks)
-    assert_offsets(offs, o_offs, o_coefs, s, tol)
+    assert_offsets(offs, coefs, o_offs, o_coefs, s, tol)
     assert np.allclose(coefs, o_coefs, rtol=1e-5 if precision == "float" else 1e-11,
                        atol=1e-6 * np.abs(o_coefs).max())
 
@@ -93,10 +98,10 @@ def test_fused_radius16(data512, precision, tol):
     from emida_gb300 import synth
     ref, pics = data512
     _, begins = synth.roi_grid(512, 6, 16, margin=30)
-    offs, _, peaks = run(ref, pics, begins, 32, "fft", 3, precision, "fused")
+    offs, coefs, peaks = run(ref, pics, begins, 32, "fft", 3, precision, "fused")
     o_offs, o_coefs, o_peaks = oracle(ref, pics, begins, 32, "fft", 3)
     assert np.array_equal(peaks, o_peaks)
-    assert_offsets(offs, o_offs, o_coefs, 3, tol)
+    assert_offsets(offs, coefs, o_offs, o_coefs, 3, tol)
 
 
 def test_fused_equals_plain_peaks_and_border_rois(data512):
@@ -110,8 +115,8 @@ def test_fused_equals_plain_peaks_and_border_rois(data512):
         o = oracle(ref, pics, begins, 64, "fft", 3)
         assert np.array_equal(f[2], o[2]) and np.array_equal(p[2], o[2])
         tol = 1e-3 if precision == "float" else 1e-9
-        assert_offsets(f[0], o[0], o[1], 3, tol)
-        assert_offsets(p[0], o[0], o[1], 3, tol)
+        assert_offsets(f[0], f[1], o[0], o[1], 3, tol)
+        assert_offsets(p[0], p[1], o[0], o[1], 3, tol)
 
 
 def test_width_not_multiple_of_8_uses_plain_loads():
@@ -122,7 +127,7 @@ def test_width_not_multiple_of_8_uses_plain_loads():
     f = run(ref, pics, begins, 64, "fft", 5, "float", "fused")
     o = oracle(ref, pics, begins, 64, "fft", 5)
     assert np.array_equal(f[2], o[2])
-    assert_offsets(f[0], o[0], o[1], 5, 1e-3)
+    assert_offsets(f[0], f[1], o[0], o[1], 5, 1e-3)
 
 
 def test_constant_roi_gives_nan_like_reference():
