@@ -60,6 +60,13 @@ SIGNATURES = {
     "emida_gb_submit": [_VP, _VP, _U32, ctypes.POINTER(ctypes.c_uint64)],
     "emida_gb_wait": [_VP, ctypes.c_uint64, _DP, _DP, _U32P],
     "emida_gb_run_device": [_VP, _VP, _U32, _VP, _VP, _VP, _VP, _VP],
+    "emida_gb_multi_create": [_U32, _U32, _I32, ctypes.POINTER(_VP)],
+    "emida_gb_multi_add_layout": [_VP, _U32P, _U32, _U32, _I32, _VP, _U32P],
+    "emida_gb_multi_count": [_VP, _U32, _U32P, ctypes.POINTER(ctypes.c_uint64)],
+    "emida_gb_multi_run": [_VP, _VP, _U32, _U32P, _VP, _VP, _VP, _I32],
+    "emida_gb_multi_synchronize": [_VP],
+    "emida_gb_multi_autotune": [_VP, _VP, _U32, _U32P, _VP, ctypes.c_char_p, _SZ],
+    "emida_gb_multi_destroy": [_VP],
     "emida_gb_resolved_mode": [_VP],
     "emida_gb_stream": [_VP],
     "emida_gb_launches_per_run": [_VP],
@@ -93,6 +100,7 @@ _RESTYPES = {
     "emida_gb_version": ctypes.c_char_p,
     "emida_gb_stream": _VP,
     "emida_gb_destroy": None,
+    "emida_gb_multi_destroy": None,
 }
 
 

@@ -282,3 +282,71 @@ def device_count():
     n = ctypes.c_int()
     st = _lib.lib().emida_gb_device_count(ctypes.byref(n))
     return n.value if st == 0 else 0
+
+
+class MultiLayout:
+    """Batches whose patterns use different ROI layouts (emida_gb_multi_*).
+
+    add_layout() registers one layout (ROI top-left corners, ROI side, fit
+    size) with its uint16 reference pattern and returns its id; run() processes
+    device-resident uint16 patterns, pattern p with layout layout_of[p].  The
+    results are flat in pattern order, then ROI order within the layout.
+    """
+
+    def __init__(self, src_size, precision="float"):
+        self.src_size = tuple(int(v) for v in src_size)
+        self.precision = _precision(precision)
+        self.T = np.float64 if self.precision == DOUBLE else np.float32
+        self.data_index = DATA_INDEX_F64 if self.precision == DOUBLE else DATA_INDEX_F32
+        h = ctypes.c_void_p()
+        _lib.call("emida_gb_multi_create", self.src_size[0], self.src_size[1], self.precision,
+                  ctypes.byref(h))
+        self._h = h
+        self.layouts = []
+
+    def add_layout(self, begins, side, fitsize, ref):
+        begins = np.ascontiguousarray(np.asarray(begins, dtype=np.uint32).reshape(-1, 2))
+        ref = np.ascontiguousarray(ref, dtype=np.uint16)
+        lid = ctypes.c_uint32()
+        _lib.call("emida_gb_multi_add_layout", self._h,
+                  begins.ctypes.data_as(ctypes.POINTER(ctypes.c_uint32)), len(begins), int(side),
+                  int(fitsize), _ptr(ref), ctypes.byref(lid))
+        self.layouts.append((begins, int(side), int(fitsize)))
+        return lid.value
+
+    def count(self, layout_of):
+        lo = np.ascontiguousarray(layout_of, dtype=np.uint32)
+        t = ctypes.c_uint64()
+        _lib.call("emida_gb_multi_count", self._h, len(lo),
+                  lo.ctypes.data_as(ctypes.POINTER(ctypes.c_uint32)), ctypes.byref(t))
+        return t.value
+
+    def run(self, dev_pics, layout_of, dev_offsets, dev_coefs=None, dev_maxes=None, graph=True):
+        self._lo = np.ascontiguousarray(layout_of, dtype=np.uint32)
+
+        def vp(b):
+            return None if b is None else b.ptr
+        _lib.call("emida_gb_multi_run", self._h, vp(dev_pics), len(self._lo),
+                  self._lo.ctypes.data_as(ctypes.POINTER(ctypes.c_uint32)), vp(dev_offsets),
+                  vp(dev_coefs), vp(dev_maxes), int(bool(graph)))
+
+    def synchronize(self):
+        _lib.call("emida_gb_multi_synchronize", self._h)
+
+    def autotune(self, dev_pics, layout_of, dev_offsets):
+        lo = np.ascontiguousarray(layout_of, dtype=np.uint32)
+        buf = ctypes.create_string_buffer(4096)
+        _lib.call("emida_gb_multi_autotune", self._h, dev_pics.ptr, len(lo),
+                  lo.ctypes.data_as(ctypes.POINTER(ctypes.c_uint32)), dev_offsets.ptr, buf, 4096)
+        return buf.value.decode()
+
+    def close(self):
+        if getattr(self, "_h", None) is not None and self._h.value:
+            _lib.lib().emida_gb_multi_destroy(self._h)
+        self._h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass

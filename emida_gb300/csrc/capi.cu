@@ -12,16 +12,18 @@
 #include <string>
 #include <vector>
 
-#include "../../include/emida_gb.h"
 #include "fft.cuh"
-#include "fused.cuh"
-#include "staged.cuh"
+#include "handle.cuh"
 
 using namespace emida_gb;
+using namespace emida_gb::host;
 
 namespace {
-
 thread_local std::string g_last_error;
+}  // namespace
+
+namespace emida_gb {
+namespace host {
 
 int fail(int code, const char *fmt, ...)
 {
@@ -34,21 +36,10 @@ int fail(int code, const char *fmt, ...)
     return code;
 }
 
-#define CK(expr)                                                                            \
-    do {                                                                                    \
-        cudaError_t e_ = (expr);                                                            \
-        if (e_ != cudaSuccess)                                                              \
-            return fail(e_ == cudaErrorMemoryAllocation ? EMIDA_GB_OUT_OF_MEMORY             \
-                                                        : EMIDA_GB_CUDA_ERROR,               \
-                        "CUDA error %d (%s) at %s:%d: %s", (int)e_, cudaGetErrorString(e_),  \
-                        __FILE__, __LINE__, #expr);                                         \
-    } while (0)
+}  // namespace host
+}  // namespace emida_gb
 
-#define CKS(expr)                                                                           \
-    do {                                                                                    \
-        int s_ = (expr);                                                                    \
-        if (s_ != EMIDA_GB_OK) return s_;                                                   \
-    } while (0)
+namespace {
 
 // ---- exact least-squares matrix ---------------------------------------------
 // (A^T A)^-1 A^T for A rows (1, x, y, x^2, xy, y^2), x fastest
@@ -90,7 +81,9 @@ q128 q_mul(q128 a, q128 b)
 q128 q_sub(q128 a, q128 b) { return q_make(a.n * b.d - b.n * a.d, a.d * b.d); }
 q128 q_div(q128 a, q128 b) { return q_mul(a, q_make(b.d, b.n)); }
 
-int lstsq_matrix(int s, double *out)
+}  // namespace
+
+int emida_gb::host::lstsq_matrix(int s, double *out)
 {
     if (s != 3 && s != 5 && s != 7 && s != 9) return -1;
     const int np = s * s, cols = 6 + np;
@@ -128,6 +121,8 @@ int lstsq_matrix(int s, double *out)
     return 0;
 }
 
+namespace {
+
 // Host fit in the reference's operation order (src/subpixel_max.hpp:14-29, :76-97).
 // This file is built with -ffp-contract=off, so each product and sum rounds once.
 void host_fit(const double *mat, const double *v, int s, double *coef, double &x, double &y)
@@ -143,12 +138,10 @@ void host_fit(const double *mat, const double *v, int s, double *coef, double &x
     x = (-e * y - b) / (2 * d);
 }
 
+}  // namespace
+
 // cuTensorMapEncodeTiled through the runtime's driver entry point (no libcuda link).
-using encode_fn = CUresult (*)(CUtensorMap *, CUtensorMapDataType, cuuint32_t, void *,
-                               const cuuint64_t *, const cuuint64_t *, const cuuint32_t *,
-                               const cuuint32_t *, CUtensorMapInterleave, CUtensorMapSwizzle,
-                               CUtensorMapL2promotion, CUtensorMapFloatOOBfill);
-encode_fn get_encoder()
+encode_fn emida_gb::host::get_encoder()
 {
     static encode_fn fn = nullptr;
     static std::once_flag once;
@@ -163,62 +156,7 @@ encode_fn get_encoder()
     return fn;
 }
 
-}  // namespace
 
-struct emida_gb_handle {
-    emida_gb_params p{};
-    std::vector<uint32_t> begins;
-    int device = 0;
-    bool dbl = false, in_f64 = false, fft = false;
-    int mode = EMIDA_GB_MODE_PLAIN;
-    size2 src{}, slice{}, cross{};
-    uint32_t S = 0, B = 0, N = 0;
-    uint32_t w2 = 0, h2 = 0, half = 0;
-    size_t in_elem = 2, t_elem = 4, c_elem = 8, di_elem = 8;
-    cudaStream_t in_stream = nullptr, out_stream = nullptr, comp = nullptr;
-    std::vector<cudaEvent_t> in_done;
-    cudaEvent_t comp_done = nullptr;
-    std::vector<void *> d_in;
-    std::atomic<uint32_t> in_next{0};
-    void *d_ref_in = nullptr;
-    uint2 *d_begins = nullptr;
-    void *d_hann = nullptr, *d_hann_fused = nullptr;
-    void *d_sums_ref = nullptr, *d_sums = nullptr;
-    void *d_ref_prep = nullptr, *d_prep = nullptr;
-    void *d_ref_spec = nullptr, *d_ref_spec_cm = nullptr, *d_spec = nullptr;
-    void *d_map = nullptr, *d_maxes = nullptr, *d_neigh = nullptr;
-    double *d_offsets = nullptr, *d_coefs = nullptr, *d_lstsq = nullptr;
-    void *d_tw_row = nullptr, *d_tw_col = nullptr;
-    uint32_t *d_err = nullptr;
-    std::vector<double> lstsq;
-    bool ref_set = false;
-    std::mutex mu;
-    std::vector<void *> allocs;
-    // submit/wait ring: one slot per input buffer
-    struct slot {
-        double *d_offsets = nullptr, *d_coefs = nullptr;
-        void *d_maxes = nullptr;
-        double *h_offsets = nullptr, *h_coefs = nullptr;
-        void *h_maxes = nullptr;
-        cudaEvent_t h2d = nullptr, comp = nullptr, done = nullptr;
-        uint64_t ticket = 0;
-        uint32_t patterns = 0;
-        bool busy = false;
-    };
-    std::vector<slot> ring;
-    uint64_t next_ticket = 1;
-
-    int alloc(void **ptr, size_t bytes, bool zero = false)
-    {
-        if (bytes == 0) bytes = 16;
-        CK(cudaMalloc(ptr, bytes));
-        allocs.push_back(*ptr);
-        if (zero) CK(cudaMemset(*ptr, 0, bytes));
-        return EMIDA_GB_OK;
-    }
-    uint32_t map_size() const { return fft ? w2 * h2 : cross.x * cross.y; }
-    size2 prep_size() const { return fft ? size2{w2, h2} : slice; }
-};
 
 namespace {
 
@@ -231,7 +169,9 @@ template <typename T> std::vector<T> hann_host(uint32_t n)
     return v;
 }
 
-int upload_hann(emida_gb_handle *h, void **dst, uint32_t nx, uint32_t ny)
+}  // namespace
+
+int emida_gb::host::upload_hann(emida_gb_handle *h, void **dst, uint32_t nx, uint32_t ny)
 {
     if (h->dbl) {
         auto x = hann_host<double>(nx), y = hann_host<double>(ny);
@@ -247,7 +187,7 @@ int upload_hann(emida_gb_handle *h, void **dst, uint32_t nx, uint32_t ny)
     return EMIDA_GB_OK;
 }
 
-int upload_twiddles(emida_gb_handle *h, void **dst, uint32_t n)
+int emida_gb::host::upload_twiddles(emida_gb_handle *h, void **dst, uint32_t n)
 {
     const double PI = 3.14159265358979323846;
     if (h->dbl) {
@@ -266,11 +206,14 @@ int upload_twiddles(emida_gb_handle *h, void **dst, uint32_t n)
     return EMIDA_GB_OK;
 }
 
-fft_tables tables(const emida_gb_handle *h) { return fft_tables{h->d_tw_row, h->d_tw_col, h->w2, h->h2}; }
+fft_tables emida_gb::host::tables(const emida_gb_handle *h)
+{
+    return fft_tables{h->d_tw_row, h->d_tw_col, h->w2, h->h2};
+}
 
 // The staged pipeline for `pats` patterns from `pics` (<= B patterns):
 // src/gpu_offset.hpp:234-278 stage by stage.
-int run_plain_chunk(emida_gb_handle *h, const void *pics, uint32_t pats, void *maxes, void *neigh,
+int emida_gb::host::run_plain_chunk(emida_gb_handle *h, const void *pics, uint32_t pats, void *maxes, void *neigh,
                     double *offsets, double *coefs, cudaStream_t st)
 {
     const uint32_t n = pats * h->S;
@@ -296,7 +239,7 @@ int run_plain_chunk(emida_gb_handle *h, const void *pics, uint32_t pats, void *m
     return EMIDA_GB_OK;
 }
 
-int run_fused(emida_gb_handle *h, const void *pics, uint32_t pats, void *maxes, void *neigh,
+int emida_gb::host::run_fused(emida_gb_handle *h, const void *pics, uint32_t pats, void *maxes, void *neigh,
               double *offsets, double *coefs, cudaStream_t st)
 {
     fused_args a{};
@@ -338,7 +281,7 @@ int run_fused(emida_gb_handle *h, const void *pics, uint32_t pats, void *maxes, 
     return EMIDA_GB_OK;
 }
 
-int run_any(emida_gb_handle *h, const void *pics, uint32_t pats, void *maxes, void *neigh,
+int emida_gb::host::run_any(emida_gb_handle *h, const void *pics, uint32_t pats, void *maxes, void *neigh,
             double *offsets, double *coefs, cudaStream_t st)
 {
     if (h->mode == EMIDA_GB_MODE_FUSED) return run_fused(h, pics, pats, maxes, neigh, offsets, coefs, st);
@@ -356,7 +299,7 @@ int run_any(emida_gb_handle *h, const void *pics, uint32_t pats, void *maxes, vo
     return EMIDA_GB_OK;
 }
 
-int check_device_error(emida_gb_handle *h)
+int emida_gb::host::check_device_error(emida_gb_handle *h)
 {
     uint32_t err = 0;
     CK(cudaMemcpy(&err, h->d_err, sizeof err, cudaMemcpyDeviceToHost));
@@ -367,6 +310,8 @@ int check_device_error(emida_gb_handle *h)
     }
     return EMIDA_GB_OK;
 }
+
+namespace {
 
 int validate(const emida_gb_params *p)
 {
@@ -455,10 +400,10 @@ int emida_gb_create(const emida_gb_params *p, emida_gb_handle **out)
     } else {
         h->cross = size2{p->cross_w, p->cross_h};
     }
-    const bool fusable = h->fft && fused_supported(h->w2);
+    const bool fusable = h->fft && fused_supported(h->w2, h->dbl);
     if (p->mode == EMIDA_GB_MODE_FUSED && !fusable) {
         delete h;
-        return fail(EMIDA_GB_UNSUPPORTED, "no fused kernel for this shape (FFT policy, 32x32 or 64x64 ROIs)");
+        return fail(EMIDA_GB_UNSUPPORTED, "no fused kernel for this shape (FFT policy; ROI side 32, 48, 64, or 96 in FP32)");
     }
     h->mode = (p->mode == EMIDA_GB_MODE_PLAIN || !fusable) ? EMIDA_GB_MODE_PLAIN : EMIDA_GB_MODE_FUSED;
 

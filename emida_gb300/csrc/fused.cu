@@ -47,7 +47,7 @@ template <int N, typename C> struct row_line {
     int a;
     __device__ __forceinline__ C *operator()(int q) const
     {
-        return sp<N>(S, a + (q >= N / 2 ? 1 : 0), q & (N / 2 - 1));
+        return q >= N / 2 ? sp<N>(S, a + 1, q - N / 2) : sp<N>(S, a, q);
     }
 };
 
@@ -115,6 +115,13 @@ __device__ __forceinline__ void better(T &bv, uint32_t &bi, T v, uint32_t i)
 
 }  // namespace
 
+// Resident CTAs per SM the register budget is sized for (shared memory allows
+// as many): FP32 128-point and 192-point transforms are register-heavy.
+__host__ __device__ constexpr int fused_min_blocks(int N, int tsize)
+{
+    return N == 192 ? 1 : N == 128 ? (tsize == 4 ? 2 : 1) : (tsize == 4 ? 4 : 2);
+}
+
 // Lane l fits buffered pair l: coefficients as sequential FP64 dot products
 // and the closed-form extremum (src/subpixel_max.hpp:14-29, :76-97), offset
 // (src/gpu_offset.hpp:296-297).  One warp instruction serves up to 32 pairs,
@@ -124,12 +131,14 @@ __device__ __forceinline__ void fit_batch(const fused_args &a, const T *fbuf, co
                                           const T *fval, int count, int lane, uint32_t cross)
 {
     if (lane < count) {
-        const int s = a.fitsize, s2 = s * s;
+        const uint32_t pair = fmeta[4 * lane], mxy = fmeta[4 * lane + 1], pks = fmeta[4 * lane + 2];
+        const uint32_t mx = mxy & 0xffffu, my = mxy >> 16;
+        const int s = (int)(pks >> 24), s2 = s * s;
+        const double *lstsq = a.items ? a.lstsq_all + lstsq_offset(s) : a.lstsq;
         double v[81];
         for (int k = 0; k < s2; ++k) v[k] = (double)fbuf[lane * 81 + k];
         double c[6];
-        for (int j = 0; j < 6; ++j) c[j] = fit_coef(a.lstsq, v, s, j);
-        const uint32_t pair = fmeta[4 * lane], mx = fmeta[4 * lane + 1], my = fmeta[4 * lane + 2];
+        for (int j = 0; j < 6; ++j) c[j] = fit_coef(lstsq, v, s, j);
         double ox, oy;
         fit_offsets(c, mx, my, cross, cross, s, ox, oy);
         a.offsets[2 * (size_t)pair] = ox;
@@ -139,55 +148,77 @@ __device__ __forceinline__ void fit_batch(const fused_args &a, const T *fbuf, co
         if (a.maxes) {
             data_index<T> *mi = reinterpret_cast<data_index<T> *>(a.maxes) + pair;
             mi->data = fval[lane];
-            mi->index = fmeta[4 * lane + 3];
+            mi->index = pks & 0xffffffu;
         }
     }
     __syncwarp();
 }
 
-template <int N, typename T, typename IN>
-__global__ void __launch_bounds__(2 * N, sizeof(T) == 4 ? 2 : 1)
+// Shared-memory layout of the fused kernel, in bytes from the (1024-aligned)
+// dynamic base.  The kernel and the launcher's size both come from here.
+template <int N, int G, typename T> struct fused_layout {
+    using C = cplx<T>;
+    static constexpr size_t up(size_t v, size_t a) { return (v + a - 1) / a * a; }
+    static constexpr size_t spectrum = 0;                                  // N x N/2 C
+    static constexpr size_t tw_fwd = spectrum + (size_t)N * (N / 2) * sizeof(C);
+    static constexpr size_t tw_inv = tw_fwd + (size_t)N * sizeof(C);      // G*E = N entries
+    static constexpr size_t hann = tw_inv + (size_t)N * sizeof(C);
+    static constexpr size_t red_val = hann + (size_t)N * sizeof(T);       // hx, hy
+    static constexpr size_t red_idx = red_val + 32 * sizeof(T);
+    static constexpr size_t red_sum = up(red_idx + 32 * sizeof(uint32_t), 8);
+    static constexpr size_t barrier = red_sum + 32 * sizeof(double);
+    static constexpr size_t fit_vals = barrier + 16;
+    static constexpr size_t fit_meta = up(fit_vals + 32 * 81 * sizeof(T), 4);
+    static constexpr size_t fit_peak = up(fit_meta + 32 * 4 * sizeof(uint32_t), sizeof(T));
+    static constexpr size_t tile = up(fit_peak + 32 * sizeof(T), 128);
+    static constexpr size_t bytes = tile + (size_t)(N / 2) * (N / 2 + 8) * sizeof(uint16_t);
+    static_assert(G * (N / G) == N, "group width must divide the transform length");
+    // the FP64-input ROI is staged in the spectrum's upper half
+    static_assert((size_t)(N / 2) * (N / 2) * sizeof(double) <=
+                      (size_t)(N / 2) * (N / 2) * sizeof(C), "FP64 tile must fit");
+};
+
+template <int N, int G, typename T, typename IN>
+__global__ void __launch_bounds__(N * G / 4, fused_min_blocks(N, sizeof(T)))
     fused_fft_kernel(const fused_args a, const __grid_constant__ CUtensorMap tmap)
 {
     using C = cplx<T>;
     constexpr int H = N / 2;           // ROI side
     constexpr int SL = N / 2;          // slots per spectrum row
-    constexpr int E = N / 8;           // elements per lane
-    constexpr int THREADS = 2 * N;
-    constexpr int GROUPS = THREADS / 8;
+    constexpr int E = N / G;           // elements per lane
+    constexpr int GROUPS = N / 4;      // one pair of ROI rows per group in the row pass
+    constexpr int THREADS = GROUPS * G;
     constexpr int WARPS = THREADS / 32;
     constexpr int TW = H + 8;          // uint16 tile row (TMA box width)
     constexpr bool U16 = sizeof(IN) == 2;
 
+    using L = fused_layout<N, G, T>;
     extern __shared__ __align__(1024) unsigned char smem[];
-    C *S = reinterpret_cast<C *>(smem);
-    C *twf = S + N * SL;               // [E][8] forward inter-pass twiddles
-    C *twi = twf + 8 * E;              // [E][8] inverse
-    T *hx = reinterpret_cast<T *>(twi + 8 * E);
+    C *S = reinterpret_cast<C *>(smem + L::spectrum);
+    C *twf = reinterpret_cast<C *>(smem + L::tw_fwd);   // [E][G] forward inter-pass twiddles
+    C *twi = reinterpret_cast<C *>(smem + L::tw_inv);   // [E][G] inverse
+    T *hx = reinterpret_cast<T *>(smem + L::hann);      // hx[H] then hy[H]
     T *hy = hx + H;
-    T *red_v = hy + H;
-    uint32_t *red_i = reinterpret_cast<uint32_t *>(red_v + 32);
-    double *red_s = reinterpret_cast<double *>(red_i + 32);  // 8-aligned: counts are even
-    double *nb = red_s + 32;                                 // 81 neighbours
-    double *cf = nb + 81;                                    // (spare)
-    uint64_t *bar = reinterpret_cast<uint64_t *>(cf + 8);
+    T *red_v = reinterpret_cast<T *>(smem + L::red_val);
+    uint32_t *red_i = reinterpret_cast<uint32_t *>(smem + L::red_idx);
+    double *red_s = reinterpret_cast<double *>(smem + L::red_sum);
+    uint64_t *bar = reinterpret_cast<uint64_t *>(smem + L::barrier);
     // neighbourhoods of up to 32 pairs wait here for one lane-per-pair fit
-    T *fbuf = reinterpret_cast<T *>(bar + 2);                // [32][81]
-    uint32_t *fmeta = reinterpret_cast<uint32_t *>(fbuf + 32 * 81);  // [32][4]
-    T *fval = reinterpret_cast<T *>(fmeta + 32 * 4);         // [32]
+    T *fbuf = reinterpret_cast<T *>(smem + L::fit_vals);            // [32][81]
+    uint32_t *fmeta = reinterpret_cast<uint32_t *>(smem + L::fit_meta);  // [32][4]
+    T *fval = reinterpret_cast<T *>(smem + L::fit_peak);            // [32]
     // uint16 ROIs: a tile of their own (128-byte aligned), refilled by TMA for
     // the next pair while this pair is in its column and inverse passes.
     // FP64 ROIs: staged in the spectrum's upper half, unused until the columns.
-    uint16_t *t16 = reinterpret_cast<uint16_t *>(
-        (reinterpret_cast<uintptr_t>(fval + 32) + 127) & ~(uintptr_t)127);
+    uint16_t *t16 = reinterpret_cast<uint16_t *>(smem + L::tile);
     double *t64 = reinterpret_cast<double *>(S + H * SL);
 
     const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
-    const int t = lane & 7, g = tid >> 3;
+    const int t = lane & (G - 1), g = tid / G;
 
     const C *gtw = reinterpret_cast<const C *>(a.twiddles);
-    for (int i = tid; i < 8 * E; i += THREADS) {
-        const C w = gtw[(i & 7) * (i >> 3)];  // W_N^{t k1}, t = i & 7, k1 = i >> 3
+    for (int i = tid; i < G * E; i += THREADS) {
+        const C w = gtw[(i % G) * (i / G)];  // W_N^{t k1}, t = i mod G, k1 = i / G
         twf[i] = w;
         twi[i] = cconj(w);
     }
@@ -200,19 +231,26 @@ __global__ void __launch_bounds__(2 * N, sizeof(T) == 4 ? 2 : 1)
     }
     __syncthreads();
 
+    // pair -> (pattern, ROI, output slot, fit size)
+    auto item = [&](uint32_t pair) -> uint4 {
+        if (a.items) return a.items[pair];
+        return make_uint4(pair / a.n_rois, pair % a.n_rois, pair, (uint32_t)a.fitsize);
+    };
     auto issue_tile = [&](uint32_t pair) {
-        const uint32_t pic = pair / a.n_rois;
-        const uint2 b = a.begins[pair % a.n_rois];
+        const uint4 it = item(pair);
+        const uint32_t pic = it.x;
+        const uint2 b = a.begins[it.y];
         fence_proxy_async();
         mbar_expect_tx(bar, TW * H * 2);
         tma_load_3d(t16, &tmap, (int)(b.x & ~7u), (int)b.y, (int)pic, bar);
     };
     if (tma && tid == 0 && blockIdx.x < a.n_pairs) issue_tile(blockIdx.x);
 
-    const int s = a.fitsize, s2 = s * s;
     uint32_t iter = 0;
     for (uint32_t pair = blockIdx.x; pair < a.n_pairs; pair += gridDim.x, ++iter) {
-        const uint32_t pic = pair / a.n_rois, roi = pair % a.n_rois;
+        const uint4 it = item(pair);
+        const uint32_t pic = it.x, roi = it.y, out = it.z;
+        const int s = (int)it.w, s2 = s * s;
         const uint2 beg = a.begins[roi];
 
         // ---- gather the ROI and sum it (sum.cu:109-158) -------------------
@@ -267,7 +305,7 @@ __global__ void __launch_bounds__(2 * N, sizeof(T) == 4 ? 2 : 1)
             C v[E];
 #pragma unroll
             for (int m = 0; m < E / 2; ++m) {
-                const int x = t + 8 * m;
+                const int x = t + G * m;
                 T pa, pb;
                 if constexpr (U16) {
                     pa = (T)t16[ra * TW + xo + x];
@@ -283,15 +321,15 @@ __global__ void __launch_bounds__(2 * N, sizeof(T) == 4 ? 2 : 1)
                 v[m] = cmake<C>(pa, pb);
             }
             row_line<N, C> line{S, ra};
-            group_fft<N, -1, true, T>(v, t, line, twf);
-            const int partner = (lane & ~7) | ((8 - t) & 7);
+            group_fft<N, -1, true, T, G>(v, t, line, twf);
+            const int partner = (lane & ~(G - 1)) | ((G - t) & (G - 1));
 #pragma unroll
             for (int j = 0; j < E / 2; ++j) {
-                C send = (t == 0) ? v[(E - j) & (E - 1)] : v[E - 1 - j];
+                C send = (t == 0) ? v[j == 0 ? 0 : E - j] : v[E - 1 - j];
                 C zm = cmake<C>(__shfl_sync(0xffffffffu, send.x, partner),
                                 __shfl_sync(0xffffffffu, send.y, partner));
                 C z = v[j];
-                const int k = t + 8 * j;
+                const int k = t + G * j;
                 if (k == 0) {
                     C zh = v[E / 2];
                     *sp<N>(S, ra, 0) = cmake<C>(z.x, zh.x);
@@ -313,9 +351,9 @@ __global__ void __launch_bounds__(2 * N, sizeof(T) == 4 ? 2 : 1)
             const int c = g + rnd * GROUPS;
             C v[E];
 #pragma unroll
-            for (int m = 0; m < E / 2; ++m) v[m] = *sp<N>(S, t + 8 * m, c);
+            for (int m = 0; m < E / 2; ++m) v[m] = *sp<N>(S, t + G * m, c);
             col_line<N, C> line{S, c};
-            group_fft<N, -1, true, T>(v, t, line, twf);
+            group_fft<N, -1, true, T, G>(v, t, line, twf);
             const C *Rc = R + (size_t)c * N;
             if (warp == 0 && rnd == 0) {
                 // This warp holds column 0, whose slot packs the DC and Nyquist
@@ -323,14 +361,14 @@ __global__ void __launch_bounds__(2 * N, sizeof(T) == 4 ? 2 : 1)
                 // half by its own reference column, repack.  The exchange goes
                 // through the warp's columns with full-warp syncs.
 #pragma unroll
-                for (int j = 0; j < E; ++j) *sp<N>(S, t + 8 * j, c) = v[j];
+                for (int j = 0; j < E; ++j) *sp<N>(S, t + G * j, c) = v[j];
                 __syncwarp();
 #pragma unroll
                 for (int j = 0; j < E; ++j) {
-                    const int ky = t + 8 * j;
+                    const int ky = t + G * j;
                     if (c == 0) {
                         C x = v[j];
-                        C xm = *sp<N>(S, (N - ky) & (N - 1), 0);
+                        C xm = *sp<N>(S, ky == 0 ? 0 : N - ky, 0);
                         C p0 = cmake<C>((x.x + xm.x) * (T)0.5, (x.y - xm.y) * (T)0.5);
                         C p64 = cmake<C>((x.y + xm.y) * (T)0.5, (xm.x - x.x) * (T)0.5);
                         C q0 = cmulc(p0, __ldg(R + ky));
@@ -343,11 +381,11 @@ __global__ void __launch_bounds__(2 * N, sizeof(T) == 4 ? 2 : 1)
                 __syncwarp();
             } else {
 #pragma unroll
-                for (int j = 0; j < E; ++j) v[j] = cmulc(v[j], __ldg(Rc + t + 8 * j));
+                for (int j = 0; j < E; ++j) v[j] = cmulc(v[j], __ldg(Rc + t + G * j));
             }
-            group_fft<N, +1, false, T>(v, t, line, twi);
+            group_fft<N, +1, false, T, G>(v, t, line, twi);
 #pragma unroll
-            for (int j = 0; j < E; ++j) *sp<N>(S, t + 8 * j, c) = v[j];
+            for (int j = 0; j < E; ++j) *sp<N>(S, t + G * j, c) = v[j];
         }
         __syncthreads();
 
@@ -362,7 +400,7 @@ __global__ void __launch_bounds__(2 * N, sizeof(T) == 4 ? 2 : 1)
             C v[E];
 #pragma unroll
             for (int j = 0; j < E; ++j) {
-                const int n = t + 8 * j;
+                const int n = t + G * j;
                 if (j < E / 2) {
                     C ga = *sp<N>(S, ra, n), gb = *sp<N>(S, rb, n);
                     v[j] = (n == 0) ? cmake<C>(ga.x, gb.x) : cmake<C>(ga.x - gb.y, ga.y + gb.x);
@@ -373,10 +411,10 @@ __global__ void __launch_bounds__(2 * N, sizeof(T) == 4 ? 2 : 1)
                 }
             }
             row_line<N, C> line{S, ra};
-            group_fft<N, +1, false, T>(v, t, line, twi);
+            group_fft<N, +1, false, T, G>(v, t, line, twi);
 #pragma unroll
             for (int j = 0; j < E; ++j) {
-                const int x = t + 8 * j;
+                const int x = t + G * j;
                 reinterpret_cast<T *>(sp<N>(S, ra, x >> 1))[x & 1] = v[j].x;
                 if (v[j].x > bv) {
                     bv = v[j].x;
@@ -385,7 +423,7 @@ __global__ void __launch_bounds__(2 * N, sizeof(T) == 4 ? 2 : 1)
             }
 #pragma unroll
             for (int j = 0; j < E; ++j) {
-                const int x = t + 8 * j;
+                const int x = t + G * j;
                 reinterpret_cast<T *>(sp<N>(S, rb, x >> 1))[x & 1] = v[j].y;
                 if (v[j].y > bv) {
                     bv = v[j].y;
@@ -423,13 +461,12 @@ __global__ void __launch_bounds__(2 * N, sizeof(T) == 4 ? 2 : 1)
                 const uint32_t qy = q / N, qx = q % N;
                 T val = reinterpret_cast<T *>(sp<N>(S, qy, qx >> 1))[qx & 1];
                 fbuf[slot * 81 + l] = val;
-                if (a.neigh) reinterpret_cast<T *>(a.neigh)[(size_t)pair * s2 + l] = val;
+                if (a.neigh) reinterpret_cast<T *>(a.neigh)[(size_t)out * s2 + l] = val;
             }
             if (lane == 0) {
-                fmeta[4 * slot] = pair;
-                fmeta[4 * slot + 1] = mx;
-                fmeta[4 * slot + 2] = my;
-                fmeta[4 * slot + 3] = pk;
+                fmeta[4 * slot] = out;
+                fmeta[4 * slot + 1] = mx | (my << 16);
+                fmeta[4 * slot + 2] = pk | ((uint32_t)s << 24);
                 fval[slot] = pv;
             }
             __syncwarp();
@@ -440,66 +477,59 @@ __global__ void __launch_bounds__(2 * N, sizeof(T) == 4 ? 2 : 1)
     }
 }
 
-template <int N, typename T>
-size_t fused_smem_bytes()
-{
-    using C = cplx<T>;
-    size_t b = (size_t)N * (N / 2) * sizeof(C);  // spectrum
-    b += 2 * (size_t)N * sizeof(C);              // forward and inverse twiddles
-    b += N * sizeof(T);                          // hx, hy
-    b += 32 * sizeof(T) + 32 * sizeof(uint32_t); // argmax scratch
-    b = (b + 7) & ~(size_t)7;
-    b += (32 + 81 + 8) * sizeof(double);         // sums, neighbours, spare
-    b += 16;                                     // mbarrier
-    b += 32 * 81 * sizeof(T) + 32 * 4 * 4 + 32 * sizeof(T);  // fit buffer
-    b = (b + 127) & ~(size_t)127;
-    b += (size_t)(N / 2) * (N / 2 + 8) * 2;      // uint16 ROI tile
-    return b;
-}
-
-template <int N, typename T, typename IN>
+template <int N, int G, typename T, typename IN>
 static cudaError_t launch_one(const fused_args &a, const CUtensorMap *tmap, int grid,
                               cudaStream_t st)
 {
-    auto k = fused_fft_kernel<N, T, IN>;
-    const size_t smem = fused_smem_bytes<N, T>();
+    auto k = fused_fft_kernel<N, G, T, IN>;
+    constexpr int threads = N * G / 4;
+    const size_t smem = fused_layout<N, G, T>::bytes;
     cudaError_t e = cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
     if (e != cudaSuccess) return e;
     if (grid <= 0) {
         int per_sm = 0, dev = 0, sms = 0;
         cudaGetDevice(&dev);
         cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
-        e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k, 2 * N, smem);
+        e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k, threads, smem);
         if (e != cudaSuccess) return e;
         if (per_sm < 1) per_sm = 1;
         grid = per_sm * sms;
     }
     if ((uint32_t)grid > a.n_pairs) grid = (int)a.n_pairs;
     if (grid < 1) return cudaSuccess;
-    k<<<grid, 2 * N, smem, st>>>(a, *tmap);
+    k<<<grid, threads, smem, st>>>(a, *tmap);
     return cudaGetLastError();
 }
 
-bool fused_supported(uint32_t fft_n) { return fft_n == 64 || fft_n == 128; }
+bool fused_supported(uint32_t fft_n, bool dbl)
+{
+    return fft_n == 64 || fft_n == 96 || fft_n == 128 || (fft_n == 192 && !dbl);
+}
+
+template <int N, int G>
+static cudaError_t launch_n(bool dbl, bool in_f64, const fused_args &a, const CUtensorMap *tmap,
+                            int grid, cudaStream_t st)
+{
+    if (dbl)
+        return in_f64 ? launch_one<N, G, double, double>(a, tmap, grid, st)
+                      : launch_one<N, G, double, uint16_t>(a, tmap, grid, st);
+    return in_f64 ? launch_one<N, G, float, double>(a, tmap, grid, st)
+                  : launch_one<N, G, float, uint16_t>(a, tmap, grid, st);
+}
 
 cudaError_t launch_fused(uint32_t fft_n, bool dbl, bool in_f64, const fused_args &a,
                          const CUtensorMap *tmap, int grid, cudaStream_t st)
 {
-    if (fft_n == 128) {
-        if (dbl)
-            return in_f64 ? launch_one<128, double, double>(a, tmap, grid, st)
-                          : launch_one<128, double, uint16_t>(a, tmap, grid, st);
-        return in_f64 ? launch_one<128, float, double>(a, tmap, grid, st)
-                      : launch_one<128, float, uint16_t>(a, tmap, grid, st);
+    if (!fused_supported(fft_n, dbl)) return cudaErrorInvalidValue;
+    switch (fft_n) {
+    case 64: return launch_n<64, 8>(dbl, in_f64, a, tmap, grid, st);
+    case 96: return launch_n<96, 4>(dbl, in_f64, a, tmap, grid, st);
+    case 128: return launch_n<128, 8>(dbl, in_f64, a, tmap, grid, st);
+    default: break;
     }
-    if (fft_n == 64) {
-        if (dbl)
-            return in_f64 ? launch_one<64, double, double>(a, tmap, grid, st)
-                          : launch_one<64, double, uint16_t>(a, tmap, grid, st);
-        return in_f64 ? launch_one<64, float, double>(a, tmap, grid, st)
-                      : launch_one<64, float, uint16_t>(a, tmap, grid, st);
-    }
-    return cudaErrorInvalidValue;
+    // 192 points, FP32 only (an FP64 spectrum would not fit in shared memory)
+    return in_f64 ? launch_one<192, 8, float, double>(a, tmap, grid, st)
+                  : launch_one<192, 8, float, uint16_t>(a, tmap, grid, st);
 }
 
 }  // namespace emida_gb

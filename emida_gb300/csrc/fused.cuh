@@ -24,9 +24,22 @@ struct fused_args {
     void *maxes;            // data_index<T>[n_pairs] or null
     void *neigh;            // T[n_pairs][s*s] or null
     uint32_t *err;          // device error word (dev_err_t bits)
+    // Work-list mode (several ROI layouts and fit sizes in one launch): item p
+    // is {pattern, ROI index into begins / ref_spec, output slot, fit size}.
+    // Without a list, pair p is pattern p / n_rois, ROI p % n_rois, slot p,
+    // fit size `fitsize`.
+    const uint4 *items;
+    const double *lstsq_all; // items mode: the tables for s = 3, 5, 7, 9 back to back
 };
 
-bool fused_supported(uint32_t fft_n);
+// Offset of the s x s table inside lstsq_all (6*9, 6*25, 6*49, 6*81 doubles).
+__host__ __device__ inline int lstsq_offset(int s)
+{
+    return s == 3 ? 0 : s == 5 ? 54 : s == 7 ? 204 : 498;
+}
+
+// Transform sizes (2 * ROI side) with a fused kernel: 64, 96, 128 and, in FP32, 192.
+bool fused_supported(uint32_t fft_n, bool dbl);
 
 // grid <= 0: one wave of resident CTAs (occupancy x SM count).
 cudaError_t launch_fused(uint32_t fft_n, bool dbl, bool in_f64, const fused_args &a,

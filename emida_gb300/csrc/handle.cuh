@@ -1,0 +1,123 @@
+// handle.cuh -- the handle behind the C ABI and the host helpers shared by the
+// translation units that drive it (capi.cu, multi.cu).
+#pragma once
+
+#include <cuda.h>
+
+#include <atomic>
+#include <cstdint>
+#include <mutex>
+#include <string>
+#include <vector>
+
+#include "../../include/emida_gb.h"
+#include "common.cuh"
+#include "fused.cuh"
+#include "staged.cuh"
+
+struct emida_gb_handle;
+
+namespace emida_gb {
+namespace host {
+
+// Records the message for emida_gb_last_error() and returns `code`.
+int fail(int code, const char *fmt, ...);
+// (A^T A)^-1 A^T for the 6-term quadratic, exact rationals rounded once.
+int lstsq_matrix(int s, double *out);
+
+using encode_fn = CUresult (*)(CUtensorMap *, CUtensorMapDataType, cuuint32_t, void *,
+                               const cuuint64_t *, const cuuint64_t *, const cuuint32_t *,
+                               const cuuint32_t *, CUtensorMapInterleave, CUtensorMapSwizzle,
+                               CUtensorMapL2promotion, CUtensorMapFloatOOBfill);
+encode_fn get_encoder();
+
+int upload_hann(emida_gb_handle *h, void **dst, uint32_t nx, uint32_t ny);
+int upload_twiddles(emida_gb_handle *h, void **dst, uint32_t n);
+fft_tables tables(const emida_gb_handle *h);
+// The staged pipeline for pats <= batch_size patterns (src/gpu_offset.hpp:234-278).
+int run_plain_chunk(emida_gb_handle *h, const void *pics, uint32_t pats, void *maxes, void *neigh,
+                    double *offsets, double *coefs, cudaStream_t st);
+int run_fused(emida_gb_handle *h, const void *pics, uint32_t pats, void *maxes, void *neigh,
+              double *offsets, double *coefs, cudaStream_t st);
+// Either form, any number of patterns.
+int run_any(emida_gb_handle *h, const void *pics, uint32_t pats, void *maxes, void *neigh,
+            double *offsets, double *coefs, cudaStream_t st);
+int check_device_error(emida_gb_handle *h);
+
+}  // namespace host
+}  // namespace emida_gb
+
+#define CK(expr)                                                                            \
+    do {                                                                                    \
+        cudaError_t e_ = (expr);                                                            \
+        if (e_ != cudaSuccess)                                                              \
+            return emida_gb::host::fail(e_ == cudaErrorMemoryAllocation ? EMIDA_GB_OUT_OF_MEMORY             \
+                                                        : EMIDA_GB_CUDA_ERROR,               \
+                        "CUDA error %d (%s) at %s:%d: %s", (int)e_, cudaGetErrorString(e_),  \
+                        __FILE__, __LINE__, #expr);                                         \
+    } while (0)
+
+#define CKS(expr)                                                                           \
+    do {                                                                                    \
+        int s_ = (expr);                                                                    \
+        if (s_ != EMIDA_GB_OK) return s_;                                                   \
+    } while (0)
+
+
+using emida_gb::size2;
+using emida_gb::data_index;
+
+struct emida_gb_handle {
+    emida_gb_params p{};
+    std::vector<uint32_t> begins;
+    int device = 0;
+    bool dbl = false, in_f64 = false, fft = false;
+    int mode = EMIDA_GB_MODE_PLAIN;
+    size2 src{}, slice{}, cross{};
+    uint32_t S = 0, B = 0, N = 0;
+    uint32_t w2 = 0, h2 = 0, half = 0;
+    size_t in_elem = 2, t_elem = 4, c_elem = 8, di_elem = 8;
+    cudaStream_t in_stream = nullptr, out_stream = nullptr, comp = nullptr;
+    std::vector<cudaEvent_t> in_done;
+    cudaEvent_t comp_done = nullptr;
+    std::vector<void *> d_in;
+    std::atomic<uint32_t> in_next{0};
+    void *d_ref_in = nullptr;
+    uint2 *d_begins = nullptr;
+    void *d_hann = nullptr, *d_hann_fused = nullptr;
+    void *d_sums_ref = nullptr, *d_sums = nullptr;
+    void *d_ref_prep = nullptr, *d_prep = nullptr;
+    void *d_ref_spec = nullptr, *d_ref_spec_cm = nullptr, *d_spec = nullptr;
+    void *d_map = nullptr, *d_maxes = nullptr, *d_neigh = nullptr;
+    double *d_offsets = nullptr, *d_coefs = nullptr, *d_lstsq = nullptr;
+    void *d_tw_row = nullptr, *d_tw_col = nullptr;
+    uint32_t *d_err = nullptr;
+    std::vector<double> lstsq;
+    bool ref_set = false;
+    std::mutex mu;
+    std::vector<void *> allocs;
+    // submit/wait ring: one slot per input buffer
+    struct slot {
+        double *d_offsets = nullptr, *d_coefs = nullptr;
+        void *d_maxes = nullptr;
+        double *h_offsets = nullptr, *h_coefs = nullptr;
+        void *h_maxes = nullptr;
+        cudaEvent_t h2d = nullptr, comp = nullptr, done = nullptr;
+        uint64_t ticket = 0;
+        uint32_t patterns = 0;
+        bool busy = false;
+    };
+    std::vector<slot> ring;
+    uint64_t next_ticket = 1;
+
+    int alloc(void **ptr, size_t bytes, bool zero = false)
+    {
+        if (bytes == 0) bytes = 16;
+        CK(cudaMalloc(ptr, bytes));
+        allocs.push_back(*ptr);
+        if (zero) CK(cudaMemset(*ptr, 0, bytes));
+        return EMIDA_GB_OK;
+    }
+    uint32_t map_size() const { return fft ? w2 * h2 : cross.x * cross.y; }
+    size2 prep_size() const { return fft ? size2{w2, h2} : slice; }
+};

@@ -1,0 +1,424 @@
+// multi.cu -- batches whose patterns use different ROI layouts: per pattern a
+// set of ROI positions, one ROI size and one fit size.  Every layout's
+// reference spectra are computed once (as gpu_offset::allocate_memory does,
+// src/gpu_offset.hpp:185-210) and kept resident, grouped by transform size.
+// A run launches one persistent fused kernel per transform size over a work
+// list of (pattern, ROI, output slot, fit size); sizes without a fused kernel
+// run the staged pipeline per pattern.  Runs can be captured in a CUDA graph
+// and replayed, and the persistent grid of each size is chosen by timing.
+#include <algorithm>
+#include <cstring>
+#include <memory>
+#include <string>
+#include <vector>
+
+#include "handle.cuh"
+
+using namespace emida_gb;
+using namespace emida_gb::host;
+
+struct emida_gb_multi {
+    struct layout {
+        uint32_t n_rois = 0, side = 0, roi_base = 0;
+        int fitsize = 3, cls = -1;
+        emida_gb_handle *h = nullptr;  // reference spectra; staged runs when not fused
+    };
+    struct size_class {
+        uint32_t n = 0;  // transform length 2 * side
+        bool fused = false;
+        std::vector<uint2> begins;
+        uint2 *d_begins = nullptr;
+        size_t begins_cap = 0;
+        void *d_spec = nullptr;  // [rois][n/2 + 1][n] complex, column-major per ROI
+        size_t spec_cap = 0;     // in ROIs
+        const void *hann = nullptr, *twiddles = nullptr;  // owned by the class's first layout
+        uint4 *d_items = nullptr;
+        size_t items_cap = 0;
+        int grid = 0;  // 0: one wave of resident CTAs
+    };
+    uint32_t src_w = 0, src_h = 0;
+    int precision = EMIDA_GB_FLOAT;
+    bool dbl = false;
+    std::vector<layout> layouts;
+    std::vector<size_class> classes;
+    double *d_lstsq_all = nullptr;
+    uint32_t *d_err = nullptr;
+    cudaStream_t stream = nullptr;
+    // graph cache: the last captured run and what it was captured for
+    cudaGraphExec_t gexec = nullptr;
+    const void *g_pics = nullptr;
+    uint32_t g_patterns = 0;
+    std::vector<uint32_t> g_layout_of;
+    double *g_offs = nullptr, *g_coefs = nullptr;
+    void *g_maxes = nullptr;
+    std::mutex mu;
+};
+
+namespace {
+
+size_t spec_bytes_per_roi(uint32_t n, bool dbl) { return (size_t)(n / 2 + 1) * n * (dbl ? 16 : 8); }
+
+int grow(void **buf, size_t *cap_bytes, size_t need, size_t keep)
+{
+    if (need <= *cap_bytes) return EMIDA_GB_OK;
+    size_t cap = std::max(need, *cap_bytes * 2);
+    void *nb = nullptr;
+    CK(cudaMalloc(&nb, cap));
+    if (*buf && keep) CK(cudaMemcpy(nb, *buf, keep, cudaMemcpyDeviceToDevice));
+    if (*buf) CK(cudaFree(*buf));
+    *buf = nb;
+    *cap_bytes = cap;
+    return EMIDA_GB_OK;
+}
+
+void drop_graph(emida_gb_multi *m)
+{
+    if (m->gexec) cudaGraphExecDestroy(m->gexec);
+    m->gexec = nullptr;
+    m->g_layout_of.clear();
+}
+
+// Work lists of one run; returns the total ROI count.
+struct staged_item {
+    uint32_t pattern, layout;
+    uint64_t base;  // first output slot
+};
+struct plan {
+    std::vector<std::vector<uint4>> items;  // per class
+    std::vector<staged_item> staged;
+    uint64_t total = 0;
+};
+
+int make_plan(emida_gb_multi *m, uint32_t patterns, const uint32_t *layout_of, plan &pl)
+{
+    pl.items.assign(m->classes.size(), {});
+    for (uint32_t p = 0; p < patterns; ++p) {
+        if (layout_of[p] >= m->layouts.size())
+            return fail(EMIDA_GB_INVALID_ARGUMENT, "pattern %u: unknown layout %u", p, layout_of[p]);
+        const auto &L = m->layouts[layout_of[p]];
+        if (m->classes[L.cls].fused) {
+            auto &v = pl.items[L.cls];
+            for (uint32_t r = 0; r < L.n_rois; ++r)
+                v.push_back(make_uint4(p, L.roi_base + r, (uint32_t)(pl.total + r), (uint32_t)L.fitsize));
+        } else {
+            pl.staged.push_back(staged_item{p, layout_of[p], pl.total});
+        }
+        pl.total += L.n_rois;
+    }
+    if (pl.total >= (1ull << 32)) return fail(EMIDA_GB_INVALID_ARGUMENT, "too many ROIs in one run");
+    return EMIDA_GB_OK;
+}
+
+int upload_plan(emida_gb_multi *m, const plan &pl, bool &realloc)
+{
+    realloc = false;
+    for (size_t c = 0; c < m->classes.size(); ++c) {
+        auto &k = m->classes[c];
+        const auto &v = pl.items[c];
+        if (v.empty()) continue;
+        const size_t need = v.size() * sizeof(uint4);
+        if (need > k.items_cap) realloc = true;
+        CKS(grow((void **)&k.d_items, &k.items_cap, need, 0));
+        CK(cudaMemcpy(k.d_items, v.data(), need, cudaMemcpyHostToDevice));
+    }
+    return EMIDA_GB_OK;
+}
+
+// The launches of one run, on m->stream (capturable).
+int launch_plan(emida_gb_multi *m, const plan &pl, const void *pics, uint32_t patterns,
+                double *offs, double *coefs, void *maxes, int only_class = -1, int grid_override = -1)
+{
+    const size_t pat_bytes = (size_t)m->src_w * m->src_h * 2;
+    const size_t di = m->dbl ? sizeof(data_index<double>) : sizeof(data_index<float>);
+    CUtensorMap map;
+    std::memset(&map, 0, sizeof map);
+    int use_tma = 0;
+    if ((m->src_w % 8) == 0 && ((uintptr_t)pics % 16) == 0) {
+        // one map per size class (the box is the ROI side + 8 by the ROI side)
+        use_tma = get_encoder() != nullptr;
+    }
+    for (size_t c = 0; c < m->classes.size(); ++c) {
+        if (only_class >= 0 && (int)c != only_class) continue;
+        auto &k = m->classes[c];
+        if (!k.fused || pl.items[c].empty()) continue;
+        fused_args a{};
+        a.pics = pics;
+        a.src_w = m->src_w;
+        a.src_h = m->src_h;
+        a.begins = k.d_begins;
+        a.n_rois = 1;
+        a.n_pairs = (uint32_t)pl.items[c].size();
+        a.ref_spec = k.d_spec;
+        a.hann = k.hann;
+        a.twiddles = k.twiddles;
+        a.lstsq = nullptr;
+        a.lstsq_all = m->d_lstsq_all;
+        a.fitsize = 3;
+        a.offsets = offs;
+        a.coefs = coefs;
+        a.maxes = maxes;
+        a.neigh = nullptr;
+        a.err = m->d_err;
+        a.items = k.d_items;
+        a.use_tma = 0;
+        if (use_tma) {
+            const uint32_t side = k.n / 2;
+            const cuuint64_t dims[3] = {m->src_w, m->src_h, patterns};
+            const cuuint64_t strides[2] = {(cuuint64_t)m->src_w * 2, (cuuint64_t)m->src_w * m->src_h * 2};
+            const cuuint32_t box[3] = {side + 8, side, 1};
+            const cuuint32_t estr[3] = {1, 1, 1};
+            if (get_encoder()(&map, CU_TENSOR_MAP_DATA_TYPE_UINT16, 3, const_cast<void *>(pics), dims,
+                              strides, box, estr, CU_TENSOR_MAP_INTERLEAVE_NONE,
+                              CU_TENSOR_MAP_SWIZZLE_NONE, CU_TENSOR_MAP_L2_PROMOTION_L2_128B,
+                              CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE) == CUDA_SUCCESS)
+                a.use_tma = 1;
+        }
+        const int grid = grid_override >= 0 ? grid_override : k.grid;
+        CK(launch_fused(k.n, m->dbl, false, a, &map, grid, m->stream));
+    }
+    if (only_class >= 0) return EMIDA_GB_OK;
+    for (const auto &e : pl.staged) {
+        emida_gb_handle *h = m->layouts[e.layout].h;
+        CKS(run_any(h, (const char *)pics + e.pattern * pat_bytes, 1,
+                    maxes ? (char *)maxes + e.base * di : nullptr, nullptr, offs + 2 * e.base,
+                    coefs ? coefs + 6 * e.base : nullptr, m->stream));
+    }
+    return EMIDA_GB_OK;
+}
+
+}  // namespace
+
+extern "C" {
+
+int emida_gb_multi_create(uint32_t src_w, uint32_t src_h, int32_t precision, emida_gb_multi **out)
+{
+    if (!out) return fail(EMIDA_GB_INVALID_ARGUMENT, "null output");
+    *out = nullptr;
+    if (src_w == 0 || src_h == 0) return fail(EMIDA_GB_INVALID_ARGUMENT, "empty pattern size");
+    if (precision != EMIDA_GB_DOUBLE && precision != EMIDA_GB_FLOAT)
+        return fail(EMIDA_GB_INVALID_ARGUMENT, "invalid precision %d", precision);
+    auto m = std::make_unique<emida_gb_multi>();
+    m->src_w = src_w;
+    m->src_h = src_h;
+    m->precision = precision;
+    m->dbl = precision == EMIDA_GB_DOUBLE;
+    std::vector<double> all(984);
+    for (int s : {3, 5, 7, 9}) lstsq_matrix(s, all.data() + lstsq_offset(s));
+    CK(cudaStreamCreateWithFlags(&m->stream, cudaStreamNonBlocking));
+    CK(cudaMalloc((void **)&m->d_lstsq_all, all.size() * sizeof(double)));
+    CK(cudaMemcpy(m->d_lstsq_all, all.data(), all.size() * sizeof(double), cudaMemcpyHostToDevice));
+    CK(cudaMalloc((void **)&m->d_err, sizeof(uint32_t)));
+    CK(cudaMemset(m->d_err, 0, sizeof(uint32_t)));
+    *out = m.release();
+    return EMIDA_GB_OK;
+}
+
+int emida_gb_multi_add_layout(emida_gb_multi *m, const uint32_t *begins, uint32_t n_rois,
+                              uint32_t side, int32_t fitsize, const uint16_t *ref,
+                              uint32_t *layout_id)
+{
+    if (!m || !begins || !ref || !layout_id) return fail(EMIDA_GB_INVALID_ARGUMENT, "null argument");
+    std::lock_guard<std::mutex> lk(m->mu);
+    emida_gb_params p{};
+    p.src_w = m->src_w;
+    p.src_h = m->src_h;
+    p.begins = begins;
+    p.n_rois = n_rois;
+    p.slice_w = p.slice_h = side;
+    p.cross_w = p.cross_h = 2 * side - 1;
+    p.batch_size = 1;
+    p.policy = EMIDA_GB_FFT;
+    p.precision = m->precision;
+    p.fitsize = fitsize;
+    p.in_type = EMIDA_GB_IN_U16;
+    p.mode = EMIDA_GB_MODE_AUTO;
+    p.in_buffers = 1;
+    emida_gb_handle *h = nullptr;
+    CKS(emida_gb_create(&p, &h));
+    int st = emida_gb_set_reference(h, ref);
+    if (st != EMIDA_GB_OK) {
+        emida_gb_destroy(h);
+        return st;
+    }
+    emida_gb_multi::layout L;
+    L.n_rois = n_rois;
+    L.side = side;
+    L.fitsize = fitsize;
+    L.h = h;
+    const uint32_t n = 2 * side;
+    int cls = -1;
+    for (size_t c = 0; c < m->classes.size(); ++c)
+        if (m->classes[c].n == n) cls = (int)c;
+    if (cls < 0) {
+        emida_gb_multi::size_class k;
+        k.n = n;
+        k.fused = emida_gb_resolved_mode(h) == EMIDA_GB_MODE_FUSED;
+        k.hann = h->d_hann_fused;
+        k.twiddles = h->d_tw_row;
+        m->classes.push_back(k);
+        cls = (int)m->classes.size() - 1;
+    }
+    L.cls = cls;
+    auto &k = m->classes[cls];
+    if (k.fused) {
+        L.roi_base = (uint32_t)k.begins.size();
+        for (uint32_t r = 0; r < n_rois; ++r) k.begins.push_back(make_uint2(begins[2 * r], begins[2 * r + 1]));
+        const size_t per = spec_bytes_per_roi(n, m->dbl);
+        size_t bcap = k.begins_cap * sizeof(uint2), scap = k.spec_cap * per;
+        CKS(grow((void **)&k.d_begins, &bcap, k.begins.size() * sizeof(uint2), 0));
+        CKS(grow(&k.d_spec, &scap, k.begins.size() * per, (size_t)L.roi_base * per));
+        k.begins_cap = bcap / sizeof(uint2);
+        k.spec_cap = scap / per;
+        CK(cudaMemcpy(k.d_begins, k.begins.data(), k.begins.size() * sizeof(uint2), cudaMemcpyHostToDevice));
+        CK(cudaMemcpy((char *)k.d_spec + (size_t)L.roi_base * per, h->d_ref_spec_cm, (size_t)n_rois * per,
+                      cudaMemcpyDeviceToDevice));
+    }
+    m->layouts.push_back(L);
+    drop_graph(m);  // spectra or tables may have moved
+    *layout_id = (uint32_t)m->layouts.size() - 1;
+    return EMIDA_GB_OK;
+}
+
+int emida_gb_multi_count(const emida_gb_multi *m, uint32_t patterns, const uint32_t *layout_of,
+                         uint64_t *total)
+{
+    if (!m || !layout_of || !total) return fail(EMIDA_GB_INVALID_ARGUMENT, "null argument");
+    uint64_t t = 0;
+    for (uint32_t p = 0; p < patterns; ++p) {
+        if (layout_of[p] >= m->layouts.size())
+            return fail(EMIDA_GB_INVALID_ARGUMENT, "pattern %u: unknown layout %u", p, layout_of[p]);
+        t += m->layouts[layout_of[p]].n_rois;
+    }
+    *total = t;
+    return EMIDA_GB_OK;
+}
+
+int emida_gb_multi_run(emida_gb_multi *m, const void *dev_patterns, uint32_t patterns,
+                       const uint32_t *layout_of, double *dev_offsets, double *dev_coefs,
+                       void *dev_maxes, int use_graph)
+{
+    if (!m || !dev_patterns || !layout_of || !dev_offsets)
+        return fail(EMIDA_GB_INVALID_ARGUMENT, "null argument");
+    std::lock_guard<std::mutex> lk(m->mu);
+    const bool same = m->gexec && m->g_pics == dev_patterns && m->g_patterns == patterns &&
+                      m->g_offs == dev_offsets && m->g_coefs == dev_coefs && m->g_maxes == dev_maxes &&
+                      std::equal(m->g_layout_of.begin(), m->g_layout_of.end(), layout_of) &&
+                      m->g_layout_of.size() == patterns;
+    if (use_graph && same) {
+        CK(cudaGraphLaunch(m->gexec, m->stream));
+        return EMIDA_GB_OK;
+    }
+    plan pl;
+    CKS(make_plan(m, patterns, layout_of, pl));
+    drop_graph(m);  // the work lists it reads are about to be overwritten
+    bool realloc = false;
+    CKS(upload_plan(m, pl, realloc));
+    if (!use_graph) return launch_plan(m, pl, dev_patterns, patterns, dev_offsets, dev_coefs, dev_maxes);
+    cudaGraph_t graph;
+    CK(cudaStreamBeginCapture(m->stream, cudaStreamCaptureModeRelaxed));
+    int st = launch_plan(m, pl, dev_patterns, patterns, dev_offsets, dev_coefs, dev_maxes);
+    cudaError_t e = cudaStreamEndCapture(m->stream, &graph);
+    if (st != EMIDA_GB_OK) {
+        if (e == cudaSuccess) cudaGraphDestroy(graph);
+        return st;
+    }
+    CK(e);
+    e = cudaGraphInstantiate(&m->gexec, graph, 0);
+    cudaGraphDestroy(graph);
+    CK(e);
+    m->g_pics = dev_patterns;
+    m->g_patterns = patterns;
+    m->g_offs = dev_offsets;
+    m->g_coefs = dev_coefs;
+    m->g_maxes = dev_maxes;
+    m->g_layout_of.assign(layout_of, layout_of + patterns);
+    CK(cudaGraphLaunch(m->gexec, m->stream));
+    return EMIDA_GB_OK;
+}
+
+int emida_gb_multi_synchronize(emida_gb_multi *m)
+{
+    if (!m) return fail(EMIDA_GB_INVALID_ARGUMENT, "null argument");
+    CK(cudaStreamSynchronize(m->stream));
+    uint32_t err = 0;
+    CK(cudaMemcpy(&err, m->d_err, sizeof err, cudaMemcpyDeviceToHost));
+    if (err) {
+        CK(cudaMemset(m->d_err, 0, sizeof err));
+        return fail(EMIDA_GB_DEVICE_CHECK, "device check failed (flags 0x%x)", err);
+    }
+    return EMIDA_GB_OK;
+}
+
+int emida_gb_multi_autotune(emida_gb_multi *m, const void *dev_patterns, uint32_t patterns,
+                            const uint32_t *layout_of, double *dev_offsets, char *report,
+                            size_t report_len)
+{
+    if (!m || !dev_patterns || !layout_of || !dev_offsets)
+        return fail(EMIDA_GB_INVALID_ARGUMENT, "null argument");
+    std::lock_guard<std::mutex> lk(m->mu);
+    plan pl;
+    CKS(make_plan(m, patterns, layout_of, pl));
+    drop_graph(m);
+    bool realloc = false;
+    CKS(upload_plan(m, pl, realloc));
+    int dev = 0, sms = 0;
+    CK(cudaGetDevice(&dev));
+    CK(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev));
+    std::string rep;
+    cudaEvent_t a, b;
+    CK(cudaEventCreate(&a));
+    CK(cudaEventCreate(&b));
+    for (size_t c = 0; c < m->classes.size(); ++c) {
+        auto &k = m->classes[c];
+        if (!k.fused || pl.items[c].empty()) continue;
+        float best = 1e30f;
+        int best_grid = 0;
+        for (int per_sm = 1; per_sm <= 4; ++per_sm) {
+            const int grid = per_sm * sms;
+            CKS(launch_plan(m, pl, dev_patterns, patterns, dev_offsets, nullptr, nullptr, (int)c, grid));
+            CK(cudaEventRecord(a, m->stream));
+            for (int r = 0; r < 3; ++r)
+                CKS(launch_plan(m, pl, dev_patterns, patterns, dev_offsets, nullptr, nullptr, (int)c, grid));
+            CK(cudaEventRecord(b, m->stream));
+            CK(cudaEventSynchronize(b));
+            float ms = 0;
+            CK(cudaEventElapsedTime(&ms, a, b));
+            if (ms < best * 0.98f) {
+                best = ms;
+                best_grid = grid;
+            }
+        }
+        k.grid = best_grid;
+        char line[160];
+        snprintf(line, sizeof line, "n=%u: %zu pairs, grid %d (%d per SM), %.3f ms\n", k.n,
+                 pl.items[c].size(), best_grid, best_grid / std::max(1, sms), best / 3);
+        rep += line;
+    }
+    cudaEventDestroy(a);
+    cudaEventDestroy(b);
+    drop_graph(m);
+    if (report && report_len) {
+        std::strncpy(report, rep.c_str(), report_len - 1);
+        report[report_len - 1] = 0;
+    }
+    return EMIDA_GB_OK;
+}
+
+void emida_gb_multi_destroy(emida_gb_multi *m)
+{
+    if (!m) return;
+    if (m->stream) cudaStreamSynchronize(m->stream);
+    drop_graph(m);
+    for (auto &k : m->classes) {
+        if (k.d_begins) cudaFree(k.d_begins);
+        if (k.d_spec) cudaFree(k.d_spec);
+        if (k.d_items) cudaFree(k.d_items);
+    }
+    for (auto &L : m->layouts) emida_gb_destroy(L.h);
+    if (m->d_lstsq_all) cudaFree(m->d_lstsq_all);
+    if (m->d_err) cudaFree(m->d_err);
+    if (m->stream) cudaStreamDestroy(m->stream);
+    delete m;
+}
+
+}  // extern "C"

@@ -131,6 +131,38 @@ int emida_gb_subpixel_max(const double *neigh, int s, uint32_t n, double *sub, d
 /* (A^T A)^-1 A^T used by the fit, 6 x s*s (src/subpixel_max.cpp:5-58). */
 int emida_gb_lstsq_matrix(int s, double *out);
 
+/* ---- multi-layout batches -------------------------------------------------
+ * No counterpart in the reference, which runs one ROI layout per gpu_offset.
+ * Patterns of one batch may each use a different layout (ROI positions, one
+ * ROI side, one fit size), all against uint16 reference patterns.  Each
+ * layout's reference spectra are computed once and stay resident.  A run
+ * processes device-resident uint16 patterns with one persistent fused launch
+ * per transform size (sizes without a fused kernel run the staged pipeline per
+ * pattern).  Results are flat in pattern order, then ROI order within the
+ * pattern's layout (emida_gb_multi_count gives the total). */
+typedef struct emida_gb_multi emida_gb_multi;
+int emida_gb_multi_create(uint32_t src_w, uint32_t src_h, int32_t precision,
+                          emida_gb_multi **out);
+int emida_gb_multi_add_layout(emida_gb_multi *m, const uint32_t *begins, uint32_t n_rois,
+                              uint32_t side, int32_t fitsize, const uint16_t *ref,
+                              uint32_t *layout_id);
+int emida_gb_multi_count(const emida_gb_multi *m, uint32_t patterns, const uint32_t *layout_of,
+                         uint64_t *total);
+/* Queues a run on the planner's stream (no synchronisation).  use_graph != 0:
+ * the launches are captured in a CUDA graph on first use and replayed while
+ * the same patterns pointer, layout assignment and output pointers repeat.
+ * dev_coefs [total][6] and dev_maxes (data_index<T>[total]) may be NULL. */
+int emida_gb_multi_run(emida_gb_multi *m, const void *dev_patterns, uint32_t patterns,
+                       const uint32_t *layout_of, double *dev_offsets, double *dev_coefs,
+                       void *dev_maxes, int use_graph);
+int emida_gb_multi_synchronize(emida_gb_multi *m);
+/* Times each fused transform size with 1..4 resident CTAs per SM on these
+ * patterns and keeps the fastest grid; writes a one-line-per-size report. */
+int emida_gb_multi_autotune(emida_gb_multi *m, const void *dev_patterns, uint32_t patterns,
+                            const uint32_t *layout_of, double *dev_offsets, char *report,
+                            size_t report_len);
+void emida_gb_multi_destroy(emida_gb_multi *m);
+
 /* ---- device memory helpers (for callers without a CUDA runtime binding) --- */
 int emida_gb_device_count(int *count);
 int emida_gb_malloc(void **dev_ptr, size_t bytes);

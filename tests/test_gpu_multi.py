@@ -1,0 +1,130 @@
+"""Multi-layout batches (patterns with different ROI sets, sizes and fit sizes
+in one run) through the C ABI, against the FP64 oracle per pattern."""
+import numpy as np
+import pytest
+
+
+pytestmark = pytest.mark.gpu
+
+
+@pytest.fixture(scope="module", autouse=True)
+def built():
+    import __graft_entry__
+    __graft_entry__.build_library()
+
+
+@pytest.fixture(scope="module")
+def scene():
+    from emida_gb300 import synth
+    ref = synth.reference_pattern(512, seed=21)
+    pics, _ = synth.deformed_patterns(512, 21, 7, sigma_eps=3e-3)
+    # (radius, fit size, ROI count): 96- and 192-point and 128-point fused
+    # sizes, a 64-point one, and 256 points (radius 64) on the staged path
+    specs = [(16, 3, 12), (24, 5, 9), (32, 7, 8), (48, 9, 4), (64, 5, 3), (32, 3, 10)]
+    layouts = []
+    for i, (r, s, n) in enumerate(specs):
+        _, begins = synth.random_layout(512, 100 + i, r, n, margin=4)
+        layouts.append((begins, 2 * r, s))
+    layout_of = np.array([0, 1, 2, 3, 4, 5, 2], dtype=np.uint32)
+    return ref, pics, layouts, layout_of
+
+
+def oracle_all(ref, pics, layouts, layout_of):
+    from oracle import oracle as eo
+    offs, coefs, peaks = [], [], []
+    for p, lid in enumerate(layout_of):
+        begins, side, s = layouts[lid]
+        o, c, k = eo.get_offsets(ref, pics[p:p + 1], begins, side, side, eo.POLICY_FFT, s)
+        offs.append(o)
+        coefs.append(c)
+        peaks.append(k)
+    return np.concatenate(offs), np.concatenate(coefs), np.concatenate(peaks)
+
+
+@pytest.mark.parametrize("precision,tol", [("float", 1e-3), ("double", 1e-9)])
+def test_multi_layout_batch_matches_oracle(scene, precision, tol):
+    from emida_gb300 import DeviceBuffer, MultiLayout
+    ref, pics, layouts, layout_of = scene
+    m = MultiLayout((512, 512), precision)
+    for begins, side, s in layouts:
+        m.add_layout(begins, side, s, ref)
+    total = m.count(layout_of)
+    assert total == sum(len(layouts[l][0]) for l in layout_of)
+    d_pics = DeviceBuffer.from_array(pics)
+    d_offs, d_coefs = DeviceBuffer(total * 16), DeviceBuffer(total * 48)
+    d_max = DeviceBuffer(total * m.data_index.itemsize)
+    m.run(d_pics, layout_of, d_offs, d_coefs, d_max, graph=False)
+    m.synchronize()
+    offs = d_offs.download(np.float64, (total, 2))
+    coefs = d_coefs.download(np.float64, (total, 6))
+    peaks = d_max.download(m.data_index, total)["index"]
+    o_offs, o_coefs, o_peaks = oracle_all(ref, pics, layouts, layout_of)
+    assert np.array_equal(peaks, o_peaks)
+    # each layout's own fit size decides which fits are well posed
+    from tests.test_gpu_synthetic import well_posed
+    start, n_ok = 0, 0
+    for p, lid in enumerate(layout_of):
+        n, s = len(layouts[lid][0]), layouts[lid][2]
+        sl = slice(start, start + n)
+        ok = well_posed(o_coefs[sl], s)
+        n_ok += int(ok.sum())
+        err = np.abs(offs[sl] - o_offs[sl]).max(axis=1)
+        assert (err[ok] <= tol).all(), (p, err[ok].max())
+        scale = np.abs(o_coefs[sl]).max(axis=1, keepdims=True)
+        rel = 1e-5 if tol >= 1e-6 else 1e-11
+        assert (np.abs(coefs[sl] - o_coefs[sl]) <= rel * scale).all()
+        start += n
+    assert n_ok > total // 2
+    # a captured graph gives the same bits, twice
+    m.run(d_pics, layout_of, d_offs, d_coefs, d_max, graph=True)
+    m.synchronize()
+    g1 = d_offs.download(np.float64, (total, 2))
+    d_offs.zero()
+    m.run(d_pics, layout_of, d_offs, d_coefs, d_max, graph=True)
+    m.synchronize()
+    g2 = d_offs.download(np.float64, (total, 2))
+    assert np.array_equal(g1, offs) and np.array_equal(g2, offs)
+    m.close()
+
+
+def test_multi_alone_equals_mixed(scene):
+    # each pattern's result is the same processed alone and in the mixed batch
+    from emida_gb300 import DeviceBuffer, MultiLayout
+    ref, pics, layouts, layout_of = scene
+    m = MultiLayout((512, 512), "float")
+    for begins, side, s in layouts:
+        m.add_layout(begins, side, s, ref)
+    total = m.count(layout_of)
+    d_pics = DeviceBuffer.from_array(pics)
+    d_offs = DeviceBuffer(total * 16)
+    m.run(d_pics, layout_of, d_offs, graph=False)
+    m.synchronize()
+    mixed = d_offs.download(np.float64, (total, 2))
+    start = 0
+    for p, lid in enumerate(layout_of):
+        n = len(layouts[lid][0])
+        d_one = DeviceBuffer.from_array(pics[p:p + 1])
+        d_o = DeviceBuffer(n * 16)
+        m.run(d_one, [lid], d_o, graph=False)
+        m.synchronize()
+        assert np.array_equal(d_o.download(np.float64, (n, 2)), mixed[start:start + n])
+        start += n
+    m.close()
+
+
+def test_multi_autotune_and_errors(scene):
+    from emida_gb300 import DeviceBuffer, EmidaError, MultiLayout
+    ref, pics, layouts, layout_of = scene
+    m = MultiLayout((512, 512), "float")
+    for begins, side, s in layouts:
+        m.add_layout(begins, side, s, ref)
+    total = m.count(layout_of)
+    d_pics = DeviceBuffer.from_array(pics)
+    d_offs = DeviceBuffer(total * 16)
+    report = m.autotune(d_pics, layout_of, d_offs)
+    assert "n=128" in report and "grid" in report
+    m.run(d_pics, layout_of, d_offs, graph=True)
+    m.synchronize()
+    with pytest.raises(EmidaError, match="unknown layout"):
+        m.run(d_pics, [99], d_offs, graph=False)
+    m.close()

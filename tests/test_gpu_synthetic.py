@@ -104,6 +104,23 @@ def test_fused_radius16(data512, precision, tol):
     assert_offsets(offs, coefs, o_offs, o_coefs, 3, tol)
 
 
+@pytest.mark.parametrize("radius,precision,tol", [(24, "float", 1e-3), (24, "double", 1e-9),
+                                                  (48, "float", 1e-3)])
+def test_fused_radius24_48(data512, radius, precision, tol):
+    # 48 x 48 ROIs (96-point transforms, 4-lane groups with radix-3 DFTs) and
+    # 96 x 96 ROIs (192-point transforms, FP32 only)
+    from emida_gb300 import synth
+    ref, pics = data512
+    _, begins = synth.roi_grid(512, 4, radius, margin=radius + 8)
+    side = 2 * radius
+    offs, coefs, peaks = run(ref, pics[:2], begins, side, "fft", 5, precision, "fused")
+    o_offs, o_coefs, o_peaks = oracle(ref, pics[:2], begins, side, "fft", 5)
+    assert np.array_equal(peaks, o_peaks)
+    assert_offsets(offs, coefs, o_offs, o_coefs, 5, tol)
+    p = run(ref, pics[:2], begins, side, "fft", 5, precision, "plain")
+    assert np.array_equal(p[2], o_peaks)
+
+
 def test_fused_equals_plain_peaks_and_border_rois(data512):
     # ROIs touching every border and with x not a multiple of 8 (TMA x rounding)
     ref, pics = data512
