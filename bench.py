@@ -57,6 +57,11 @@ def parse():
     ap.add_argument("--profile-case", type=int, default=0,
                     help="run only N patterns through the chosen form a few times (for ncu)")
     ap.add_argument("--no-plain", action="store_true", help="skip the plain-form comparison")
+    ap.add_argument("--config", default="detector", choices=["detector", "batching", "serving"],
+                    help="detector: 256 x 1024^2, 100 ROIs r=32 (default); batching: patterns on "
+                         "uneven layouts; serving: Poisson stream of scan rows")
+    ap.add_argument("--rate", type=float, default=50.0, help="serving: rows per second")
+    ap.add_argument("--duration", type=float, default=8.0, help="serving: seconds of arrivals")
     return ap.parse_args()
 
 
@@ -200,11 +205,171 @@ def run_reference(args, rank, world):
     print(json.dumps(line), flush=True)
 
 
+def pinned_u16(shape):
+    """A uint16 array in pinned host memory (freed with the process)."""
+    import ctypes
+    from emida_gb300 import _lib
+    n = int(np.prod(shape))
+    p = ctypes.c_void_p()
+    _lib.call("emida_gb_malloc_host", ctypes.byref(p), n * 2)
+    return np.ctypeslib.as_array(ctypes.cast(p, ctypes.POINTER(ctypes.c_uint16)), (n,)).reshape(shape)
+
+
+def random_layouts(size, count, seed, radii, rois, margin=4):
+    """`count` seeded layouts: (begins, side, fit size)."""
+    from emida_gb300 import synth
+    rng = np.random.default_rng(seed)
+    out = []
+    for i in range(count):
+        r = int(rng.choice(radii)) if len(radii) > 2 else int(rng.integers(radii[0], radii[1] + 1))
+        n = int(rng.integers(rois[0], rois[1] + 1))
+        _, begins = synth.random_layout(size, seed * 100 + i, r, n, margin=margin)
+        out.append((begins, 2 * r, int(rng.choice([3, 5, 7, 9]))))
+    return out
+
+
+def run_batching(args):
+    """4096 patterns of 1024^2 on 32 seeded layouts (radius 16..64, 25-400 ROIs,
+    fit size 3..9): one multi-layout run per step, replayed from a CUDA graph,
+    grids autotuned per ROI size."""
+    import time
+    import __graft_entry__
+    __graft_entry__.build_library()
+    from emida_gb300 import DeviceBuffer, MultiLayout, _lib, synth
+    from oracle import oracle as eo
+    P, L = 4096, 32
+    ref = synth.reference_pattern(1024, 77)
+    uniq, _ = synth.deformed_patterns(1024, 77, L, sigma_eps=5e-3)
+    layouts = random_layouts(1024, L, 77, [16, 24, 32, 48, 64], (25, 400))
+    m = MultiLayout((1024, 1024), args.precision)
+    for begins, side, fs in layouts:
+        m.add_layout(begins, side, fs, ref)
+    layout_of = np.arange(P, dtype=np.uint32) % L
+    d_pics = DeviceBuffer(P * 1024 * 1024 * 2)
+    d_uniq = DeviceBuffer.from_array(uniq)
+    import ctypes
+    for k in range(P // L):  # the 32 patterns repeated, on the device
+        _lib.call("emida_gb_memcpy_d2d", ctypes.c_void_p(d_pics.ptr.value + k * L * 1024 * 1024 * 2),
+                  d_uniq.ptr, L * 1024 * 1024 * 2)
+    total = m.count(layout_of)
+    d_offs, d_coefs = DeviceBuffer(total * 16), DeviceBuffer(total * 48)
+    report = m.autotune(d_pics, layout_of, d_offs)
+    m.run(d_pics, layout_of, d_offs, d_coefs, graph=True)
+    m.synchronize()
+    # parity: the first pattern of every layout against the FP64 oracle
+    offs = d_offs.download(np.float64, (total, 2))
+    coefs = d_coefs.download(np.float64, (total, 6))
+    import concurrent.futures as cf
+    starts = np.concatenate([[0], np.cumsum([len(layouts[l][0]) for l in layout_of])])
+
+    def check(p):
+        begins, side, fs = layouts[layout_of[p]]
+        o, c, _ = eo.get_offsets(ref, uniq[p:p + 1], begins, side, side, eo.POLICY_FFT, fs)
+        sl = slice(starts[p], starts[p + 1])
+        ok = well_posed(c, fs)
+        d = np.abs(offs[sl] - o)
+        return float(d[ok].max()) if ok.any() else 0.0, int(ok.sum() // 2), len(o)
+    with cf.ThreadPoolExecutor(os.cpu_count()) as ex:
+        res = list(ex.map(check, range(L)))
+    err = max(r[0] for r in res)
+    assert err <= 1e-2, f"offset error {err} px"
+    for _ in range(args.warmup):
+        m.run(d_pics, layout_of, d_offs, d_coefs, graph=True)
+    m.synchronize()
+    with ClockSampler(0) as clk:
+        t0 = time.perf_counter()
+        for _ in range(args.steps):
+            m.run(d_pics, layout_of, d_offs, d_coefs, graph=True)
+        m.synchronize()
+        dt = (time.perf_counter() - t0) / args.steps
+    radii = sorted({l[1] // 2 for l in layouts})
+    print(json.dumps({
+        "metric": "ROI pairs/s, patterns on uneven ROI layouts (one graph-replayed multi-layout run)",
+        "value": total / dt, "unit": "ROI pairs/s", "n_gpus": 1, "steps": args.steps,
+        "warmup": args.warmup, "ms_per_step": dt * 1000, "higher_is_better": True,
+        "dtype": "f32" if args.precision == "float" else "f64", "data": "synthetic",
+        "config": {"workload": f"{P} x 1024^2 uint16 patterns on {L} seeded layouts, radius "
+                               f"{radii}, 25-400 ROIs, fit 3-9", "patterns": P, "pairs": int(total)},
+        "autotune": report.strip().splitlines(),
+        "parity": {"max_abs_err_px": err, "well_posed_fits": sum(r[1] for r in res),
+                   "checked_pairs": sum(r[2] for r in res), "vs": "FP64 oracle, one pattern per layout"},
+        "clocks": clk.summary()}), flush=True)
+    m.close()
+
+
+def run_serving(args):
+    """A Poisson stream of scan rows (32-512 patterns, 512^2 or 1024^2, each on
+    its own layout: 25-225 ROIs of radius 24-48, fit 3-9) through the request
+    loop; p50/p99 row latency and sustained ROI pairs/s."""
+    import time
+    import __graft_entry__
+    __graft_entry__.build_library()
+    from emida_gb300 import Server, synth
+    from oracle import oracle as eo
+    rng = np.random.default_rng(99)
+    srv = Server(args.precision, hbm_bytes=24 << 30, step_patterns=128)
+    rows_src, layouts = {}, {}
+    for size in (512, 1024):
+        ref = synth.reference_pattern(size, 90 + size)
+        uniq, _ = synth.deformed_patterns(size, 90 + size, 16, sigma_eps=5e-3)
+        buf = pinned_u16((512, size, size))
+        for i in range(512):
+            buf[i] = uniq[i % 16]
+        rows_src[size] = (ref, buf)
+        lay = random_layouts(size, 8, size, (24, 48), (25, 225))
+        layouts[size] = [(srv.add_layout((size, size), b, side, fs, ref), b, side, fs) for b, side, fs in lay]
+    # parity of one row per size against the FP64 oracle (not timed)
+    errs = []
+    for size in (512, 1024):
+        lid, begins, side, fs = layouts[size][0]
+        ref, buf = rows_src[size]
+        offs, coefs, _ = srv.wait(srv.submit(lid, buf[:2]))
+        o, c, _ = eo.get_offsets(ref, buf[:2], begins, side, side, eo.POLICY_FFT, fs)
+        ok = well_posed(c, fs)
+        errs.append(float(np.abs(offs - o)[ok].max()))
+    srv.reset_stats()
+    # arrivals
+    pending, sent_pairs = [], 0
+    t_end = time.perf_counter() + args.duration
+    with ClockSampler(0) as clk:
+        t = time.perf_counter()
+        while t < t_end:
+            size = 512 if rng.random() < 0.5 else 1024
+            lid, begins, side, fs = layouts[size][int(rng.integers(0, 8))]
+            n = int(rng.integers(32, 513))
+            pending.append(srv.submit(lid, rows_src[size][1][:n]))
+            sent_pairs += n * len(begins)
+            t += rng.exponential(1.0 / args.rate)
+            delay = t - time.perf_counter()
+            if delay > 0:
+                time.sleep(delay)
+        for rid in pending:
+            srv.wait(rid)
+    st = srv.stats()
+    print(json.dumps({
+        "metric": "row latency p50/p99 and ROI pairs/s under a Poisson stream of scan rows",
+        "value": st["pairs_per_s"], "unit": "ROI pairs/s", "n_gpus": 1,
+        "latency_ms": {"p50": st["p50_ms"], "p99": st["p99_ms"]}, "rows": st["completed"],
+        "pairs": sent_pairs, "higher_is_better": True,
+        "dtype": "f32" if args.precision == "float" else "f64", "data": "synthetic",
+        "config": {"workload": "Poisson rows: 32-512 patterns of 512^2 or 1024^2 (50/50), 8 layouts "
+                               "per size, 25-225 ROIs radius 24-48, fit 3-9",
+                   "rate_rows_per_s": args.rate, "duration_s": args.duration,
+                   "hbm_arena_bytes_per_size": 24 << 30, "step_patterns": 128},
+        "parity": {"max_abs_err_px": max(errs), "vs": "FP64 oracle, one row per size"},
+        "clocks": clk.summary()}), flush=True)
+    srv.close()
+
+
 def main():
     args = parse()
     rank, world, local = dist_env()
     if args.impl == "reference":
         return run_reference(args, rank, world)
+    if args.config == "batching":
+        return run_batching(args)
+    if args.config == "serving":
+        return run_serving(args)
 
     import __graft_entry__
     __graft_entry__.build_library()

@@ -350,3 +350,76 @@ class MultiLayout:
             self.close()
         except Exception:
             pass
+
+
+class Server:
+    """Request loop over multi-layout batches (emida_gb_server_*).
+
+    Rows of uint16 patterns are submitted against registered layouts; rows are
+    admitted while the device arena of their pattern size has room (`hbm_bytes`
+    per size) and computed in shared steps of up to `step_patterns` patterns.
+    """
+
+    def __init__(self, precision="float", hbm_bytes=8 << 30, step_patterns=64):
+        self.precision = _precision(precision)
+        h = ctypes.c_void_p()
+        _lib.call("emida_gb_server_create", self.precision, int(hbm_bytes), int(step_patterns),
+                  ctypes.byref(h))
+        self._h = h
+        self.rois = []
+        self._rows = {}
+
+    def add_layout(self, src_size, begins, side, fitsize, ref):
+        begins = np.ascontiguousarray(np.asarray(begins, dtype=np.uint32).reshape(-1, 2))
+        ref = np.ascontiguousarray(ref, dtype=np.uint16)
+        lid = ctypes.c_uint32()
+        _lib.call("emida_gb_server_add_layout", self._h, int(src_size[0]), int(src_size[1]),
+                  begins.ctypes.data_as(ctypes.POINTER(ctypes.c_uint32)), len(begins), int(side),
+                  int(fitsize), _ptr(ref), ctypes.byref(lid))
+        self.rois.append(len(begins))
+        return lid.value
+
+    def submit(self, layout_id, patterns):
+        """Queues a row; `patterns` ([n][h][w] uint16) is kept alive until wait()."""
+        patterns = np.ascontiguousarray(patterns, dtype=np.uint16)
+        rid = ctypes.c_uint64()
+        _lib.call("emida_gb_server_submit", self._h, int(layout_id), _ptr(patterns), len(patterns),
+                  ctypes.byref(rid))
+        self._rows[rid.value] = (patterns, layout_id)
+        return rid.value
+
+    def wait(self, request_id):
+        """(offsets [n*rois][2], coefs [n*rois][6], latency_ms) of a row."""
+        patterns, lid = self._rows[request_id]
+        n = len(patterns) * self.rois[lid]
+        offs = np.zeros((n, 2))
+        coefs = np.zeros((n, 6))
+        lat = ctypes.c_double()
+        try:
+            _lib.call("emida_gb_server_wait", self._h, ctypes.c_uint64(request_id), _dptr(offs),
+                      _dptr(coefs), ctypes.byref(lat))
+        finally:
+            del self._rows[request_id]
+        return offs, coefs, lat.value
+
+    def stats(self):
+        p50, p99, rate = ctypes.c_double(), ctypes.c_double(), ctypes.c_double()
+        done = ctypes.c_uint64()
+        _lib.call("emida_gb_server_stats", self._h, ctypes.byref(p50), ctypes.byref(p99),
+                  ctypes.byref(rate), ctypes.byref(done))
+        return {"p50_ms": p50.value, "p99_ms": p99.value, "pairs_per_s": rate.value,
+                "completed": done.value}
+
+    def reset_stats(self):
+        _lib.call("emida_gb_server_reset_stats", self._h)
+
+    def close(self):
+        if getattr(self, "_h", None) is not None and self._h.value:
+            _lib.lib().emida_gb_server_destroy(self._h)
+        self._h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass

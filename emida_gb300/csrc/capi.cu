@@ -249,6 +249,7 @@ int emida_gb::host::run_fused(emida_gb_handle *h, const void *pics, uint32_t pat
     a.begins = h->d_begins;
     a.n_rois = h->S;
     a.n_pairs = pats * h->S;
+    a.side = h->slice.x;
     a.ref_spec = h->d_ref_spec_cm;
     a.hann = h->d_hann_fused;
     a.twiddles = h->d_tw_row;
@@ -268,7 +269,7 @@ int emida_gb::host::run_fused(emida_gb_handle *h, const void *pics, uint32_t pat
             const cuuint64_t dims[3] = {h->src.x, h->src.y, pats};
             const cuuint64_t strides[2] = {(cuuint64_t)h->src.x * 2,
                                            (cuuint64_t)h->src.x * h->src.y * 2};
-            const cuuint32_t box[3] = {h->slice.x + 8, h->slice.y, 1};
+            const cuuint32_t box[3] = {(h->slice.x + 14) & ~7u, h->slice.y, 1};
             const cuuint32_t estr[3] = {1, 1, 1};
             if (enc(&map, CU_TENSOR_MAP_DATA_TYPE_UINT16, 3, const_cast<void *>(pics), dims,
                     strides, box, estr, CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_NONE,
@@ -400,12 +401,22 @@ int emida_gb_create(const emida_gb_params *p, emida_gb_handle **out)
     } else {
         h->cross = size2{p->cross_w, p->cross_h};
     }
-    const bool fusable = h->fft && fused_supported(h->w2, h->dbl);
+    // The fused kernel takes square ROIs up to 96 pixels (64 in FP64); a ROI
+    // whose 2*side is not one of its transform lengths is zero-padded into the
+    // next one, which leaves every lag of the 2*side-1 window unchanged.
+    const uint32_t fn = h->fft ? fused_size_for(p->slice_w, h->dbl) : 0;
+    const bool fusable = fn != 0;
     if (p->mode == EMIDA_GB_MODE_FUSED && !fusable) {
         delete h;
-        return fail(EMIDA_GB_UNSUPPORTED, "no fused kernel for this shape (FFT policy; ROI side 32, 48, 64, or 96 in FP32)");
+        return fail(EMIDA_GB_UNSUPPORTED,
+                    "no fused kernel for this shape (FFT policy, ROI side <= 96 in FP32, <= 64 in FP64)");
     }
     h->mode = (p->mode == EMIDA_GB_MODE_PLAIN || !fusable) ? EMIDA_GB_MODE_PLAIN : EMIDA_GB_MODE_FUSED;
+    if (h->mode == EMIDA_GB_MODE_FUSED) {
+        // the resident reference spectra are computed at the fused length
+        h->w2 = h->h2 = fn;
+        h->half = fn / 2 + 1;
+    }
 
     auto bail = [&](int st) {
         emida_gb_destroy(h);
@@ -750,6 +761,11 @@ int emida_gb_memset(void *p, int v, size_t bytes)
 int emida_gb_memcpy_h2d(void *d, const void *s, size_t bytes)
 {
     CK(cudaMemcpy(d, s, bytes, cudaMemcpyHostToDevice));
+    return EMIDA_GB_OK;
+}
+int emida_gb_memcpy_d2d(void *d, const void *s, size_t bytes)
+{
+    CK(cudaMemcpy(d, s, bytes, cudaMemcpyDeviceToDevice));
     return EMIDA_GB_OK;
 }
 int emida_gb_memcpy_d2h(void *d, const void *s, size_t bytes)

@@ -189,7 +189,11 @@ __global__ void __launch_bounds__(N * G / 4, fused_min_blocks(N, sizeof(T)))
     constexpr int GROUPS = N / 4;      // one pair of ROI rows per group in the row pass
     constexpr int THREADS = GROUPS * G;
     constexpr int WARPS = THREADS / 32;
-    constexpr int TW = H + 8;          // uint16 tile row (TMA box width)
+    // ROI side (<= H): smaller ROIs are zero-padded into this transform length
+    const int side = a.side;
+    // uint16 tile row = TMA box width: covers x offsets 0..7 and keeps the box
+    // a whole number of 16-byte units
+    const int TW = (side + 14) & ~7;
     constexpr bool U16 = sizeof(IN) == 2;
 
     using L = fused_layout<N, G, T>;
@@ -198,7 +202,7 @@ __global__ void __launch_bounds__(N * G / 4, fused_min_blocks(N, sizeof(T)))
     C *twf = reinterpret_cast<C *>(smem + L::tw_fwd);   // [E][G] forward inter-pass twiddles
     C *twi = reinterpret_cast<C *>(smem + L::tw_inv);   // [E][G] inverse
     T *hx = reinterpret_cast<T *>(smem + L::hann);      // hx[H] then hy[H]
-    T *hy = hx + H;
+    T *hy = hx + a.side;
     T *red_v = reinterpret_cast<T *>(smem + L::red_val);
     uint32_t *red_i = reinterpret_cast<uint32_t *>(smem + L::red_idx);
     double *red_s = reinterpret_cast<double *>(smem + L::red_sum);
@@ -223,7 +227,7 @@ __global__ void __launch_bounds__(N * G / 4, fused_min_blocks(N, sizeof(T)))
         twi[i] = cconj(w);
     }
     const T *ghann = reinterpret_cast<const T *>(a.hann);
-    for (int i = tid; i < 2 * H; i += THREADS) hx[i] = ghann[i];  // hx then hy
+    for (int i = tid; i < 2 * a.side; i += THREADS) hx[i] = ghann[i];  // hx then hy
     const bool tma = U16 && a.use_tma;
     if (tid == 0) {
         mbar_init(bar, 1);
@@ -241,7 +245,7 @@ __global__ void __launch_bounds__(N * G / 4, fused_min_blocks(N, sizeof(T)))
         const uint32_t pic = it.x;
         const uint2 b = a.begins[it.y];
         fence_proxy_async();
-        mbar_expect_tx(bar, TW * H * 2);
+        mbar_expect_tx(bar, TW * side * 2);
         tma_load_3d(t16, &tmap, (int)(b.x & ~7u), (int)b.y, (int)pic, bar);
     };
     if (tma && tid == 0 && blockIdx.x < a.n_pairs) issue_tile(blockIdx.x);
@@ -266,12 +270,12 @@ __global__ void __launch_bounds__(N * G / 4, fused_min_blocks(N, sizeof(T)))
                 const uint16_t *src = reinterpret_cast<const uint16_t *>(a.pics) +
                                       (size_t)pic * a.src_w * a.src_h +
                                       (size_t)beg.y * a.src_w + beg.x;
-                for (int i = tid; i < H * H; i += THREADS)
-                    t16[(i / H) * TW + xo + (i % H)] = src[(size_t)(i / H) * a.src_w + (i % H)];
+                for (int i = tid; i < side * side; i += THREADS)
+                    t16[(i / side) * TW + xo + (i % side)] = src[(size_t)(i / side) * a.src_w + (i % side)];
                 __syncthreads();
             }
             uint32_t acc = 0;
-            for (int i = tid; i < H * H; i += THREADS) acc += t16[(i / H) * TW + xo + (i % H)];
+            for (int i = tid; i < side * side; i += THREADS) acc += t16[(i / side) * TW + xo + (i % side)];
 #pragma unroll
             for (int o = 16; o; o >>= 1) acc += __shfl_xor_sync(0xffffffffu, acc, o);
             if (lane == 0) red_i[warp] = acc;
@@ -279,13 +283,13 @@ __global__ void __launch_bounds__(N * G / 4, fused_min_blocks(N, sizeof(T)))
             uint32_t total = 0;
 #pragma unroll
             for (int w = 0; w < WARPS; ++w) total += red_i[w];
-            mean = (T)total / (T)(H * H);
+            mean = (T)total / (T)(side * side);
         } else {
             const double *src = reinterpret_cast<const double *>(a.pics) +
                                 (size_t)pic * a.src_w * a.src_h + (size_t)beg.y * a.src_w + beg.x;
             double acc = 0;
-            for (int i = tid; i < H * H; i += THREADS) {
-                double v = src[(size_t)(i / H) * a.src_w + (i % H)];
+            for (int i = tid; i < side * side; i += THREADS) {
+                double v = src[(size_t)(i / side) * a.src_w + (i % side)];
                 t64[i] = v;
                 acc += v;
             }
@@ -296,28 +300,31 @@ __global__ void __launch_bounds__(N * G / 4, fused_min_blocks(N, sizeof(T)))
             double total = 0;
 #pragma unroll
             for (int w = 0; w < WARPS; ++w) total += red_s[w];
-            mean = (T)total / (T)(H * H);
+            mean = (T)total / (T)(side * side);
         }
 
         // ---- forward rows: pairs of real rows as one complex FFT ----------
         {
             const int ra = 2 * g, rb = ra + 1;
+            const bool live = ra < side;  // side is even: rb < side too
             C v[E];
 #pragma unroll
             for (int m = 0; m < E / 2; ++m) {
                 const int x = t + G * m;
-                T pa, pb;
-                if constexpr (U16) {
-                    pa = (T)t16[ra * TW + xo + x];
-                    pb = (T)t16[rb * TW + xo + x];
-                } else {
-                    pa = (T)t64[ra * H + x];
-                    pb = (T)t64[rb * H + x];
+                T pa = (T)0, pb = (T)0;
+                if (live && x < side) {
+                    if constexpr (U16) {
+                        pa = (T)t16[ra * TW + xo + x];
+                        pb = (T)t16[rb * TW + xo + x];
+                    } else {
+                        pa = (T)t64[ra * side + x];
+                        pb = (T)t64[rb * side + x];
+                    }
+                    pa -= mean;
+                    pb -= mean;
+                    pa = pa * hx[x] * hy[ra];
+                    pb = pb * hx[x] * hy[rb];
                 }
-                pa -= mean;
-                pb -= mean;
-                pa = pa * hx[x] * hy[ra];
-                pb = pb * hx[x] * hy[rb];
                 v[m] = cmake<C>(pa, pb);
             }
             row_line<N, C> line{S, ra};
@@ -460,14 +467,25 @@ __global__ void __launch_bounds__(N * G / 4, fused_min_blocks(N, sizeof(T)))
                 const uint32_t q = (uint32_t)policy_index(POLICY_FFT, x, y, N - 1, N - 1);
                 const uint32_t qy = q / N, qx = q % N;
                 T val = reinterpret_cast<T *>(sp<N>(S, qy, qx >> 1))[qx & 1];
+                // an unnormalised inverse of length N scales values by N^2:
+                // report them at the reference's (2*side)^2
+                if (2 * side != N) val *= (T)(4 * side * side) / (T)(N * N);
                 fbuf[slot * 81 + l] = val;
                 if (a.neigh) reinterpret_cast<T *>(a.neigh)[(size_t)out * s2 + l] = val;
             }
             if (lane == 0) {
+                // the argmax index as the reference reports it: in its own
+                // 2*side map (the same index unless the ROI was zero-padded)
+                uint32_t pref = pk;
+                if (2 * side != N) {
+                    const int ns = 2 * side, c0 = N / 2 - 1;
+                    const int lx = (int)mx - c0, ly = (int)my - c0;
+                    pref = (uint32_t)(((ly % ns + ns) % ns) * ns + ((lx % ns + ns) % ns));
+                }
                 fmeta[4 * slot] = out;
                 fmeta[4 * slot + 1] = mx | (my << 16);
-                fmeta[4 * slot + 2] = pk | ((uint32_t)s << 24);
-                fval[slot] = pv;
+                fmeta[4 * slot + 2] = pref | ((uint32_t)s << 24);
+                fval[slot] = 2 * side != N ? pv * ((T)(4 * side * side) / (T)(N * N)) : pv;
             }
             __syncwarp();
             const bool last = pair + gridDim.x >= a.n_pairs;
@@ -504,6 +522,13 @@ static cudaError_t launch_one(const fused_args &a, const CUtensorMap *tmap, int 
 bool fused_supported(uint32_t fft_n, bool dbl)
 {
     return fft_n == 64 || fft_n == 96 || fft_n == 128 || (fft_n == 192 && !dbl);
+}
+
+uint32_t fused_size_for(uint32_t side, bool dbl)
+{
+    for (uint32_t n : {64u, 96u, 128u, 192u})
+        if (2 * side <= n && fused_supported(n, dbl)) return n;
+    return 0;
 }
 
 template <int N, int G>

@@ -13,8 +13,9 @@ struct fused_args {
     const uint2 *begins;    // [n_rois] ROI top-left (x, y)
     uint32_t n_rois;
     uint32_t n_pairs;       // batch * n_rois
+    uint32_t side;          // ROI side; <= N/2, zero-padded to N when smaller
     const void *ref_spec;   // [n_rois][N/2 + 1][N] complex: column kx holds X[0..N-1][kx]
-    const void *hann;       // [2 * (N/2)]: x window then y window, element type T
+    const void *hann;       // [2 * side]: x window then y window, element type T
     const void *twiddles;   // [N] complex T: exp(-2 pi i j / N)
     const double *lstsq;    // (A^T A)^-1 A^T, 6 x s*s
     int fitsize;
@@ -38,8 +39,10 @@ __host__ __device__ inline int lstsq_offset(int s)
     return s == 3 ? 0 : s == 5 ? 54 : s == 7 ? 204 : 498;
 }
 
-// Transform sizes (2 * ROI side) with a fused kernel: 64, 96, 128 and, in FP32, 192.
+// Transform sizes with a fused kernel: 64, 96, 128 and, in FP32, 192.
 bool fused_supported(uint32_t fft_n, bool dbl);
+// The smallest fused transform that holds a zero-padded ROI of this side (0: none).
+uint32_t fused_size_for(uint32_t side, bool dbl);
 
 // grid <= 0: one wave of resident CTAs (occupancy x SM count).
 cudaError_t launch_fused(uint32_t fft_n, bool dbl, bool in_f64, const fused_args &a,

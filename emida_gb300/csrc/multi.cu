@@ -24,7 +24,8 @@ struct emida_gb_multi {
         emida_gb_handle *h = nullptr;  // reference spectra; staged runs when not fused
     };
     struct size_class {
-        uint32_t n = 0;  // transform length 2 * side
+        uint32_t n = 0;     // fused transform length (>= 2 * side)
+        uint32_t side = 0;  // ROI side of every layout in the class
         bool fused = false;
         std::vector<uint2> begins;
         uint2 *d_begins = nullptr;
@@ -89,19 +90,25 @@ struct plan {
     uint64_t total = 0;
 };
 
-int make_plan(emida_gb_multi *m, uint32_t patterns, const uint32_t *layout_of, plan &pl)
+// Entry p reads pattern slots[p] (p itself without a slot list) of the device
+// pattern array and writes its ROIs after those of entries 0..p-1.
+int make_plan(emida_gb_multi *m, uint32_t patterns, const uint32_t *layout_of, plan &pl,
+              const uint32_t *slots = nullptr, uint32_t arena = 0)
 {
     pl.items.assign(m->classes.size(), {});
     for (uint32_t p = 0; p < patterns; ++p) {
         if (layout_of[p] >= m->layouts.size())
             return fail(EMIDA_GB_INVALID_ARGUMENT, "pattern %u: unknown layout %u", p, layout_of[p]);
+        const uint32_t slot = slots ? slots[p] : p;
+        if (slots && slot >= arena)
+            return fail(EMIDA_GB_INVALID_ARGUMENT, "pattern %u: slot %u outside the array", p, slot);
         const auto &L = m->layouts[layout_of[p]];
         if (m->classes[L.cls].fused) {
             auto &v = pl.items[L.cls];
             for (uint32_t r = 0; r < L.n_rois; ++r)
-                v.push_back(make_uint4(p, L.roi_base + r, (uint32_t)(pl.total + r), (uint32_t)L.fitsize));
+                v.push_back(make_uint4(slot, L.roi_base + r, (uint32_t)(pl.total + r), (uint32_t)L.fitsize));
         } else {
-            pl.staged.push_back(staged_item{p, layout_of[p], pl.total});
+            pl.staged.push_back(staged_item{slot, layout_of[p], pl.total});
         }
         pl.total += L.n_rois;
     }
@@ -112,6 +119,8 @@ int make_plan(emida_gb_multi *m, uint32_t patterns, const uint32_t *layout_of, p
 int upload_plan(emida_gb_multi *m, const plan &pl, bool &realloc)
 {
     realloc = false;
+    // the work-list buffers are read by the previous run's kernels: let them finish
+    CK(cudaStreamSynchronize(m->stream));
     for (size_t c = 0; c < m->classes.size(); ++c) {
         auto &k = m->classes[c];
         const auto &v = pl.items[c];
@@ -148,6 +157,7 @@ int launch_plan(emida_gb_multi *m, const plan &pl, const void *pics, uint32_t pa
         a.begins = k.d_begins;
         a.n_rois = 1;
         a.n_pairs = (uint32_t)pl.items[c].size();
+        a.side = k.side;
         a.ref_spec = k.d_spec;
         a.hann = k.hann;
         a.twiddles = k.twiddles;
@@ -162,10 +172,10 @@ int launch_plan(emida_gb_multi *m, const plan &pl, const void *pics, uint32_t pa
         a.items = k.d_items;
         a.use_tma = 0;
         if (use_tma) {
-            const uint32_t side = k.n / 2;
+            const uint32_t side = k.side;
             const cuuint64_t dims[3] = {m->src_w, m->src_h, patterns};
             const cuuint64_t strides[2] = {(cuuint64_t)m->src_w * 2, (cuuint64_t)m->src_w * m->src_h * 2};
-            const cuuint32_t box[3] = {side + 8, side, 1};
+            const cuuint32_t box[3] = {(side + 14) & ~7u, side, 1};
             const cuuint32_t estr[3] = {1, 1, 1};
             if (get_encoder()(&map, CU_TENSOR_MAP_DATA_TYPE_UINT16, 3, const_cast<void *>(pics), dims,
                               strides, box, estr, CU_TENSOR_MAP_INTERLEAVE_NONE,
@@ -245,13 +255,16 @@ int emida_gb_multi_add_layout(emida_gb_multi *m, const uint32_t *begins, uint32_
     L.side = side;
     L.fitsize = fitsize;
     L.h = h;
-    const uint32_t n = 2 * side;
+    // one class per ROI side (the Hann windows differ); its transform length
+    // is the handle's (2 * side, or the fused length it is padded to)
+    const uint32_t n = h->w2;
     int cls = -1;
     for (size_t c = 0; c < m->classes.size(); ++c)
-        if (m->classes[c].n == n) cls = (int)c;
+        if (m->classes[c].side == side) cls = (int)c;
     if (cls < 0) {
         emida_gb_multi::size_class k;
         k.n = n;
+        k.side = side;
         k.fused = emida_gb_resolved_mode(h) == EMIDA_GB_MODE_FUSED;
         k.hann = h->d_hann_fused;
         k.twiddles = h->d_tw_row;
@@ -336,6 +349,23 @@ int emida_gb_multi_run(emida_gb_multi *m, const void *dev_patterns, uint32_t pat
     return EMIDA_GB_OK;
 }
 
+int emida_gb_multi_run_slots(emida_gb_multi *m, const void *dev_patterns, uint32_t arena,
+                             uint32_t patterns, const uint32_t *slots, const uint32_t *layout_of,
+                             double *dev_offsets, double *dev_coefs, void *dev_maxes)
+{
+    if (!m || !dev_patterns || !slots || !layout_of || !dev_offsets)
+        return fail(EMIDA_GB_INVALID_ARGUMENT, "null argument");
+    std::lock_guard<std::mutex> lk(m->mu);
+    plan pl;
+    CKS(make_plan(m, patterns, layout_of, pl, slots, arena));
+    drop_graph(m);
+    bool realloc = false;
+    CKS(upload_plan(m, pl, realloc));
+    return launch_plan(m, pl, dev_patterns, arena, dev_offsets, dev_coefs, dev_maxes);
+}
+
+void *emida_gb_multi_stream(emida_gb_multi *m) { return m ? (void *)m->stream : nullptr; }
+
 int emida_gb_multi_synchronize(emida_gb_multi *m)
 {
     if (!m) return fail(EMIDA_GB_INVALID_ARGUMENT, "null argument");
@@ -390,8 +420,8 @@ int emida_gb_multi_autotune(emida_gb_multi *m, const void *dev_patterns, uint32_
         }
         k.grid = best_grid;
         char line[160];
-        snprintf(line, sizeof line, "n=%u: %zu pairs, grid %d (%d per SM), %.3f ms\n", k.n,
-                 pl.items[c].size(), best_grid, best_grid / std::max(1, sms), best / 3);
+        snprintf(line, sizeof line, "side %u (n=%u): %zu pairs, grid %d (%d per SM), %.3f ms\n",
+                 k.side, k.n, pl.items[c].size(), best_grid, best_grid / std::max(1, sms), best / 3);
         rep += line;
     }
     cudaEventDestroy(a);

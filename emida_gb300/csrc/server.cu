@@ -1,0 +1,408 @@
+// server.cu -- a request loop over the multi-layout planner.  A request is a
+// scan row: n patterns of one size on one registered ROI layout (reference
+// spectra resident per layout).  Rows are admitted while the device pattern
+// arena of their size has room for all their patterns (admission by free
+// HBM), copied in on their own stream, and computed in steps that take
+// patterns from every admitted row in turn (continuous batching): a row that
+// arrives while others run joins the next step.  Each pattern size has its
+// own planner and streams, so their steps overlap on the device.  The
+// reference's counterpart is the load / GPU / finalize thread pipeline of
+// src/process_files.hpp:79-237, which runs one layout and one row at a time.
+#include <algorithm>
+#include <chrono>
+#include <condition_variable>
+#include <cstring>
+#include <deque>
+#include <map>
+#include <memory>
+#include <thread>
+#include <vector>
+
+#include "handle.cuh"
+
+using namespace emida_gb;
+using namespace emida_gb::host;
+
+namespace {
+
+using clock_t_ = std::chrono::steady_clock;
+
+struct request {
+    uint64_t id = 0;
+    uint32_t layout = 0, pool = 0, n = 0, rois = 0;
+    const uint16_t *host = nullptr;
+    std::vector<uint32_t> slots;
+    uint32_t next = 0, done = 0;  // patterns scheduled / finished
+    std::vector<double> offsets, coefs;
+    cudaEvent_t copied = nullptr;
+    bool admitted = false, complete = false;
+    int status = EMIDA_GB_OK;
+    clock_t_::time_point t_submit, t_done;
+};
+
+struct step {
+    struct part {
+        request *r;
+        uint32_t first, count;  // patterns of the request
+        uint64_t out;           // first output ROI of the part in this step
+    };
+    std::vector<part> parts;
+    std::vector<uint32_t> slots;
+    uint64_t rois = 0;
+    double *d_offs = nullptr, *d_coefs = nullptr, *h_offs = nullptr, *h_coefs = nullptr;
+    size_t cap = 0;  // ROIs
+    cudaEvent_t done = nullptr;
+    bool busy = false;
+};
+
+struct pool {
+    uint32_t w = 0, h = 0;
+    emida_gb_multi *m = nullptr;
+    uint16_t *arena = nullptr;
+    uint32_t slots = 0;
+    std::vector<uint32_t> free_slots;
+    cudaStream_t copy = nullptr, out = nullptr;
+    std::deque<request *> pending;
+    std::vector<request *> active;
+    size_t rr = 0;  // round-robin cursor over active rows
+    step steps[2];
+};
+
+}  // namespace
+
+struct emida_gb_server {
+    int precision = EMIDA_GB_FLOAT;
+    uint64_t budget = 0;
+    uint32_t step_patterns = 64;
+    std::vector<std::unique_ptr<pool>> pools;
+    struct layout_ref {
+        uint32_t pool, id, rois;
+    };
+    std::vector<layout_ref> layouts;
+    std::map<uint64_t, std::unique_ptr<request>> requests;
+    uint64_t next_id = 1;
+    std::vector<double> latencies;  // ms, completed rows
+    uint64_t pairs_done = 0;
+    clock_t_::time_point t_first;
+    bool started = false;
+    std::mutex mu;
+    std::condition_variable cv;  // submissions and completions
+    std::thread loop;
+    bool stop = false;
+    int error = EMIDA_GB_OK;
+    std::string error_msg;
+};
+
+namespace {
+
+int admit(emida_gb_server *sv, pool &p)
+{
+    while (!p.pending.empty()) {
+        request *r = p.pending.front();
+        if (p.free_slots.size() < r->n) break;  // wait for slots: rows are admitted whole
+        p.pending.pop_front();
+        r->slots.assign(p.free_slots.end() - r->n, p.free_slots.end());
+        p.free_slots.resize(p.free_slots.size() - r->n);
+        const size_t bytes = (size_t)p.w * p.h * 2;
+        for (uint32_t i = 0; i < r->n; ++i)
+            CK(cudaMemcpyAsync(p.arena + (size_t)r->slots[i] * p.w * p.h, r->host + i * (size_t)p.w * p.h,
+                               bytes, cudaMemcpyHostToDevice, p.copy));
+        CK(cudaEventCreateWithFlags(&r->copied, cudaEventDisableTiming));
+        CK(cudaEventRecord(r->copied, p.copy));
+        r->admitted = true;
+        p.active.push_back(r);
+    }
+    (void)sv;
+    return EMIDA_GB_OK;
+}
+
+int ensure_step_buffers(step &st, size_t rois)
+{
+    if (rois <= st.cap) return EMIDA_GB_OK;
+    if (st.d_offs) cudaFree(st.d_offs);
+    if (st.d_coefs) cudaFree(st.d_coefs);
+    if (st.h_offs) cudaFreeHost(st.h_offs);
+    if (st.h_coefs) cudaFreeHost(st.h_coefs);
+    st.d_offs = st.d_coefs = st.h_offs = st.h_coefs = nullptr;
+    const size_t cap = std::max(rois, 2 * st.cap);
+    CK(cudaMalloc((void **)&st.d_offs, cap * 2 * sizeof(double)));
+    CK(cudaMalloc((void **)&st.d_coefs, cap * 6 * sizeof(double)));
+    CK(cudaMallocHost((void **)&st.h_offs, cap * 2 * sizeof(double)));
+    CK(cudaMallocHost((void **)&st.h_coefs, cap * 6 * sizeof(double)));
+    st.cap = cap;
+    if (!st.done) CK(cudaEventCreateWithFlags(&st.done, cudaEventDisableTiming));
+    return EMIDA_GB_OK;
+}
+
+// Builds and queues one step from the rows whose patterns are on the device.
+int launch_step(emida_gb_server *sv, pool &p, step &st)
+{
+    st.parts.clear();
+    st.slots.clear();
+    std::vector<uint32_t> layout_of;
+    st.rois = 0;
+    uint32_t budget = sv->step_patterns;
+    const size_t na = p.active.size();
+    for (size_t k = 0; k < na && budget; ++k) {
+        request *r = p.active[(p.rr + k) % na];
+        if (r->next >= r->n) continue;
+        if (cudaEventQuery(r->copied) != cudaSuccess) continue;
+        // an even share per row keeps every row moving
+        uint32_t take = std::min(r->n - r->next, std::max(1u, sv->step_patterns / (uint32_t)na));
+        take = std::min(take, budget);
+        st.parts.push_back(step::part{r, r->next, take, st.rois});
+        for (uint32_t i = 0; i < take; ++i) {
+            st.slots.push_back(r->slots[r->next + i]);
+            layout_of.push_back(sv->layouts[r->layout].id);
+        }
+        st.rois += (uint64_t)take * r->rois;
+        r->next += take;
+        budget -= take;
+    }
+    p.rr = na ? (p.rr + 1) % na : 0;
+    if (st.parts.empty()) return EMIDA_GB_OK;
+    CKS(ensure_step_buffers(st, st.rois));
+    CKS(emida_gb_multi_run_slots(p.m, p.arena, p.slots, (uint32_t)st.slots.size(), st.slots.data(),
+                                 layout_of.data(), st.d_offs, st.d_coefs, nullptr));
+    cudaStream_t ms = (cudaStream_t)emida_gb_multi_stream(p.m);
+    CK(cudaEventRecord(st.done, ms));
+    CK(cudaStreamWaitEvent(p.out, st.done, 0));
+    CK(cudaMemcpyAsync(st.h_offs, st.d_offs, st.rois * 2 * sizeof(double), cudaMemcpyDeviceToHost, p.out));
+    CK(cudaMemcpyAsync(st.h_coefs, st.d_coefs, st.rois * 6 * sizeof(double), cudaMemcpyDeviceToHost, p.out));
+    CK(cudaEventRecord(st.done, p.out));
+    st.busy = true;
+    return EMIDA_GB_OK;
+}
+
+// Hands a finished step's results to its rows; frees their arena slots.
+void retire_step(emida_gb_server *sv, pool &p, step &st)
+{
+    for (const auto &part : st.parts) {
+        request *r = part.r;
+        const size_t n = (size_t)part.count * r->rois;
+        const size_t at = (size_t)part.first * r->rois;
+        std::memcpy(r->offsets.data() + 2 * at, st.h_offs + 2 * part.out, n * 2 * sizeof(double));
+        std::memcpy(r->coefs.data() + 6 * at, st.h_coefs + 6 * part.out, n * 6 * sizeof(double));
+        for (uint32_t i = 0; i < part.count; ++i) p.free_slots.push_back(r->slots[part.first + i]);
+        r->done += part.count;
+        sv->pairs_done += n;
+        if (r->done == r->n) {
+            r->complete = true;
+            r->t_done = clock_t_::now();
+            sv->latencies.push_back(
+                std::chrono::duration<double, std::milli>(r->t_done - r->t_submit).count());
+            p.active.erase(std::find(p.active.begin(), p.active.end(), r));
+            cudaEventDestroy(r->copied);
+            r->copied = nullptr;
+        }
+    }
+    st.parts.clear();
+    st.busy = false;
+}
+
+void server_loop(emida_gb_server *sv)
+{
+    std::unique_lock<std::mutex> lk(sv->mu);
+    while (!sv->stop) {
+        bool progress = false;
+        for (auto &pp : sv->pools) {
+            pool &p = *pp;
+            for (auto &st : p.steps)
+                if (st.busy && cudaEventQuery(st.done) == cudaSuccess) {
+                    retire_step(sv, p, st);
+                    progress = true;
+                }
+            int rc = admit(sv, p);
+            for (auto &st : p.steps)
+                if (rc == EMIDA_GB_OK && !st.busy && !p.active.empty()) rc = launch_step(sv, p, st);
+            if (rc != EMIDA_GB_OK) {
+                // a failed launch fails the rows it would have served
+                sv->error = rc;
+                sv->error_msg = emida_gb_last_error();
+                for (request *r : p.active) {
+                    r->status = rc;
+                    r->complete = true;
+                }
+                p.active.clear();
+                progress = true;
+            }
+        }
+        if (progress) sv->cv.notify_all();
+        bool busy = false;
+        for (auto &pp : sv->pools)
+            busy |= !pp->active.empty() || !pp->pending.empty();
+        if (busy)
+            sv->cv.wait_for(lk, std::chrono::microseconds(50));
+        else
+            sv->cv.wait_for(lk, std::chrono::milliseconds(20));
+    }
+}
+
+}  // namespace
+
+extern "C" {
+
+int emida_gb_server_create(int32_t precision, uint64_t hbm_bytes, uint32_t step_patterns,
+                           emida_gb_server **out)
+{
+    if (!out) return fail(EMIDA_GB_INVALID_ARGUMENT, "null output");
+    *out = nullptr;
+    if (precision != EMIDA_GB_DOUBLE && precision != EMIDA_GB_FLOAT)
+        return fail(EMIDA_GB_INVALID_ARGUMENT, "invalid precision %d", precision);
+    if (step_patterns == 0) return fail(EMIDA_GB_INVALID_ARGUMENT, "step_patterns must be > 0");
+    auto sv = std::make_unique<emida_gb_server>();
+    sv->precision = precision;
+    sv->budget = hbm_bytes;
+    sv->step_patterns = step_patterns;
+    sv->loop = std::thread(server_loop, sv.get());
+    *out = sv.release();
+    return EMIDA_GB_OK;
+}
+
+int emida_gb_server_add_layout(emida_gb_server *sv, uint32_t src_w, uint32_t src_h,
+                               const uint32_t *begins, uint32_t n_rois, uint32_t side,
+                               int32_t fitsize, const uint16_t *ref, uint32_t *layout_id)
+{
+    if (!sv || !layout_id) return fail(EMIDA_GB_INVALID_ARGUMENT, "null argument");
+    std::lock_guard<std::mutex> lk(sv->mu);
+    uint32_t pi = 0;
+    while (pi < sv->pools.size() && !(sv->pools[pi]->w == src_w && sv->pools[pi]->h == src_h)) ++pi;
+    if (pi == sv->pools.size()) {
+        auto p = std::make_unique<pool>();
+        p->w = src_w;
+        p->h = src_h;
+        const size_t bytes = (size_t)src_w * src_h * 2;
+        p->slots = (uint32_t)std::min<uint64_t>(sv->budget / bytes, 1u << 20);
+        if (p->slots == 0) return fail(EMIDA_GB_INVALID_ARGUMENT, "the HBM budget holds no pattern");
+        CKS(emida_gb_multi_create(src_w, src_h, sv->precision, &p->m));
+        CK(cudaMalloc((void **)&p->arena, (size_t)p->slots * bytes));
+        for (uint32_t s = 0; s < p->slots; ++s) p->free_slots.push_back(p->slots - 1 - s);
+        CK(cudaStreamCreateWithFlags(&p->copy, cudaStreamNonBlocking));
+        CK(cudaStreamCreateWithFlags(&p->out, cudaStreamNonBlocking));
+        sv->pools.push_back(std::move(p));
+    }
+    uint32_t id = 0;
+    CKS(emida_gb_multi_add_layout(sv->pools[pi]->m, begins, n_rois, side, fitsize, ref, &id));
+    sv->layouts.push_back({pi, id, n_rois});
+    *layout_id = (uint32_t)sv->layouts.size() - 1;
+    return EMIDA_GB_OK;
+}
+
+int emida_gb_server_submit(emida_gb_server *sv, uint32_t layout_id, const uint16_t *patterns,
+                           uint32_t n, uint64_t *request_id)
+{
+    if (!sv || !patterns || !request_id || n == 0) return fail(EMIDA_GB_INVALID_ARGUMENT, "bad argument");
+    std::lock_guard<std::mutex> lk(sv->mu);
+    if (layout_id >= sv->layouts.size()) return fail(EMIDA_GB_INVALID_ARGUMENT, "unknown layout %u", layout_id);
+    const auto &L = sv->layouts[layout_id];
+    pool &p = *sv->pools[L.pool];
+    if (n > p.slots)
+        return fail(EMIDA_GB_INVALID_ARGUMENT, "a row of %u patterns exceeds the %u-pattern arena", n, p.slots);
+    auto r = std::make_unique<request>();
+    r->id = sv->next_id++;
+    r->layout = layout_id;
+    r->pool = L.pool;
+    r->n = n;
+    r->rois = L.rois;
+    r->host = patterns;
+    r->offsets.assign((size_t)n * L.rois * 2, 0.0);
+    r->coefs.assign((size_t)n * L.rois * 6, 0.0);
+    r->t_submit = clock_t_::now();
+    if (!sv->started) {
+        sv->started = true;
+        sv->t_first = r->t_submit;
+    }
+    p.pending.push_back(r.get());
+    *request_id = r->id;
+    sv->requests[r->id] = std::move(r);
+    sv->cv.notify_all();
+    return EMIDA_GB_OK;
+}
+
+int emida_gb_server_wait(emida_gb_server *sv, uint64_t request_id, double *offsets, double *coefs,
+                         double *latency_ms)
+{
+    if (!sv) return fail(EMIDA_GB_INVALID_ARGUMENT, "null argument");
+    std::unique_lock<std::mutex> lk(sv->mu);
+    auto it = sv->requests.find(request_id);
+    if (it == sv->requests.end())
+        return fail(EMIDA_GB_INVALID_ARGUMENT, "unknown request %llu", (unsigned long long)request_id);
+    request *r = it->second.get();
+    sv->cv.wait(lk, [&] { return r->complete; });
+    const int st = r->status;
+    if (st == EMIDA_GB_OK) {
+        if (offsets) std::memcpy(offsets, r->offsets.data(), r->offsets.size() * sizeof(double));
+        if (coefs) std::memcpy(coefs, r->coefs.data(), r->coefs.size() * sizeof(double));
+        if (latency_ms) *latency_ms = std::chrono::duration<double, std::milli>(r->t_done - r->t_submit).count();
+    }
+    sv->requests.erase(it);
+    if (st != EMIDA_GB_OK) return fail(st, "request failed: %s", sv->error_msg.c_str());
+    return EMIDA_GB_OK;
+}
+
+int emida_gb_server_stats(emida_gb_server *sv, double *p50_ms, double *p99_ms, double *pairs_per_s,
+                          uint64_t *completed)
+{
+    if (!sv) return fail(EMIDA_GB_INVALID_ARGUMENT, "null argument");
+    std::lock_guard<std::mutex> lk(sv->mu);
+    std::vector<double> l = sv->latencies;
+    std::sort(l.begin(), l.end());
+    auto pct = [&](double q) {
+        if (l.empty()) return 0.0;
+        const size_t i = std::min(l.size() - 1, (size_t)(q * (l.size() - 1) + 0.5));
+        return l[i];
+    };
+    if (p50_ms) *p50_ms = pct(0.50);
+    if (p99_ms) *p99_ms = pct(0.99);
+    if (completed) *completed = l.size();
+    if (pairs_per_s) {
+        const double s = sv->started ? std::chrono::duration<double>(clock_t_::now() - sv->t_first).count() : 0;
+        *pairs_per_s = s > 0 ? sv->pairs_done / s : 0;
+    }
+    return EMIDA_GB_OK;
+}
+
+int emida_gb_server_reset_stats(emida_gb_server *sv)
+{
+    if (!sv) return fail(EMIDA_GB_INVALID_ARGUMENT, "null argument");
+    std::lock_guard<std::mutex> lk(sv->mu);
+    sv->latencies.clear();
+    sv->pairs_done = 0;
+    sv->started = false;
+    return EMIDA_GB_OK;
+}
+
+void emida_gb_server_destroy(emida_gb_server *sv)
+{
+    if (!sv) return;
+    {
+        std::lock_guard<std::mutex> lk(sv->mu);
+        sv->stop = true;
+        sv->cv.notify_all();
+    }
+    if (sv->loop.joinable()) sv->loop.join();
+    for (auto &pp : sv->pools)
+        if (pp->copy) cudaStreamSynchronize(pp->copy);
+    for (auto &kv : sv->requests)
+        if (kv.second->copied) cudaEventDestroy(kv.second->copied);
+    for (auto &pp : sv->pools) {
+        pool &p = *pp;
+        if (p.m) emida_gb_multi_synchronize(p.m);
+        if (p.copy) cudaStreamSynchronize(p.copy);
+        if (p.out) cudaStreamSynchronize(p.out);
+        for (auto &st : p.steps) {
+            if (st.d_offs) cudaFree(st.d_offs);
+            if (st.d_coefs) cudaFree(st.d_coefs);
+            if (st.h_offs) cudaFreeHost(st.h_offs);
+            if (st.h_coefs) cudaFreeHost(st.h_coefs);
+            if (st.done) cudaEventDestroy(st.done);
+        }
+        if (p.arena) cudaFree(p.arena);
+        if (p.copy) cudaStreamDestroy(p.copy);
+        if (p.out) cudaStreamDestroy(p.out);
+        emida_gb_multi_destroy(p.m);
+    }
+    delete sv;
+}
+
+}  // extern "C"

@@ -155,6 +155,13 @@ int emida_gb_multi_count(const emida_gb_multi *m, uint32_t patterns, const uint3
 int emida_gb_multi_run(emida_gb_multi *m, const void *dev_patterns, uint32_t patterns,
                        const uint32_t *layout_of, double *dev_offsets, double *dev_coefs,
                        void *dev_maxes, int use_graph);
+/* The same for patterns at arbitrary positions of a device pattern array of
+ * `arena` patterns: entry p reads pattern slots[p]; no graph. */
+int emida_gb_multi_run_slots(emida_gb_multi *m, const void *dev_patterns, uint32_t arena,
+                             uint32_t patterns, const uint32_t *slots, const uint32_t *layout_of,
+                             double *dev_offsets, double *dev_coefs, void *dev_maxes);
+/* The planner's stream (a cudaStream_t) and a wait for its work. */
+void *emida_gb_multi_stream(emida_gb_multi *m);
 int emida_gb_multi_synchronize(emida_gb_multi *m);
 /* Times each fused transform size with 1..4 resident CTAs per SM on these
  * patterns and keeps the fastest grid; writes a one-line-per-size report. */
@@ -163,6 +170,33 @@ int emida_gb_multi_autotune(emida_gb_multi *m, const void *dev_patterns, uint32_
                             size_t report_len);
 void emida_gb_multi_destroy(emida_gb_multi *m);
 
+/* ---- serving: a request loop over multi-layout batches ----------------------
+ * No counterpart in the reference (its process_files pipeline runs one layout,
+ * one row at a time).  A request is a scan row of n uint16 patterns on one
+ * registered layout.  Rows wait until the device pattern arena of their size
+ * (hbm_bytes per pattern size) can hold all their patterns, then are copied in
+ * and computed in steps of up to step_patterns patterns drawn from every
+ * admitted row in turn, so rows that arrive while others run share the next
+ * steps.  The host patterns must stay valid until the request is waited for;
+ * pinned memory lets the copies overlap.  Results are per row, pattern-major. */
+typedef struct emida_gb_server emida_gb_server;
+int emida_gb_server_create(int32_t precision, uint64_t hbm_bytes, uint32_t step_patterns,
+                           emida_gb_server **out);
+int emida_gb_server_add_layout(emida_gb_server *s, uint32_t src_w, uint32_t src_h,
+                               const uint32_t *begins, uint32_t n_rois, uint32_t side,
+                               int32_t fitsize, const uint16_t *ref, uint32_t *layout_id);
+int emida_gb_server_submit(emida_gb_server *s, uint32_t layout_id, const uint16_t *patterns,
+                           uint32_t n, uint64_t *request_id);
+/* Blocks until the row is done; offsets [n*rois][2], coefs [n*rois][6] may be
+ * NULL; latency_ms = submission to completion. */
+int emida_gb_server_wait(emida_gb_server *s, uint64_t request_id, double *offsets, double *coefs,
+                         double *latency_ms);
+/* p50/p99 row latency of completed rows and ROI pairs/s since the first submission. */
+int emida_gb_server_stats(emida_gb_server *s, double *p50_ms, double *p99_ms,
+                          double *pairs_per_s, uint64_t *completed);
+int emida_gb_server_reset_stats(emida_gb_server *s);
+void emida_gb_server_destroy(emida_gb_server *s);
+
 /* ---- device memory helpers (for callers without a CUDA runtime binding) --- */
 int emida_gb_device_count(int *count);
 int emida_gb_malloc(void **dev_ptr, size_t bytes);
@@ -170,6 +204,7 @@ int emida_gb_free(void *dev_ptr);
 int emida_gb_memset(void *dev_ptr, int value, size_t bytes);
 int emida_gb_memcpy_h2d(void *dev_dst, const void *host_src, size_t bytes);
 int emida_gb_memcpy_d2h(void *host_dst, const void *dev_src, size_t bytes);
+int emida_gb_memcpy_d2d(void *dev_dst, const void *dev_src, size_t bytes);
 int emida_gb_malloc_host(void **host_ptr, size_t bytes);
 int emida_gb_free_host(void *host_ptr);
 int emida_gb_synchronize(void);

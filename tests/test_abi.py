@@ -91,11 +91,13 @@ def test_no_cpu_fallback_when_library_missing(tmp_path, monkeypatch):
 
 
 def test_fused_form_availability(lib):
-    # FP64 192-point spectra do not fit in shared memory: the fused form is
-    # refused explicitly, "auto" falls back to the staged form (a GPU path)
+    # FP64 192-point spectra do not fit in shared memory and no fused
+    # transform holds a 100-pixel ROI: the fused form is refused explicitly,
+    # "auto" takes the staged form there (a GPU path)
     from emida_gb300 import EmidaError, GpuOffset
     with pytest.raises(EmidaError, match="no fused kernel"):
         GpuOffset((256, 256), [(0, 0)], (96, 96), (191, 191), 1, "fft", 3, 1, "double",
                   mode="fused")
     with pytest.raises(EmidaError, match="no fused kernel"):
-        GpuOffset((256, 256), [(0, 0)], (40, 40), (79, 79), 1, "fft", 3, 1, "float", mode="fused")
+        GpuOffset((256, 256), [(0, 0)], (100, 100), (199, 199), 1, "fft", 3, 1, "float",
+                  mode="fused")

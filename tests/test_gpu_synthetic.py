@@ -121,6 +121,24 @@ def test_fused_radius24_48(data512, radius, precision, tol):
     assert np.array_equal(p[2], o_peaks)
 
 
+@pytest.mark.parametrize("side,precision,tol", [(40, "float", 1e-3), (40, "double", 1e-9),
+                                                (50, "float", 1e-3), (76, "float", 1e-3),
+                                                (58, "double", 1e-9)])
+def test_fused_zero_padded_sides(data512, side, precision, tol):
+    # ROI sides whose 2*side is not a fused length are zero-padded into the next
+    # one (96, 128, 192): every lag of the 2*side-1 window is unchanged, and the
+    # peak index is reported in the reference's 2*side map.
+    from emida_gb300 import synth
+    ref, pics = data512
+    _, begins = synth.roi_grid(512, 4, side // 2, margin=side // 2 + 8)
+    offs, coefs, peaks = run(ref, pics[:2], begins, side, "fft", 5, precision, "fused")
+    o_offs, o_coefs, o_peaks = oracle(ref, pics[:2], begins, side, "fft", 5)
+    assert np.array_equal(peaks, o_peaks)
+    assert_offsets(offs, coefs, o_offs, o_coefs, 5, tol)
+    p = run(ref, pics[:2], begins, side, "fft", 5, precision, "plain")
+    assert np.array_equal(p[2], o_peaks)
+
+
 def test_fused_equals_plain_peaks_and_border_rois(data512):
     # ROIs touching every border and with x not a multiple of 8 (TMA x rounding)
     ref, pics = data512
