@@ -36,6 +36,8 @@ import numpy as np
 ROOT = os.path.dirname(os.path.abspath(__file__))
 sys.path.insert(0, ROOT)
 
+from emida_gb300.shard import dist_env, max_over_ranks, whole_job_rate  # noqa: E402
+
 METRIC = "ROI pairs/s at <=0.01 px vs FP64 oracle"
 UNIQUE = 32
 # DRAM traffic of the fused FP32 kernel on this workload, from one ncu capture
@@ -63,13 +65,6 @@ def parse():
     ap.add_argument("--rate", type=float, default=50.0, help="serving: rows per second")
     ap.add_argument("--duration", type=float, default=8.0, help="serving: seconds of arrivals")
     return ap.parse_args()
-
-
-def dist_env():
-    rank = int(os.environ.get("RANK", "0"))
-    world = int(os.environ.get("WORLD_SIZE", "1"))
-    local = int(os.environ.get("LOCAL_RANK", "0"))
-    return rank, world, local
 
 
 def workload(seed=2024):
@@ -382,7 +377,7 @@ def main():
         torch.cuda.set_device(local)
         dist.init_process_group("nccl")
     import ctypes
-    ctypes.CDLL(_lib.LIB_PATH)  # loaded before any device use
+    _lib.call("emida_gb_set_device", local)  # the library keeps its own current device
 
     ref, uniq, begins = workload()
     P = args.patterns
@@ -429,13 +424,9 @@ def main():
         ms = g.time_device(d_pics, P, d_offs, args.steps)
     _lib.call("emida_gb_synchronize")
     barrier()
-    if dist is not None:
-        import torch
-        t = torch.tensor([ms], device="cuda")
-        dist.all_reduce(t, op=dist.ReduceOp.MAX)
-        ms = float(t.item())
+    ms = max_over_ranks(ms, dist, device="cuda")
     ms_step = ms / args.steps
-    value = world * pairs_per_step / (ms_step / 1000.0)
+    value = whole_job_rate(pairs_per_step, ms_step / 1000.0, world)
 
     # per-launch duration of the dominant kernel (fused: one launch per step)
     launches = g.launches_per_run()
@@ -486,8 +477,8 @@ def main():
     for _ in range(e2e_steps):
         e2e_step()
     barrier()
-    e2e_ms = (time.perf_counter() - t0) * 1000 / e2e_steps
-    e2e_value = world * pairs_per_step / (e2e_ms / 1000.0)
+    e2e_ms = max_over_ranks((time.perf_counter() - t0) * 1000 / e2e_steps, dist, device="cuda")
+    e2e_value = whole_job_rate(pairs_per_step, e2e_ms / 1000.0, world)
     _lib.call("emida_gb_free_host", hbuf)
 
     cpu = None

@@ -85,6 +85,7 @@ SIGNATURES = {
     "emida_gb_subpixel_max": [_DP, _I32, _U32, _DP, _DP],
     "emida_gb_lstsq_matrix": [_I32, _DP],
     "emida_gb_device_count": [ctypes.POINTER(_I32)],
+    "emida_gb_set_device": [_I32],
     "emida_gb_malloc": [ctypes.POINTER(_VP), _SZ],
     "emida_gb_free": [_VP],
     "emida_gb_memset": [_VP, _I32, _SZ],

@@ -738,6 +738,12 @@ void emida_gb_destroy(emida_gb_handle *h)
 }
 
 // ---- memory helpers -----------------------------------------------------------
+int emida_gb_set_device(int device)
+{
+    CK(cudaSetDevice(device));
+    return EMIDA_GB_OK;
+}
+
 int emida_gb_device_count(int *count)
 {
     CK(cudaGetDeviceCount(count));

@@ -199,6 +199,8 @@ void emida_gb_server_destroy(emida_gb_server *s);
 
 /* ---- device memory helpers (for callers without a CUDA runtime binding) --- */
 int emida_gb_device_count(int *count);
+/* Device for this thread's subsequent handles and helpers (one process per GPU). */
+int emida_gb_set_device(int device);
 int emida_gb_malloc(void **dev_ptr, size_t bytes);
 int emida_gb_free(void *dev_ptr);
 int emida_gb_memset(void *dev_ptr, int value, size_t bytes);

@@ -70,6 +70,8 @@ def test_cli_end_to_end_matches_oracle(tmp_path, policy, precision, fit, tol):
             vals = np.array([float(v) for v in row[2:4]])
             assert np.abs(vals - o_offs[k]).max() <= tol + 1e-6
             assert len(row) == 10  # -q: six coefficients
-            # "%f" keeps six decimals of each coefficient
-            assert np.allclose([float(v) for v in row[4:]], o_coefs[k],
-                               rtol=1e-4 if precision == "float" else 1e-9, atol=1e-6)
+            # "%f" keeps six decimals of each coefficient; the fit's rounding error
+            # scales with the largest coefficient (the map's peak), not each one
+            scale = np.abs(o_coefs[k]).max()
+            rel = 1e-5 if precision == "float" else 1e-9
+            assert np.abs(np.array([float(v) for v in row[4:]]) - o_coefs[k]).max() <= rel * scale + 1e-6
