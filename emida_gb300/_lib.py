@@ -101,6 +101,7 @@ SIGNATURES = {
                              _U32, _U32, _U32, _U32],
     "emida_gb_run_cross_corr": [_VP, _VP, _VP, _I32, _U32, _U32, _U32, _U32, _U32, _U32],
     "emida_gb_run_fft_r2c": [_VP, _VP, _U32, _U32, _U32, _I32],
+    "emida_gb_run_fft_r2c_noalloc": [_VP, _VP, _U32, _U32, _U32, _I32],
     "emida_gb_run_fft_c2r": [_VP, _VP, _U32, _U32, _U32, _I32],
     "emida_gb_run_hadamard": [_VP, _VP, _U32, _U32, _U32, _I32],
     "emida_gb_run_maxarg": [_VP, _U32, _U32, _VP, _I32],

@@ -869,6 +869,98 @@ int emida_gb_run_fft_c2r(void *spec, void *real_out, uint32_t maps, uint32_t w2,
     return st;
 }
 
+}  // extern "C"
+
+// ---- allocation-free forward FFT --------------------------------------------------
+// emida_gb_run_fft_r2c builds its two twiddle tables in cudaMalloc'd memory and
+// frees them on return.  The variant below keeps them in one fixed device array
+// instead: the row table at byte 0, the column table at byte NOALLOC_COL_OFFSET,
+// each up to NOALLOC_MAX_SIDE complex doubles, 32 KiB in all.
+namespace {
+
+constexpr uint32_t NOALLOC_MAX_SIDE = 1024;
+constexpr size_t NOALLOC_COL_OFFSET = NOALLOC_MAX_SIDE * sizeof(double2);
+constexpr int NOALLOC_MAX_DEVICES = 64;
+
+__device__ __align__(256) unsigned char g_noalloc_twiddles[2 * NOALLOC_COL_OFFSET];
+
+std::mutex g_noalloc_mutex;
+void *g_noalloc_ptr[NOALLOC_MAX_DEVICES];  // device address of the array, per device
+
+// Address of g_noalloc_twiddles on the current device, looked up on the first
+// call made with that device current and cached afterwards.
+int noalloc_scratch(void **out)
+{
+    int dev = 0;
+    CK(cudaGetDevice(&dev));
+    if (dev < 0 || dev >= NOALLOC_MAX_DEVICES)
+        return fail(EMIDA_GB_UNSUPPORTED, "fft r2c (no-alloc): device %d beyond the %d supported",
+                    dev, NOALLOC_MAX_DEVICES);
+    std::lock_guard<std::mutex> lock(g_noalloc_mutex);
+    if (!g_noalloc_ptr[dev]) {
+        void *p = nullptr;
+        cudaError_t e = cudaGetSymbolAddress(&p, g_noalloc_twiddles);
+        if (e != cudaSuccess || !p)
+            return fail(EMIDA_GB_CUDA_ERROR, "fft r2c (no-alloc): scratch address on device %d: %s",
+                        dev, cudaGetErrorString(e));
+        g_noalloc_ptr[dev] = p;
+    }
+    *out = g_noalloc_ptr[dev];
+    return EMIDA_GB_OK;
+}
+
+// The same values emida_gb::host::upload_twiddles computes, written into a
+// caller-provided host array.
+template <typename C> void twiddles_into(C *w, uint32_t n)
+{
+    const double PI = 3.14159265358979323846;
+    for (uint32_t j = 0; j < n; ++j) {
+        if constexpr (sizeof(C) == sizeof(double2))
+            w[j] = make_double2(std::cos(2 * PI * j / n), -std::sin(2 * PI * j / n));
+        else
+            w[j] = make_float2((float)std::cos(2 * PI * j / n), (float)-std::sin(2 * PI * j / n));
+    }
+}
+
+template <typename C>
+int fft_r2c_noalloc(const void *real_in, void *spec, uint32_t maps, uint32_t w2, uint32_t h2,
+                    unsigned char *scratch)
+{
+    // Host staging on the stack: two tables of at most NOALLOC_MAX_SIDE entries.
+    C row[NOALLOC_MAX_SIDE], col[NOALLOC_MAX_SIDE];
+    twiddles_into(row, w2);
+    twiddles_into(col, h2);
+    CK(cudaMemcpy(scratch, row, w2 * sizeof(C), cudaMemcpyHostToDevice));
+    CK(cudaMemcpy(scratch + NOALLOC_COL_OFFSET, col, h2 * sizeof(C), cudaMemcpyHostToDevice));
+    const fft_tables t{scratch, scratch + NOALLOC_COL_OFFSET, w2, h2};
+    CK(run_fft_r2c(real_in, spec, maps, t, sizeof(C) == sizeof(double2), 0));
+    CK(cudaDeviceSynchronize());
+    return EMIDA_GB_OK;
+}
+
+}  // namespace
+
+extern "C" {
+
+int emida_gb_run_fft_r2c_noalloc(const void *real_in, void *spec, uint32_t maps, uint32_t w2,
+                                 uint32_t h2, int precision)
+{
+    if (precision != EMIDA_GB_DOUBLE && precision != EMIDA_GB_FLOAT)
+        return fail(EMIDA_GB_INVALID_ARGUMENT, "fft r2c (no-alloc): unknown precision %d", precision);
+    if (w2 == 0 || h2 == 0 || w2 > NOALLOC_MAX_SIDE || h2 > NOALLOC_MAX_SIDE)
+        return fail(EMIDA_GB_INVALID_ARGUMENT,
+                    "fft r2c (no-alloc): transform %u x %u outside 1..%u per side (the fixed "
+                    "twiddle scratch holds %u entries per table)",
+                    w2, h2, NOALLOC_MAX_SIDE, NOALLOC_MAX_SIDE);
+    if (maps == 0) return EMIDA_GB_OK;
+    if (!real_in || !spec) return fail(EMIDA_GB_INVALID_ARGUMENT, "fft r2c (no-alloc): null buffer");
+    void *scratch = nullptr;
+    CKS(noalloc_scratch(&scratch));
+    auto *s = static_cast<unsigned char *>(scratch);
+    return precision == EMIDA_GB_DOUBLE ? fft_r2c_noalloc<double2>(real_in, spec, maps, w2, h2, s)
+                                        : fft_r2c_noalloc<float2>(real_in, spec, maps, w2, h2, s);
+}
+
 int emida_gb_run_hadamard(void *pics, const void *ref, uint32_t one_area, uint32_t ref_slices,
                           uint32_t batch, int precision)
 {

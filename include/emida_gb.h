@@ -232,6 +232,19 @@ int emida_gb_run_cross_corr(const void *pics, const void *ref, void *res, int pr
 /* forward R2C of [maps][h2][w2] real into [maps][h2][w2/2+1] complex (cuFFT layout). */
 int emida_gb_run_fft_r2c(const void *real_in, void *spec, uint32_t maps, uint32_t w2,
                          uint32_t h2, int precision);
+/* Allocation-free form of emida_gb_run_fft_r2c (no counterpart in the reference):
+ * same arguments, same results.  It is for callers that must not allocate device
+ * memory during a run, e.g. a pipeline whose other streams must not be stalled by
+ * the device-wide synchronisation cudaFree implies, or one whose memory pool has
+ * claimed the free HBM up front.  Its twiddle tables live in one fixed 32 KiB
+ * device array shared by every call, so w2 and h2 must each be 1..1024 (larger
+ * sizes return EMIDA_GB_INVALID_ARGUMENT), and calls that overlap in time on the
+ * same device (other host threads) race on that array.  The first call on each
+ * device looks the array's address up with that device current; make that first
+ * call before any stream capture begins.  Each call writes both tables before
+ * its kernels read them, so nothing in the array has to start at zero. */
+int emida_gb_run_fft_r2c_noalloc(const void *real_in, void *spec, uint32_t maps, uint32_t w2,
+                                 uint32_t h2, int precision);
 /* unnormalised C2R of [maps][h2][w2/2+1] (overwritten) into [maps][h2][w2] real. */
 int emida_gb_run_fft_c2r(void *spec, void *real_out, uint32_t maps, uint32_t w2, uint32_t h2,
                          int precision);
