@@ -59,9 +59,11 @@ def parse():
     ap.add_argument("--profile-case", type=int, default=0,
                     help="run only N patterns through the chosen form a few times (for ncu)")
     ap.add_argument("--no-plain", action="store_true", help="skip the plain-form comparison")
-    ap.add_argument("--config", default="detector", choices=["detector", "batching", "serving"],
+    ap.add_argument("--config", default="detector",
+                    choices=["detector", "batching", "serving", "precision"],
                     help="detector: 256 x 1024^2, 100 ROIs r=32 (default); batching: patterns on "
-                         "uneven layouts; serving: Poisson stream of scan rows")
+                         "uneven layouts; serving: Poisson stream of scan rows; precision: 2048 "
+                         "patterns, brute on the tensor cores beside the FP32 FFT")
     ap.add_argument("--rate", type=float, default=50.0, help="serving: rows per second")
     ap.add_argument("--duration", type=float, default=8.0, help="serving: seconds of arrivals")
     return ap.parse_args()
@@ -356,6 +358,89 @@ def run_serving(args):
     srv.close()
 
 
+def run_precision(args):
+    """2048 patterns of 1024^2, 100 ROIs r=32 (10 x 10 grid), fit size 7: the
+    brute policy's 127 x 127-lag correlation as a BF16 hi/lo contraction on the
+    tcgen05 tensor cores (FP64 sums, means and fit) beside the FP32 fused FFT,
+    both against the FP64 brute oracle (the reference's --precision double)."""
+    import ctypes
+    import __graft_entry__
+    __graft_entry__.build_library()
+    from emida_gb300 import DeviceBuffer, GpuOffset, _lib
+    from oracle import oracle as eo
+    P, s = 2048, 7
+    ref, uniq, begins = workload()
+    S = len(begins)
+    pairs = P * S
+    pat = 1024 * 1024 * 2
+    d_pics = DeviceBuffer(P * pat)
+    d_uniq = DeviceBuffer.from_array(uniq)
+    for k in range(P // UNIQUE):  # the 32 distinct patterns repeated, on the device
+        _lib.call("emida_gb_memcpy_d2d", ctypes.c_void_p(d_pics.ptr.value + k * UNIQUE * pat),
+                  d_uniq.ptr, UNIQUE * pat)
+    n_check = 2
+    o_offs, o_coefs, o_peaks = eo.get_offsets(ref, uniq[:n_check], begins, 64, 64, eo.POLICY_BRUTE, s)
+    ok = well_posed(o_coefs, s)
+    peak, peak_kind = (json.load(open(os.path.join(ROOT, "MEASURED_PEAKS.json"))).get("bf16_tflops"),
+                       "measured") if os.path.exists(os.path.join(ROOT, "MEASURED_PEAKS.json")) \
+        else (1900.0, "fallback")
+    forms = {}
+    for name, policy, mode in (("tensor", "brute", "tensor"), ("fft", "fft", "fused")):
+        g = GpuOffset((1024, 1024), begins, (64, 64), (127, 127), 32, policy, s, 1, "float",
+                      np.uint16, mode)
+        g.allocate_memory(ref)
+        d_offs, d_coefs = DeviceBuffer(pairs * 16), DeviceBuffer(pairs * 48)
+        d_maxes = DeviceBuffer(pairs * 8)
+        g.run_device(d_pics, P, d_offs, d_coefs, d_maxes)
+        _lib.call("emida_gb_synchronize")
+        offs = d_offs.download(np.float64, (pairs, 2))[:n_check * S]
+        idx = d_maxes.download(np.dtype([("data", "<f4"), ("index", "<u4")]), pairs)["index"][:n_check * S]
+        if mode == "fused":  # FFT map index -> lag-window index of the brute map
+            qx, qy = idx % 128, idx // 128
+            idx = ((qx + 63) % 128) + 127 * ((qy + 63) % 128)
+        d = np.abs(offs - o_offs)
+        for _ in range(args.warmup):
+            g.run_device(d_pics, P, d_offs)
+        _lib.call("emida_gb_synchronize")
+        with ClockSampler(0) as clk:
+            ms = g.time_device(d_pics, P, d_offs, args.steps) / args.steps
+        forms[name] = {
+            "value": pairs / (ms / 1000.0), "ms_per_step": ms, "form": g.mode,
+            "peak_match_rate": float(np.mean(idx == o_peaks)),
+            "max_abs_err_px": float(d[ok].max()), "rms_err_px": float(np.sqrt(np.mean(d[ok] ** 2))),
+            "clocks": clk.summary(), "launches_per_step": g.launches_per_run(),
+        }
+        g.close()
+    t = forms["tensor"]
+    useful = 2.0 * 64 ** 4            # sum over lags of the overlap products
+    issued = 3 * 2.0 * 128 * 128 * 4096  # three split products of the 128 x 128 x 4096 GEMM
+    sec = t["ms_per_step"] / 1000.0
+    line = {
+        "metric": "ROI pairs/s, brute 127x127 lags as a BF16 hi/lo tensor-core contraction",
+        "value": t["value"], "unit": "ROI pairs/s", "n_gpus": 1, "steps": args.steps,
+        "warmup": args.warmup, "ms_per_step": t["ms_per_step"], "higher_is_better": True,
+        "scaling": "weak", "vs_baseline": None, "dtype": "bf16x3->f32", "data": "synthetic",
+        "config": {"workload": "2048 x 1024^2 uint16 patterns, 100 ROIs r=32 (64x64), brute "
+                               "127x127 lags, s=7", "patterns": P, "rois": S, "fitsize": s,
+                   "l2": "inputs larger than L2 (4 GiB of patterns)"},
+        "parity": {"vs": f"FP64 brute oracle, first {n_check} patterns ({n_check * S} pairs)",
+                   "well_posed_fits": int(ok[:, 0].sum()), "tensor": {k: t[k] for k in (
+                       "peak_match_rate", "max_abs_err_px", "rms_err_px")},
+                   "fft_fp32": {k: forms["fft"][k] for k in ("peak_match_rate", "max_abs_err_px",
+                                                             "rms_err_px")}},
+        "roofline": {"bound": "tensor", "achieved": pairs * issued / sec / 1e12, "peak": peak,
+                     "unit": "TFLOP/s", "frac": pairs * issued / sec / 1e12 / peak,
+                     "peak_kind": peak_kind, "traffic": None,
+                     "note": "issued BF16 MMA flops (3 x 2 x 128 x 128 x 4096 per pair) vs the "
+                             "bf16 GEMM peak; useful flops are 2 x 64^4 per pair"},
+        "useful_tflops": pairs * useful / sec / 1e12,
+        "fft_fp32": {k: forms["fft"][k] for k in ("value", "ms_per_step", "form")},
+        "gpu_launches": t["launches_per_step"] * args.steps,
+        "clocks": t["clocks"],
+    }
+    print(json.dumps(line), flush=True)
+
+
 def main():
     args = parse()
     rank, world, local = dist_env()
@@ -365,6 +450,8 @@ def main():
         return run_batching(args)
     if args.config == "serving":
         return run_serving(args)
+    if args.config == "precision":
+        return run_precision(args)
 
     import __graft_entry__
     __graft_entry__.build_library()

@@ -15,7 +15,7 @@ OK = 0
 BRUTE, FFT = 0, 1
 DOUBLE, FLOAT = 0, 1
 IN_U16, IN_F64 = 0, 1
-MODE_AUTO, MODE_PLAIN, MODE_FUSED = 0, 1, 2
+MODE_AUTO, MODE_PLAIN, MODE_FUSED, MODE_TENSOR = 0, 1, 2, 3
 
 
 class EmidaError(RuntimeError):

@@ -11,7 +11,8 @@ import ctypes
 import numpy as np
 
 from . import _lib
-from ._lib import BRUTE, DOUBLE, FFT, FLOAT, IN_F64, IN_U16, MODE_AUTO, MODE_FUSED, MODE_PLAIN
+from ._lib import (BRUTE, DOUBLE, FFT, FLOAT, IN_F64, IN_U16, MODE_AUTO, MODE_FUSED, MODE_PLAIN,
+                   MODE_TENSOR)
 
 CROSS_POLICY_BRUTE, CROSS_POLICY_FFT = BRUTE, FFT
 
@@ -45,7 +46,7 @@ def _policy(p):
 
 
 def _mode(m):
-    return {"auto": MODE_AUTO, "plain": MODE_PLAIN, "fused": MODE_FUSED}.get(m, m)
+    return {"auto": MODE_AUTO, "plain": MODE_PLAIN, "fused": MODE_FUSED, "tensor": MODE_TENSOR}.get(m, m)
 
 
 class DeviceBuffer:
@@ -142,7 +143,8 @@ class GpuOffset:
 
     @property
     def mode(self):
-        return {MODE_PLAIN: "plain", MODE_FUSED: "fused"}[_lib.lib().emida_gb_resolved_mode(self._h)]
+        return {MODE_PLAIN: "plain", MODE_FUSED: "fused", MODE_TENSOR: "tensor"}[
+            _lib.lib().emida_gb_resolved_mode(self._h)]
 
     def allocate_memory(self, temp=None):
         """src/gpu_offset.hpp:127-211: buffers exist from construction; with a

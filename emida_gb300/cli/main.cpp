@@ -7,7 +7,7 @@
 //   -s,--slicesize X,Y (radius)   -c,--crosssize X,Y   --precision double|float
 //   -f,--fitsize 3|5|7|9   --crosspolicy brute|fft   --batchsize N   --loadworkers N
 //   -q,--writecoefs   -a,--analysis   -o,--outpics DIR (accepted, unused as in the
-//   reference)   --slicestep X,Y   --mode auto|plain|fused   -h,--help
+//   reference)   --slicestep X,Y   --mode auto|plain|fused|tensor   -h,--help
 // Output on stdout, per pattern: "%f %f %llu %s" (position, ROI count, file),
 // then per ROI "%lu %lu %f %f" (mid, offset) or with -q six more "%f" coefficients.
 #include <algorithm>
@@ -63,7 +63,8 @@ const char *usage =
     "  --crosspolicy brute|fft    (default fft)\n"
     "  --batchsize N              patterns per batch (default 1)\n"
     "  --loadworkers N            pattern loading threads (default 1)\n"
-    "  --mode auto|plain|fused    execution form (default auto)\n"
+    "  --mode auto|plain|fused|tensor  execution form (default auto; tensor: brute\n"
+    "                             policy on the tensor cores, float, 64x64 ROIs)\n"
     "  -h,--help\n";
 
 bool parse_pair(const std::string &v, size2_t &out)
@@ -236,7 +237,10 @@ bool parse(int argc, char **argv, params &a, bool &help)
     }
     if (v.count("mode")) {
         const std::string m = v["mode"];
-        a.mode = m == "plain" ? EMIDA_GB_MODE_PLAIN : m == "fused" ? EMIDA_GB_MODE_FUSED : EMIDA_GB_MODE_AUTO;
+        a.mode = m == "plain" ? EMIDA_GB_MODE_PLAIN
+                 : m == "fused" ? EMIDA_GB_MODE_FUSED
+                 : m == "tensor" ? EMIDA_GB_MODE_TENSOR
+                                 : EMIDA_GB_MODE_AUTO;
     }
     a.analysis = v.count("analysis") > 0;
     a.write_coefs = v.count("writecoefs") > 0;

@@ -282,10 +282,34 @@ int emida_gb::host::run_fused(emida_gb_handle *h, const void *pics, uint32_t pat
     return EMIDA_GB_OK;
 }
 
+int emida_gb::host::run_tensor(emida_gb_handle *h, const void *pics, uint32_t pats, void *maxes, void *neigh,
+               double *offsets, double *coefs, cudaStream_t st)
+{
+    brute_tc_args a{};
+    a.pics = static_cast<const uint16_t *>(pics);
+    a.src_w = h->src.x;
+    a.src_h = h->src.y;
+    a.begins = h->d_begins;
+    a.n_rois = h->S;
+    a.n_patterns = pats;
+    a.ref_prep = h->d_ref_prep64;
+    a.hann = h->d_hann64;
+    a.lstsq = h->d_lstsq;
+    a.fitsize = h->p.fitsize;
+    a.offsets = offsets ? offsets : h->d_offsets;
+    a.coefs = coefs;
+    a.maxes = maxes;
+    a.neigh = static_cast<float *>(neigh);
+    a.err = h->d_err;
+    CK(launch_brute_tc(a, 0, st));
+    return EMIDA_GB_OK;
+}
+
 int emida_gb::host::run_any(emida_gb_handle *h, const void *pics, uint32_t pats, void *maxes, void *neigh,
             double *offsets, double *coefs, cudaStream_t st)
 {
     if (h->mode == EMIDA_GB_MODE_FUSED) return run_fused(h, pics, pats, maxes, neigh, offsets, coefs, st);
+    if (h->mode == EMIDA_GB_MODE_TENSOR) return run_tensor(h, pics, pats, maxes, neigh, offsets, coefs, st);
     const size_t pat_bytes = (size_t)h->src.x * h->src.y * h->in_elem;
     const size_t s2 = (size_t)h->p.fitsize * h->p.fitsize;
     for (uint32_t done = 0; done < pats; done += h->B) {
@@ -306,8 +330,9 @@ int emida_gb::host::check_device_error(emida_gb_handle *h)
     CK(cudaMemcpy(&err, h->d_err, sizeof err, cudaMemcpyDeviceToHost));
     if (err) {
         CK(cudaMemset(h->d_err, 0, sizeof err));
-        return fail(EMIDA_GB_DEVICE_CHECK, "device check failed (flags 0x%x%s)", err,
-                    (err & DEV_ERR_TMA_TIMEOUT) ? ": TMA wait ran out" : "");
+        return fail(EMIDA_GB_DEVICE_CHECK, "device check failed (flags 0x%x%s%s)", err,
+                    (err & DEV_ERR_TMA_TIMEOUT) ? ": TMA wait ran out" : "",
+                    (err & DEV_ERR_WAIT_TIMEOUT) ? ": pipeline wait ran out" : "");
     }
     return EMIDA_GB_OK;
 }
@@ -341,6 +366,15 @@ int validate(const emida_gb_params *p)
     } else if (p->slice_w != p->slice_h) {
         return fail(EMIDA_GB_UNSUPPORTED, "the FFT policy needs square ROIs");
     }
+    if (p->mode < EMIDA_GB_MODE_AUTO || p->mode > EMIDA_GB_MODE_TENSOR)
+        return fail(EMIDA_GB_INVALID_ARGUMENT, "invalid mode %d", p->mode);
+    if (p->mode == EMIDA_GB_MODE_TENSOR &&
+        (p->policy != EMIDA_GB_BRUTE || p->precision != EMIDA_GB_FLOAT || p->in_type != EMIDA_GB_IN_U16 ||
+         p->slice_w != BRUTE_TC_SIDE || p->slice_h != BRUTE_TC_SIDE || p->cross_w != BRUTE_TC_CROSS ||
+         p->cross_h != BRUTE_TC_CROSS))
+        return fail(EMIDA_GB_UNSUPPORTED,
+                    "the tensor-core form takes the brute policy, float precision, uint16 input, "
+                    "64x64 ROIs and a 127x127 lag window");
     return EMIDA_GB_OK;
 }
 
@@ -412,6 +446,7 @@ int emida_gb_create(const emida_gb_params *p, emida_gb_handle **out)
                     "no fused kernel for this shape (FFT policy, ROI side <= 96 in FP32, <= 64 in FP64)");
     }
     h->mode = (p->mode == EMIDA_GB_MODE_PLAIN || !fusable) ? EMIDA_GB_MODE_PLAIN : EMIDA_GB_MODE_FUSED;
+    if (p->mode == EMIDA_GB_MODE_TENSOR) h->mode = EMIDA_GB_MODE_TENSOR;
     if (h->mode == EMIDA_GB_MODE_FUSED) {
         // the resident reference spectra are computed at the fused length
         h->w2 = h->h2 = fn;
@@ -467,6 +502,12 @@ int emida_gb_create(const emida_gb_params *p, emida_gb_handle **out)
     if (h->mode == EMIDA_GB_MODE_FUSED) {
         TRY(upload_hann(h, &h->d_hann_fused, h->slice.x, h->slice.y));
         TRY(h->alloc(&h->d_ref_spec_cm, (size_t)h->h2 * h->half * h->S * h->c_elem));
+    } else if (h->mode == EMIDA_GB_MODE_TENSOR) {
+        // FP64 windows and reference ROIs; no per-batch scratch
+        h->dbl = true;
+        TRY(upload_hann(h, (void **)&h->d_hann64, h->slice.x, h->slice.y));
+        h->dbl = false;
+        TRY(h->alloc((void **)&h->d_ref_prep64, (size_t)ps.x * ps.y * h->S * sizeof(double), true));
     } else {
         TRY(h->alloc(&h->d_sums, sum_elem * h->N));
         TRY(h->alloc(&h->d_prep, (size_t)ps.x * ps.y * h->N * h->t_elem, true));
@@ -492,6 +533,9 @@ int emida_gb_set_reference(emida_gb_handle *h, const void *ref)
     CK(run_sums(h->d_ref_in, in_type, h->src, h->d_begins, h->S, h->slice, 1, h->d_sums_ref, h->comp));
     CK(run_prepare(h->d_ref_in, in_type, h->dbl, h->d_ref_prep, h->d_hann, h->d_sums_ref,
                    h->d_begins, h->src, h->slice, h->prep_size(), h->S, 1, h->comp));
+    if (h->mode == EMIDA_GB_MODE_TENSOR)
+        CK(run_prepare(h->d_ref_in, in_type, true, h->d_ref_prep64, h->d_hann64, h->d_sums_ref,
+                       h->d_begins, h->src, h->slice, h->prep_size(), h->S, 1, h->comp));
     if (h->fft) {
         CK(run_fft_r2c(h->d_ref_prep, h->d_ref_spec, h->S, tables(h), h->dbl, h->comp));
         if (h->d_ref_spec_cm)
@@ -710,7 +754,7 @@ void *emida_gb_stream(emida_gb_handle *h) { return h ? (void *)h->comp : nullptr
 int emida_gb_launches_per_run(const emida_gb_handle *h)
 {
     if (!h) return -1;
-    if (h->mode == EMIDA_GB_MODE_FUSED) return 1;
+    if (h->mode == EMIDA_GB_MODE_FUSED || h->mode == EMIDA_GB_MODE_TENSOR) return 1;
     return h->fft ? 10 : 6;
 }
 

@@ -42,6 +42,7 @@ enum status_t : int32_t {
 enum dev_err_t : uint32_t {
     DEV_ERR_TMA_TIMEOUT = 1u,
     DEV_ERR_BAD_INDEX = 2u,
+    DEV_ERR_WAIT_TIMEOUT = 4u,  // a pipeline wait (mbarrier) ran out
 };
 
 }  // namespace emida_gb

@@ -12,6 +12,7 @@
 
 #include "../../include/emida_gb.h"
 #include "common.cuh"
+#include "brute_tc.cuh"
 #include "fused.cuh"
 #include "staged.cuh"
 
@@ -39,6 +40,8 @@ int run_plain_chunk(emida_gb_handle *h, const void *pics, uint32_t pats, void *m
                     double *offsets, double *coefs, cudaStream_t st);
 int run_fused(emida_gb_handle *h, const void *pics, uint32_t pats, void *maxes, void *neigh,
               double *offsets, double *coefs, cudaStream_t st);
+int run_tensor(emida_gb_handle *h, const void *pics, uint32_t pats, void *maxes, void *neigh,
+               double *offsets, double *coefs, cudaStream_t st);
 // Either form, any number of patterns.
 int run_any(emida_gb_handle *h, const void *pics, uint32_t pats, void *maxes, void *neigh,
             double *offsets, double *coefs, cudaStream_t st);
@@ -85,6 +88,7 @@ struct emida_gb_handle {
     void *d_ref_in = nullptr;
     uint2 *d_begins = nullptr;
     void *d_hann = nullptr, *d_hann_fused = nullptr;
+    double *d_hann64 = nullptr, *d_ref_prep64 = nullptr;  // tensor mode: FP64 reference ROIs
     void *d_sums_ref = nullptr, *d_sums = nullptr;
     void *d_ref_prep = nullptr, *d_prep = nullptr;
     void *d_ref_spec = nullptr, *d_ref_spec_cm = nullptr, *d_spec = nullptr;

@@ -39,8 +39,18 @@ enum { EMIDA_GB_BRUTE = 0, EMIDA_GB_FFT = 1 };
 enum { EMIDA_GB_DOUBLE = 0, EMIDA_GB_FLOAT = 1 };
 /* the IN template parameter of gpu_offset<T, IN> */
 enum { EMIDA_GB_IN_U16 = 0, EMIDA_GB_IN_F64 = 1 };
-/* execution form: AUTO picks FUSED where a fused kernel covers the shape */
-enum { EMIDA_GB_MODE_AUTO = 0, EMIDA_GB_MODE_PLAIN = 1, EMIDA_GB_MODE_FUSED = 2 };
+/* execution form: AUTO picks FUSED where a fused kernel covers the shape.
+ * TENSOR (requested explicitly, never chosen by AUTO): the brute policy on the
+ * tcgen05 tensor cores with BF16 hi/lo split operands and FP32 accumulation,
+ * fused with maxarg, neighbours and the FP64 fit; FLOAT precision, uint16
+ * input, 64 x 64 ROIs and the full 127 x 127 lag window only.  Its offsets
+ * agree with the FP64 path to about 1e-2 px instead of the FP32 paths' 1e-3. */
+enum {
+    EMIDA_GB_MODE_AUTO = 0,
+    EMIDA_GB_MODE_PLAIN = 1,
+    EMIDA_GB_MODE_FUSED = 2,
+    EMIDA_GB_MODE_TENSOR = 3
+};
 
 typedef struct emida_gb_handle emida_gb_handle;
 
@@ -114,7 +124,7 @@ int emida_gb_run_device(emida_gb_handle *h, const void *dev_patterns, uint32_t p
                         double *dev_offsets, double *dev_coefs, void *dev_maxes,
                         void *dev_neigh, void *stream);
 
-/* Which form the handle runs: EMIDA_GB_MODE_PLAIN or EMIDA_GB_MODE_FUSED. */
+/* Which form the handle runs: EMIDA_GB_MODE_PLAIN, _FUSED or _TENSOR. */
 int emida_gb_resolved_mode(const emida_gb_handle *h);
 /* The handle's compute stream (a cudaStream_t). */
 void *emida_gb_stream(emida_gb_handle *h);

@@ -101,3 +101,20 @@ def test_fused_form_availability(lib):
     with pytest.raises(EmidaError, match="no fused kernel"):
         GpuOffset((256, 256), [(0, 0)], (100, 100), (199, 199), 1, "fft", 3, 1, "float",
                   mode="fused")
+
+
+@pytest.mark.parametrize("kw", [
+    dict(policy="fft"),
+    dict(precision="double"),
+    dict(slice_size=(32, 32), cross_size=(63, 63)),
+    dict(cross_size=(101, 101)),
+    dict(in_dtype=np.float64),
+])
+def test_tensor_form_shape_limits(lib, kw):
+    # the tensor-core form takes brute / float / uint16 / 64x64 ROIs / 127x127 lags
+    from emida_gb300 import EmidaError, GpuOffset
+    args = dict(src_size=(256, 256), begins=[(0, 0)], slice_size=(64, 64), cross_size=(127, 127),
+                batch_size=1, policy="brute", s=3, precision="float", mode="tensor")
+    args.update(kw)
+    with pytest.raises(EmidaError, match="tensor-core form"):
+        GpuOffset(**args)
