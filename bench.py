@@ -378,6 +378,28 @@ def run_precision(args):
     for k in range(P // UNIQUE):  # the 32 distinct patterns repeated, on the device
         _lib.call("emida_gb_memcpy_d2d", ctypes.c_void_p(d_pics.ptr.value + k * UNIQUE * pat),
                   d_uniq.ptr, UNIQUE * pat)
+    if args.profile_case:  # a few launches of the tensor form only (for ncu)
+        g = GpuOffset((1024, 1024), begins, (64, 64), (127, 127), 32, "brute", s, 1, "float",
+                      np.uint16, "tensor")
+        g.allocate_memory(ref)
+        d_offs = DeviceBuffer(args.profile_case * S * 16)
+        for _ in range(3):
+            g.run_device(d_pics, args.profile_case, d_offs)
+        _lib.call("emida_gb_synchronize")
+        print(json.dumps({"profile_case_patterns": args.profile_case, "mode": g.mode}))
+        g.close()
+        return
+    # the staged FP32 brute form (CUDA cores, the reference's kernels) on a slice
+    n_plain = 32
+    gp = GpuOffset((1024, 1024), begins, (64, 64), (127, 127), 32, "brute", s, 1, "float",
+                   np.uint16, "plain")
+    gp.allocate_memory(ref)
+    d_po = DeviceBuffer(n_plain * S * 16)
+    gp.run_device(d_pics, n_plain, d_po)
+    plain_ms = gp.time_device(d_pics, n_plain, d_po, 2) / 2
+    plain = {"value": n_plain * S / (plain_ms / 1000.0), "ms_per_step": plain_ms * P / n_plain,
+             "sample": f"{n_plain} patterns, scaled to {P}"}
+    gp.close()
     n_check = 2
     o_offs, o_coefs, o_peaks = eo.get_offsets(ref, uniq[:n_check], begins, 64, 64, eo.POLICY_BRUTE, s)
     ok = well_posed(o_coefs, s)
@@ -435,6 +457,7 @@ def run_precision(args):
                              "bf16 GEMM peak; useful flops are 2 x 64^4 per pair"},
         "useful_tflops": pairs * useful / sec / 1e12,
         "fft_fp32": {k: forms["fft"][k] for k in ("value", "ms_per_step", "form")},
+        "plain_brute_fp32": plain,
         "gpu_launches": t["launches_per_step"] * args.steps,
         "clocks": t["clocks"],
     }
