@@ -11,8 +11,11 @@ L2 flush is needed between steps).
 
 value: device-resident throughput of the chosen form (inputs in HBM when the
 timed region starts), CUDA events on the launching stream.
-e2e: the same job through the public C ABI from pinned host memory: per batch
-the host->device copy, the path, and the device->host read of the offsets.
+e2e: the same job through the public C ABI (submit/wait) from pinned host
+memory, three batches in flight: per batch the host->device copy (overlapping
+the previous batch's path; only the row bands that hold ROI pixels are
+copied), the path, and the offsets, coefficients and maxima back to the host.  e2e_zero_copy: the same with the kernels reading each
+batch's ROI pixels in place from host memory instead of a copy.
 
 --impl reference times the reference algorithm on the host cores instead (the
 CPU FP64 oracle port of the same path; the reference's own CPU code is built
@@ -66,6 +69,11 @@ def parse():
                          "patterns, brute on the tensor cores beside the FP32 FFT")
     ap.add_argument("--rate", type=float, default=50.0, help="serving: rows per second")
     ap.add_argument("--duration", type=float, default=8.0, help="serving: seconds of arrivals")
+    ap.add_argument("--layout", default="mixed", choices=["mixed", "detector"],
+                    help="serving: mixed sizes and layouts, or the detector grid at 1024^2")
+    ap.add_argument("--step-patterns", type=int, default=128, help="serving: patterns per step")
+    ap.add_argument("--copy-rows", action="store_true",
+                    help="serving: copy every row into the device arena (no in-place reads)")
     return ap.parse_args()
 
 
@@ -202,6 +210,14 @@ def run_reference(args, rank, world):
     print(json.dumps(line), flush=True)
 
 
+def roi_rows(begins, side):
+    """Pattern rows that hold ROI pixels (the rows a batch copy moves)."""
+    rows = np.zeros(1 + max(int(y) for _, y in begins) + side, dtype=bool)
+    for _, y in begins:
+        rows[int(y):int(y) + side] = True
+    return int(rows.sum())
+
+
 def pinned_u16(shape):
     """A uint16 array in pinned host memory (freed with the process)."""
     import ctypes
@@ -295,29 +311,38 @@ def run_batching(args):
 
 
 def run_serving(args):
-    """A Poisson stream of scan rows (32-512 patterns, 512^2 or 1024^2, each on
-    its own layout: 25-225 ROIs of radius 24-48, fit 3-9) through the request
-    loop; p50/p99 row latency and sustained ROI pairs/s."""
+    """A Poisson stream of scan rows of 32-512 patterns through the request
+    loop; p50/p99 row latency and sustained ROI pairs/s.  --layout mixed:
+    512^2 or 1024^2 rows (50/50), each on one of 8 seeded layouts per size
+    (25-225 ROIs of radius 24-48, fit 3-9).  --layout detector: 1024^2 rows on
+    the 10 x 10 grid of 64 x 64 ROIs, fit 5."""
     import time
     import __graft_entry__
     __graft_entry__.build_library()
     from emida_gb300 import Server, synth
     from oracle import oracle as eo
     rng = np.random.default_rng(99)
-    srv = Server(args.precision, hbm_bytes=24 << 30, step_patterns=128)
+    detector = args.layout == "detector"
+    sizes = (1024,) if detector else (512, 1024)
+    srv = Server(args.precision, hbm_bytes=24 << 30, step_patterns=args.step_patterns,
+                 zero_copy=not args.copy_rows)
     rows_src, layouts = {}, {}
-    for size in (512, 1024):
+    for size in sizes:
         ref = synth.reference_pattern(size, 90 + size)
         uniq, _ = synth.deformed_patterns(size, 90 + size, 16, sigma_eps=5e-3)
         buf = pinned_u16((512, size, size))
         for i in range(512):
             buf[i] = uniq[i % 16]
         rows_src[size] = (ref, buf)
-        lay = random_layouts(size, 8, size, (24, 48), (25, 225))
+        if detector:
+            _, grid = synth.roi_grid(size, 10, 32, margin=40)
+            lay = [(grid, 64, 5)] * 8
+        else:
+            lay = random_layouts(size, 8, size, (24, 48), (25, 225))
         layouts[size] = [(srv.add_layout((size, size), b, side, fs, ref), b, side, fs) for b, side, fs in lay]
     # parity of one row per size against the FP64 oracle (not timed)
     errs = []
-    for size in (512, 1024):
+    for size in sizes:
         lid, begins, side, fs = layouts[size][0]
         ref, buf = rows_src[size]
         offs, coefs, _ = srv.wait(srv.submit(lid, buf[:2]))
@@ -331,7 +356,7 @@ def run_serving(args):
     with ClockSampler(0) as clk:
         t = time.perf_counter()
         while t < t_end:
-            size = 512 if rng.random() < 0.5 else 1024
+            size = 1024 if detector or rng.random() >= 0.5 else 512
             lid, begins, side, fs = layouts[size][int(rng.integers(0, 8))]
             n = int(rng.integers(32, 513))
             pending.append(srv.submit(lid, rows_src[size][1][:n]))
@@ -349,10 +374,14 @@ def run_serving(args):
         "latency_ms": {"p50": st["p50_ms"], "p99": st["p99_ms"]}, "rows": st["completed"],
         "pairs": sent_pairs, "higher_is_better": True,
         "dtype": "f32" if args.precision == "float" else "f64", "data": "synthetic",
-        "config": {"workload": "Poisson rows: 32-512 patterns of 512^2 or 1024^2 (50/50), 8 layouts "
-                               "per size, 25-225 ROIs radius 24-48, fit 3-9",
+        "config": {"workload": ("Poisson rows: 32-512 patterns of 1024^2, 100 ROIs of 64x64 (10x10 "
+                                "grid), fit 5" if detector else
+                                "Poisson rows: 32-512 patterns of 512^2 or 1024^2 (50/50), 8 layouts "
+                                "per size, 25-225 ROIs radius 24-48, fit 3-9"),
                    "rate_rows_per_s": args.rate, "duration_s": args.duration,
-                   "hbm_arena_bytes_per_size": 24 << 30, "step_patterns": 128},
+                   "hbm_arena_bytes_per_size": 24 << 30, "step_patterns": args.step_patterns,
+                   "rows": "copied into the device arena" if args.copy_rows else
+                           "pinned rows read in place where ROIs cover <= half the pattern"},
         "parity": {"max_abs_err_px": max(errs), "vs": "FP64 oracle, one row per size"},
         "clocks": clk.summary()}), flush=True)
     srv.close()
@@ -589,6 +618,23 @@ def main():
     barrier()
     e2e_ms = max_over_ranks((time.perf_counter() - t0) * 1000 / e2e_steps, dist, device="cuda")
     e2e_value = whole_job_rate(pairs_per_step, e2e_ms / 1000.0, world)
+    # the other ingest modes: kernels reading the ROI pixels in place (no
+    # copy), and every other batch each way
+    ingest = {}
+    for mode in ("in_place", "split"):
+        g.ingest = mode
+        if g.ingest != mode:
+            continue
+        e2e_step()
+        assert np.array_equal(host_offs, offs), f"{mode} offsets differ from the device-resident run"
+        barrier()
+        t0 = time.perf_counter()
+        for _ in range(e2e_steps):
+            e2e_step()
+        barrier()
+        m_ms = max_over_ranks((time.perf_counter() - t0) * 1000 / e2e_steps, dist, device="cuda")
+        ingest[mode] = {"value": whole_job_rate(pairs_per_step, m_ms / 1000.0, world), "ms_per_step": m_ms}
+    g.ingest = "copy"
     _lib.call("emida_gb_free_host", hbuf)
 
     cpu = None
@@ -623,8 +669,12 @@ def main():
             "plain": plain,
             "cpu_baseline": cpu,
             "e2e": {"value": e2e_value, "unit": "ROI pairs/s",
-                    "h2d_bytes_per_step": int(pics.nbytes), "d2h_bytes_per_step": pairs_per_step * 16,
-                    "ms_per_step": e2e_ms},
+                    "h2d_bytes_per_step": int(P * roi_rows(begins, 64) * 1024 * 2),
+                    "d2h_bytes_per_step": pairs_per_step * (16 + 48 + 8),
+                    "ms_per_step": e2e_ms,
+                    "input": f"pinned host batches; the {roi_rows(begins, 64)} of 1024 rows that hold "
+                             "ROI pixels are copied (one pitched copy per row band)"},
+            "e2e_ingest": ingest,
             "gpu_launches": launches * args.steps,
             "clocks": clk.summary(),
         }

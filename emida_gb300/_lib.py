@@ -65,6 +65,7 @@ SIGNATURES = {
     "emida_gb_multi_count": [_VP, _U32, _U32P, ctypes.POINTER(ctypes.c_uint64)],
     "emida_gb_multi_run": [_VP, _VP, _U32, _U32P, _VP, _VP, _VP, _I32],
     "emida_gb_multi_run_slots": [_VP, _VP, _U32, _U32, _U32P, _U32P, _VP, _VP, _VP],
+    "emida_gb_multi_run_table": [_VP, ctypes.POINTER(_VP), _U32, _U32P, _VP, _VP, _VP],
     "emida_gb_multi_stream": [_VP],
     "emida_gb_multi_synchronize": [_VP],
     "emida_gb_multi_autotune": [_VP, _VP, _U32, _U32P, _VP, ctypes.c_char_p, _SZ],
@@ -72,11 +73,14 @@ SIGNATURES = {
     "emida_gb_server_create": [_I32, ctypes.c_uint64, _U32, ctypes.POINTER(_VP)],
     "emida_gb_server_add_layout": [_VP, _U32, _U32, _U32P, _U32, _U32, _I32, _VP, _U32P],
     "emida_gb_server_submit": [_VP, _U32, _VP, _U32, ctypes.POINTER(ctypes.c_uint64)],
+    "emida_gb_server_set_zero_copy": [_VP, _I32],
     "emida_gb_server_wait": [_VP, ctypes.c_uint64, _DP, _DP, _DP],
     "emida_gb_server_stats": [_VP, _DP, _DP, _DP, ctypes.POINTER(ctypes.c_uint64)],
     "emida_gb_server_reset_stats": [_VP],
     "emida_gb_server_destroy": [_VP],
     "emida_gb_resolved_mode": [_VP],
+    "emida_gb_ingest": [_VP],
+    "emida_gb_set_ingest": [_VP, _I32],
     "emida_gb_stream": [_VP],
     "emida_gb_launches_per_run": [_VP],
     "emida_gb_destroy": [_VP],

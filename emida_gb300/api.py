@@ -49,6 +49,34 @@ def _mode(m):
     return {"auto": MODE_AUTO, "plain": MODE_PLAIN, "fused": MODE_FUSED, "tensor": MODE_TENSOR}.get(m, m)
 
 
+class _PinnedBlock:
+    """Pinned host memory from emida_gb_malloc_host, freed with its last user."""
+
+    def __init__(self, nbytes):
+        self.ptr = ctypes.c_void_p()
+        _lib.call("emida_gb_malloc_host", ctypes.byref(self.ptr), max(1, int(nbytes)))
+
+    def __del__(self):
+        try:
+            if self.ptr.value:
+                _lib.lib().emida_gb_free_host(self.ptr)
+                self.ptr = ctypes.c_void_p()
+        except Exception:
+            pass
+
+
+def pinned_array(shape, dtype=np.uint16):
+    """A numpy array in pinned (page-locked) host memory.  Pinned batches let
+    copies overlap compute, and where a form reads its input in place (see
+    GpuOffset.zero_copy) only the ROI pixels cross the host link."""
+    dtype = np.dtype(dtype)
+    nbytes = int(np.prod(shape)) * dtype.itemsize
+    block = _PinnedBlock(nbytes)
+    buf = (ctypes.c_char * max(1, nbytes)).from_address(block.ptr.value)
+    buf._block = block  # the memory lives as long as any view of it
+    return np.frombuffer(buf, dtype=dtype, count=int(np.prod(shape))).reshape(shape)
+
+
 class DeviceBuffer:
     """A device allocation made through the C ABI (emida_gb_malloc)."""
 
@@ -233,6 +261,21 @@ class GpuOffset:
     def stream(self):
         return _lib.lib().emida_gb_stream(self._h)
 
+    INGEST = ("copy", "in_place", "split")
+
+    @property
+    def ingest(self):
+        """How submit() brings pinned host batches to the kernels: "copy",
+        "in_place" (kernels read the ROI pixels over the host link, no copy) or
+        "split" (alternate batches, copy engine and host reads in parallel)."""
+        return self.INGEST[_lib.lib().emida_gb_ingest(self._h)]
+
+    @ingest.setter
+    def ingest(self, mode):
+        """In-place modes are honoured only when the ROIs cover at most half
+        of each pattern (a fused or tensor form); otherwise "copy" stays."""
+        _lib.call("emida_gb_set_ingest", self._h, self.INGEST.index(mode))
+
     def launches_per_run(self):
         return _lib.lib().emida_gb_launches_per_run(self._h)
 
@@ -332,6 +375,21 @@ class MultiLayout:
                   self._lo.ctypes.data_as(ctypes.POINTER(ctypes.c_uint32)), vp(dev_offsets),
                   vp(dev_coefs), vp(dev_maxes), int(bool(graph)))
 
+    def run_table(self, patterns, layout_of, dev_offsets, dev_coefs=None, dev_maxes=None):
+        """One run over patterns given by address (device memory or pinned host
+        memory read in place); `patterns` holds ints, DeviceBuffers or pinned
+        arrays, which must stay alive until synchronize()."""
+        self._lo = np.ascontiguousarray(layout_of, dtype=np.uint32)
+        addr = [p.ptr.value if isinstance(p, DeviceBuffer) else
+                (p.ctypes.data if isinstance(p, np.ndarray) else int(p)) for p in patterns]
+        self._table = (ctypes.c_void_p * len(addr))(*addr)
+
+        def vp(b):
+            return None if b is None else b.ptr
+        _lib.call("emida_gb_multi_run_table", self._h, self._table, len(addr),
+                  self._lo.ctypes.data_as(ctypes.POINTER(ctypes.c_uint32)), vp(dev_offsets),
+                  vp(dev_coefs), vp(dev_maxes))
+
     def synchronize(self):
         _lib.call("emida_gb_multi_synchronize", self._h)
 
@@ -362,7 +420,7 @@ class Server:
     per size) and computed in shared steps of up to `step_patterns` patterns.
     """
 
-    def __init__(self, precision="float", hbm_bytes=8 << 30, step_patterns=64):
+    def __init__(self, precision="float", hbm_bytes=8 << 30, step_patterns=64, zero_copy=True):
         self.precision = _precision(precision)
         h = ctypes.c_void_p()
         _lib.call("emida_gb_server_create", self.precision, int(hbm_bytes), int(step_patterns),
@@ -370,6 +428,7 @@ class Server:
         self._h = h
         self.rois = []
         self._rows = {}
+        _lib.call("emida_gb_server_set_zero_copy", h, int(bool(zero_copy)))
 
     def add_layout(self, src_size, begins, side, fitsize, ref):
         begins = np.ascontiguousarray(np.asarray(begins, dtype=np.uint32).reshape(-1, 2))

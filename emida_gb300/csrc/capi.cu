@@ -4,6 +4,7 @@
 // and the per-stage launch exports.
 #include <cuda.h>
 
+#include <algorithm>
 #include <atomic>
 #include <cmath>
 #include <cstdarg>
@@ -263,8 +264,10 @@ int emida_gb::host::run_fused(emida_gb_handle *h, const void *pics, uint32_t pat
     a.err = h->d_err;
     CUtensorMap map;
     std::memset(&map, 0, sizeof map);
-    a.use_tma = 0;
-    if (!h->in_f64 && (h->src.x % 8) == 0 && ((uintptr_t)pics % 16) == 0) {
+    a.stage = STAGE_PLAIN;
+    bool on_device = true;
+    CKS(pattern_location(pics, on_device));
+    if (on_device && !h->in_f64 && (h->src.x % 8) == 0 && ((uintptr_t)pics % 16) == 0) {
         if (encode_fn enc = get_encoder()) {
             const cuuint64_t dims[3] = {h->src.x, h->src.y, pats};
             const cuuint64_t strides[2] = {(cuuint64_t)h->src.x * 2,
@@ -275,7 +278,7 @@ int emida_gb::host::run_fused(emida_gb_handle *h, const void *pics, uint32_t pat
                     strides, box, estr, CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_NONE,
                     CU_TENSOR_MAP_L2_PROMOTION_L2_128B,
                     CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE) == CUDA_SUCCESS)
-                a.use_tma = 1;
+                a.stage = STAGE_TMA;
         }
     }
     CK(launch_fused(h->w2, h->dbl, h->in_f64, a, &map, 0, st));
@@ -323,6 +326,62 @@ int emida_gb::host::run_any(emida_gb_handle *h, const void *pics, uint32_t pats,
     }
     return EMIDA_GB_OK;
 }
+
+int emida_gb::host::pattern_location(const void *patterns, bool &on_device)
+{
+    cudaPointerAttributes pa{};
+    CK(cudaPointerGetAttributes(&pa, patterns));
+    if (pa.type == cudaMemoryTypeDevice || pa.type == cudaMemoryTypeManaged) {
+        on_device = true;
+        return EMIDA_GB_OK;
+    }
+    if (pa.type == cudaMemoryTypeHost) {
+        on_device = false;
+        return EMIDA_GB_OK;
+    }
+    return fail(EMIDA_GB_INVALID_ARGUMENT, "patterns must be in device memory or pinned host memory");
+}
+
+int emida_gb::host::copy_patterns(emida_gb_handle *h, void *dst, const void *src, uint32_t patterns,
+                                  cudaStream_t st)
+{
+    const size_t row = (size_t)h->src.x * h->in_elem, pat = row * h->src.y;
+    if (h->bands.size() == 1 && h->bands[0].first == 0 && h->bands[0].second == h->src.y) {
+        CK(cudaMemcpyAsync(dst, src, pat * patterns, cudaMemcpyHostToDevice, st));
+        return EMIDA_GB_OK;
+    }
+    for (const auto &b : h->bands)
+        CK(cudaMemcpy2DAsync((char *)dst + b.first * row, pat, (const char *)src + b.first * row, pat,
+                             b.second * row, patterns, cudaMemcpyHostToDevice, st));
+    return EMIDA_GB_OK;
+}
+
+namespace {
+
+// Merged row bands of the ROIs; one full band when they cover 90 % of the rows.
+void row_bands(emida_gb_handle *h)
+{
+    std::vector<std::pair<uint32_t, uint32_t>> iv;  // [start, end)
+    for (uint32_t r = 0; r < h->S; ++r) iv.push_back({h->begins[2 * r + 1], h->begins[2 * r + 1] + h->slice.y});
+    std::sort(iv.begin(), iv.end());
+    std::vector<std::pair<uint32_t, uint32_t>> merged;
+    for (const auto &v : iv) {
+        if (!merged.empty() && v.first <= merged.back().second)
+            merged.back().second = std::max(merged.back().second, v.second);
+        else
+            merged.push_back(v);
+    }
+    uint64_t covered = 0;
+    for (const auto &m : merged) covered += m.second - m.first;
+    h->bands.clear();
+    if (covered * 10 >= (uint64_t)h->src.y * 9) {
+        h->bands.push_back({0, h->src.y});
+        return;
+    }
+    for (const auto &m : merged) h->bands.push_back({m.first, m.second - m.first});
+}
+
+}  // namespace
 
 int emida_gb::host::check_device_error(emida_gb_handle *h)
 {
@@ -447,6 +506,9 @@ int emida_gb_create(const emida_gb_params *p, emida_gb_handle **out)
     }
     h->mode = (p->mode == EMIDA_GB_MODE_PLAIN || !fusable) ? EMIDA_GB_MODE_PLAIN : EMIDA_GB_MODE_FUSED;
     if (p->mode == EMIDA_GB_MODE_TENSOR) h->mode = EMIDA_GB_MODE_TENSOR;
+    row_bands(h);
+    h->in_place_allowed = h->mode != EMIDA_GB_MODE_PLAIN &&
+                          2 * (uint64_t)p->n_rois * p->slice_w * p->slice_h <= (uint64_t)p->src_w * p->src_h;
     if (h->mode == EMIDA_GB_MODE_FUSED) {
         // the resident reference spectra are computed at the fused length
         h->w2 = h->h2 = fn;
@@ -551,8 +613,7 @@ int emida_gb_transfer_async(emida_gb_handle *h, const void *batch, uint32_t *buf
 {
     if (!h || !batch) return fail(EMIDA_GB_INVALID_ARGUMENT, "null argument");
     const uint32_t i = h->in_next.fetch_add(1) % (uint32_t)h->d_in.size();
-    const size_t bytes = (size_t)h->src.x * h->src.y * h->in_elem * h->B;
-    CK(cudaMemcpyAsync(h->d_in[i], batch, bytes, cudaMemcpyHostToDevice, h->in_stream));
+    CKS(copy_patterns(h, h->d_in[i], batch, h->B, h->in_stream));
     CK(cudaEventRecord(h->in_done[i], h->in_stream));
     if (buffer_index) *buffer_index = i;
     return EMIDA_GB_OK;
@@ -619,8 +680,7 @@ int emida_gb_get_offset(emida_gb_handle *h, const void *batch, double *offsets, 
     if (!h || !batch || !offsets) return fail(EMIDA_GB_INVALID_ARGUMENT, "null argument");
     if (!h->ref_set) return fail(EMIDA_GB_INVALID_ARGUMENT, "reference pattern not set");
     std::lock_guard<std::mutex> lk(h->mu);
-    const size_t bytes = (size_t)h->src.x * h->src.y * h->in_elem * h->B;
-    CK(cudaMemcpyAsync(h->d_in[0], batch, bytes, cudaMemcpyHostToDevice, h->comp));
+    CKS(copy_patterns(h, h->d_in[0], batch, h->B, h->comp));
     CKS(run_any(h, h->d_in[0], h->B, h->d_maxes, h->d_neigh, h->d_offsets, h->d_coefs, h->comp));
     CK(cudaMemcpyAsync(offsets, h->d_offsets, 2 * sizeof(double) * h->N, cudaMemcpyDeviceToHost, h->comp));
     if (coefs)
@@ -673,12 +733,24 @@ int emida_gb_submit(emida_gb_handle *h, const void *batch, uint32_t patterns, ui
         return fail(EMIDA_GB_INVALID_ARGUMENT, "all %zu slots in flight: wait for ticket %llu first",
                     h->ring.size(), (unsigned long long)r.ticket);
     const size_t bytes = (size_t)h->src.x * h->src.y * h->in_elem * patterns;
-    // the input buffer is free once the slot's previous computation ran
-    CK(cudaStreamWaitEvent(h->in_stream, r.comp, 0));
-    CK(cudaMemcpyAsync(h->d_in[si], batch, bytes, cudaMemcpyHostToDevice, h->in_stream));
-    CK(cudaEventRecord(r.h2d, h->in_stream));
-    CK(cudaStreamWaitEvent(h->comp, r.h2d, 0));
-    CKS(run_any(h, h->d_in[si], patterns, r.d_maxes, h->d_neigh, r.d_offsets, r.d_coefs, h->comp));
+    cudaPointerAttributes pa{};
+    CK(cudaPointerGetAttributes(&pa, batch));
+    // device batches are used in place; pinned host batches are copied or read
+    // in place as the ingest mode says (SPLIT: every other batch each way, so
+    // the copy engine and the kernels' host reads share the load)
+    const bool in_place_host = pa.type == cudaMemoryTypeHost &&
+                               (h->ingest == EMIDA_GB_INGEST_IN_PLACE ||
+                                (h->ingest == EMIDA_GB_INGEST_SPLIT && (t & 1)));
+    const void *src = batch;
+    if (!(pa.type == cudaMemoryTypeDevice || pa.type == cudaMemoryTypeManaged || in_place_host)) {
+        // the input buffer is free once the slot's previous computation ran
+        CK(cudaStreamWaitEvent(h->in_stream, r.comp, 0));
+        CKS(copy_patterns(h, h->d_in[si], batch, patterns, h->in_stream));
+        CK(cudaEventRecord(r.h2d, h->in_stream));
+        CK(cudaStreamWaitEvent(h->comp, r.h2d, 0));
+        src = h->d_in[si];
+    }
+    CKS(run_any(h, src, patterns, r.d_maxes, h->d_neigh, r.d_offsets, r.d_coefs, h->comp));
     CK(cudaEventRecord(r.comp, h->comp));
     CK(cudaStreamWaitEvent(h->out_stream, r.comp, 0));
     const size_t n = (size_t)patterns * h->S;
@@ -726,6 +798,8 @@ int emida_gb_run_device(emida_gb_handle *h, const void *dev_patterns, uint32_t p
 {
     if (!h || !dev_patterns || !dev_offsets) return fail(EMIDA_GB_INVALID_ARGUMENT, "null argument");
     if (!h->ref_set) return fail(EMIDA_GB_INVALID_ARGUMENT, "reference pattern not set");
+    bool on_device = true;
+    CKS(pattern_location(dev_patterns, on_device));  // device or pinned host memory
     cudaStream_t st = stream ? (cudaStream_t)stream : h->comp;
     std::lock_guard<std::mutex> lk(h->mu);
     return run_any(h, dev_patterns, patterns, dev_maxes, dev_neigh, dev_offsets, dev_coefs, st);
@@ -750,6 +824,18 @@ int emida_gb_time_device(emida_gb_handle *h, const void *dev_patterns, uint32_t 
 }
 
 int emida_gb_resolved_mode(const emida_gb_handle *h) { return h ? h->mode : -1; }
+
+int emida_gb_ingest(const emida_gb_handle *h) { return h ? h->ingest : -1; }
+
+int emida_gb_set_ingest(emida_gb_handle *h, int mode)
+{
+    if (!h) return fail(EMIDA_GB_INVALID_ARGUMENT, "null handle");
+    if (mode < EMIDA_GB_INGEST_COPY || mode > EMIDA_GB_INGEST_SPLIT)
+        return fail(EMIDA_GB_INVALID_ARGUMENT, "invalid ingest mode %d", mode);
+    std::lock_guard<std::mutex> lk(h->mu);
+    h->ingest = h->in_place_allowed ? mode : EMIDA_GB_INGEST_COPY;
+    return EMIDA_GB_OK;
+}
 void *emida_gb_stream(emida_gb_handle *h) { return h ? (void *)h->comp : nullptr; }
 int emida_gb_launches_per_run(const emida_gb_handle *h)
 {

@@ -228,7 +228,7 @@ __global__ void __launch_bounds__(N * G / 4, fused_min_blocks(N, sizeof(T)))
     }
     const T *ghann = reinterpret_cast<const T *>(a.hann);
     for (int i = tid; i < 2 * a.side; i += THREADS) hx[i] = ghann[i];  // hx then hy
-    const bool tma = U16 && a.use_tma;
+    const bool tma = U16 && a.stage == STAGE_TMA;
     if (tid == 0) {
         mbar_init(bar, 1);
         fence_proxy_async();
@@ -239,6 +239,10 @@ __global__ void __launch_bounds__(N * G / 4, fused_min_blocks(N, sizeof(T)))
     auto item = [&](uint32_t pair) -> uint4 {
         if (a.items) return a.items[pair];
         return make_uint4(pair / a.n_rois, pair % a.n_rois, pair, (uint32_t)a.fitsize);
+    };
+    auto pattern_base = [&](uint32_t pic) -> const IN * {
+        if (a.pattern_ptrs) return reinterpret_cast<const IN *>(a.pattern_ptrs[pic]);
+        return reinterpret_cast<const IN *>(a.pics) + (size_t)pic * a.src_w * a.src_h;
     };
     auto issue_tile = [&](uint32_t pair) {
         const uint4 it = item(pair);
@@ -267,8 +271,7 @@ __global__ void __launch_bounds__(N * G / 4, fused_min_blocks(N, sizeof(T)))
                     return;
                 }
             } else {
-                const uint16_t *src = reinterpret_cast<const uint16_t *>(a.pics) +
-                                      (size_t)pic * a.src_w * a.src_h +
+                const uint16_t *src = reinterpret_cast<const uint16_t *>(pattern_base(pic)) +
                                       (size_t)beg.y * a.src_w + beg.x;
                 for (int i = tid; i < side * side; i += THREADS)
                     t16[(i / side) * TW + xo + (i % side)] = src[(size_t)(i / side) * a.src_w + (i % side)];
@@ -285,8 +288,8 @@ __global__ void __launch_bounds__(N * G / 4, fused_min_blocks(N, sizeof(T)))
             for (int w = 0; w < WARPS; ++w) total += red_i[w];
             mean = (T)total / (T)(side * side);
         } else {
-            const double *src = reinterpret_cast<const double *>(a.pics) +
-                                (size_t)pic * a.src_w * a.src_h + (size_t)beg.y * a.src_w + beg.x;
+            const double *src = reinterpret_cast<const double *>(pattern_base(pic)) +
+                                (size_t)beg.y * a.src_w + beg.x;
             double acc = 0;
             for (int i = tid; i < side * side; i += THREADS) {
                 double v = src[(size_t)(i / side) * a.src_w + (i % side)];

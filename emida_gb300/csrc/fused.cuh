@@ -7,6 +7,14 @@
 
 namespace emida_gb {
 
+// How a uint16 ROI reaches shared memory.  Pinned host patterns are read in
+// place with plain loads: over the host link the ROI rows arrive at about
+// 100 GB/s either way, and plain loads fetch only the ROI's own pixels.
+enum fused_stage : int {
+    STAGE_PLAIN = 0,  // synchronous loads by every thread
+    STAGE_TMA = 1,    // one TMA box per ROI (device-resident patterns), next ROI prefetched
+};
+
 struct fused_args {
     const void *pics;       // [batch][src_h][src_w] uint16 or double
     uint32_t src_w, src_h;
@@ -19,7 +27,7 @@ struct fused_args {
     const void *twiddles;   // [N] complex T: exp(-2 pi i j / N)
     const double *lstsq;    // (A^T A)^-1 A^T, 6 x s*s
     int fitsize;
-    int use_tma;            // stage the uint16 ROI through a TMA tensor map
+    int stage;              // fused_stage; TMA needs src_w % 8 == 0 and 16-byte aligned patterns
     double *offsets;        // [n_pairs][2]
     double *coefs;          // [n_pairs][6] or null
     void *maxes;            // data_index<T>[n_pairs] or null
@@ -31,6 +39,9 @@ struct fused_args {
     // fit size `fitsize`.
     const uint4 *items;
     const double *lstsq_all; // items mode: the tables for s = 3, 5, 7, 9 back to back
+    // Optional table of pattern base pointers: the pattern of item/pair p is
+    // pattern_ptrs[pattern index] instead of pics + index * src_w * src_h.
+    const void *const *pattern_ptrs;
 };
 
 // Offset of the s x s table inside lstsq_all (6*9, 6*25, 6*49, 6*81 doubles).

@@ -46,6 +46,15 @@ int run_tensor(emida_gb_handle *h, const void *pics, uint32_t pats, void *maxes,
 int run_any(emida_gb_handle *h, const void *pics, uint32_t pats, void *maxes, void *neigh,
             double *offsets, double *coefs, cudaStream_t st);
 int check_device_error(emida_gb_handle *h);
+// Host -> device copy of `patterns` whole patterns as the kernels need them:
+// only the row bands that hold ROI pixels (one pitched copy per band over all
+// patterns), or everything when the bands cover most of a pattern.
+int copy_patterns(emida_gb_handle *h, void *dst, const void *src, uint32_t patterns, cudaStream_t st);
+// Where a pattern array lives.  Device memory is staged through TMA; pinned
+// host memory is read in place by the kernels with plain loads (over the
+// NVLink-C2C host link on Grace systems), which skips the host-to-device copy
+// of the pixels outside the ROIs.  Pageable memory is refused.
+int pattern_location(const void *patterns, bool &on_device);
 
 }  // namespace host
 }  // namespace emida_gb
@@ -98,6 +107,13 @@ struct emida_gb_handle {
     uint32_t *d_err = nullptr;
     std::vector<double> lstsq;
     bool ref_set = false;
+    // How submit brings pinned host batches to the kernels (EMIDA_GB_INGEST_*).
+    // Reading in place is allowed when the ROIs cover at most half of each
+    // pattern and a fused or tensor form runs.
+    bool in_place_allowed = false;
+    // rows [first, first + second) of a pattern that hold ROI pixels, merged
+    std::vector<std::pair<uint32_t, uint32_t>> bands;
+    int ingest = EMIDA_GB_INGEST_COPY;
     std::mutex mu;
     std::vector<void *> allocs;
     // submit/wait ring: one slot per input buffer

@@ -33,10 +33,24 @@ struct emida_gb_multi {
         void *d_spec = nullptr;  // [rois][n/2 + 1][n] complex, column-major per ROI
         size_t spec_cap = 0;     // in ROIs
         const void *hann = nullptr, *twiddles = nullptr;  // owned by the class's first layout
-        uint4 *d_items = nullptr;
-        size_t items_cap = 0;
         int grid = 0;  // 0: one wave of resident CTAs
     };
+    // Work lists of a run, per size class.  Plain runs rotate through RING
+    // sets, so uploading one run's lists waits only for the run RING back, not
+    // for the stream; the last set belongs to the captured graph.
+    struct work_set {
+        std::vector<uint4 *> d_items;  // per size class
+        std::vector<size_t> cap;       // bytes
+        uint4 *h_stage = nullptr;      // pinned staging of every class's items (and pointers)
+        size_t h_cap = 0;              // bytes
+        const void **d_ptrs = nullptr; // pattern pointer table of a table run
+        size_t ptrs_cap = 0;           // bytes
+        cudaEvent_t done = nullptr;    // recorded after the launches that read this set
+        bool pending = false;
+    };
+    static constexpr int RING = 3;
+    work_set sets[RING + 1];
+    int ring_next = 0;
     uint32_t src_w = 0, src_h = 0;
     int precision = EMIDA_GB_FLOAT;
     bool dbl = false;
@@ -116,36 +130,82 @@ int make_plan(emida_gb_multi *m, uint32_t patterns, const uint32_t *layout_of, p
     return EMIDA_GB_OK;
 }
 
-int upload_plan(emida_gb_multi *m, const plan &pl, bool &realloc)
+using work_set = emida_gb_multi::work_set;
+
+// Stages the plan's work lists in `ws` and queues their copies on m->stream,
+// ahead of the launches that read them.  The set must not be read by work
+// still in flight: the graph's set waits for the stream (a replay may be
+// running), a ring set for the run that used it last.
+int upload_plan(emida_gb_multi *m, const plan &pl, work_set &ws, bool graph_set,
+                const void *const *ptrs = nullptr, uint32_t n_ptrs = 0)
 {
-    realloc = false;
-    // the work-list buffers are read by the previous run's kernels: let them finish
-    CK(cudaStreamSynchronize(m->stream));
+    if (graph_set)
+        CK(cudaStreamSynchronize(m->stream));
+    else if (ws.pending)
+        CK(cudaEventSynchronize(ws.done));
+    ws.pending = false;
+    ws.d_items.resize(m->classes.size(), nullptr);
+    ws.cap.resize(m->classes.size(), 0);
+    size_t total = ((size_t)n_ptrs * sizeof(void *) + 15) / 16 * 16;
+    for (const auto &v : pl.items) total += v.size() * sizeof(uint4);
+    if (total > ws.h_cap) {
+        if (ws.h_stage) CK(cudaFreeHost(ws.h_stage));
+        ws.h_stage = nullptr;
+        const size_t cap = std::max(total, 2 * ws.h_cap);
+        CK(cudaMallocHost((void **)&ws.h_stage, cap));
+        ws.h_cap = cap;
+    }
+    size_t off = 0;
+    if (n_ptrs) {
+        const size_t need = (size_t)n_ptrs * sizeof(void *);
+        CKS(grow((void **)&ws.d_ptrs, &ws.ptrs_cap, need, 0));
+        std::memcpy(ws.h_stage, ptrs, need);
+        CK(cudaMemcpyAsync(ws.d_ptrs, ws.h_stage, need, cudaMemcpyHostToDevice, m->stream));
+        off = (need + 15) / 16 * 16;
+    }
     for (size_t c = 0; c < m->classes.size(); ++c) {
-        auto &k = m->classes[c];
         const auto &v = pl.items[c];
         if (v.empty()) continue;
         const size_t need = v.size() * sizeof(uint4);
-        if (need > k.items_cap) realloc = true;
-        CKS(grow((void **)&k.d_items, &k.items_cap, need, 0));
-        CK(cudaMemcpy(k.d_items, v.data(), need, cudaMemcpyHostToDevice));
+        CKS(grow((void **)&ws.d_items[c], &ws.cap[c], need, 0));
+        char *stage = reinterpret_cast<char *>(ws.h_stage) + off;
+        std::memcpy(stage, v.data(), need);
+        CK(cudaMemcpyAsync(ws.d_items[c], stage, need, cudaMemcpyHostToDevice, m->stream));
+        off += need;
     }
     return EMIDA_GB_OK;
 }
 
+work_set &next_ring_set(emida_gb_multi *m)
+{
+    work_set &ws = m->sets[m->ring_next];
+    m->ring_next = (m->ring_next + 1) % emida_gb_multi::RING;
+    return ws;
+}
+
+int mark_used(emida_gb_multi *m, work_set &ws)
+{
+    CK(cudaEventRecord(ws.done, m->stream));
+    ws.pending = true;
+    return EMIDA_GB_OK;
+}
+
 // The launches of one run, on m->stream (capturable).
-int launch_plan(emida_gb_multi *m, const plan &pl, const void *pics, uint32_t patterns,
-                double *offs, double *coefs, void *maxes, int only_class = -1, int grid_override = -1)
+// `pics` is the pattern array that work-list entries index; with a pointer
+// table (`table`, the host copy of ws.d_ptrs) entries index the table instead.
+int launch_plan(emida_gb_multi *m, const plan &pl, const work_set &ws, const void *pics,
+                uint32_t patterns, double *offs, double *coefs, void *maxes, int only_class = -1,
+                int grid_override = -1, const void *const *table = nullptr)
 {
     const size_t pat_bytes = (size_t)m->src_w * m->src_h * 2;
     const size_t di = m->dbl ? sizeof(data_index<double>) : sizeof(data_index<float>);
     CUtensorMap map;
     std::memset(&map, 0, sizeof map);
-    int use_tma = 0;
-    if ((m->src_w % 8) == 0 && ((uintptr_t)pics % 16) == 0) {
-        // one map per size class (the box is the ROI side + 8 by the ROI side)
-        use_tma = get_encoder() != nullptr;
-    }
+    bool on_device = false;
+    if (!table) CKS(pattern_location(pics, on_device));
+    // one TMA map per size class (the box is the ROI side + 8 by the ROI side)
+    const bool use_tma = on_device && (m->src_w % 8) == 0 && ((uintptr_t)pics % 16) == 0 &&
+                         get_encoder() != nullptr;
     for (size_t c = 0; c < m->classes.size(); ++c) {
         if (only_class >= 0 && (int)c != only_class) continue;
         auto &k = m->classes[c];
@@ -169,8 +229,9 @@ int launch_plan(emida_gb_multi *m, const plan &pl, const void *pics, uint32_t pa
         a.maxes = maxes;
         a.neigh = nullptr;
         a.err = m->d_err;
-        a.items = k.d_items;
-        a.use_tma = 0;
+        a.items = ws.d_items[c];
+        a.pattern_ptrs = table ? ws.d_ptrs : nullptr;
+        a.stage = STAGE_PLAIN;
         if (use_tma) {
             const uint32_t side = k.side;
             const cuuint64_t dims[3] = {m->src_w, m->src_h, patterns};
@@ -181,7 +242,7 @@ int launch_plan(emida_gb_multi *m, const plan &pl, const void *pics, uint32_t pa
                               strides, box, estr, CU_TENSOR_MAP_INTERLEAVE_NONE,
                               CU_TENSOR_MAP_SWIZZLE_NONE, CU_TENSOR_MAP_L2_PROMOTION_L2_128B,
                               CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE) == CUDA_SUCCESS)
-                a.use_tma = 1;
+                a.stage = STAGE_TMA;
         }
         const int grid = grid_override >= 0 ? grid_override : k.grid;
         CK(launch_fused(k.n, m->dbl, false, a, &map, grid, m->stream));
@@ -189,7 +250,8 @@ int launch_plan(emida_gb_multi *m, const plan &pl, const void *pics, uint32_t pa
     if (only_class >= 0) return EMIDA_GB_OK;
     for (const auto &e : pl.staged) {
         emida_gb_handle *h = m->layouts[e.layout].h;
-        CKS(run_any(h, (const char *)pics + e.pattern * pat_bytes, 1,
+        const void *src = table ? table[e.pattern] : (const char *)pics + e.pattern * pat_bytes;
+        CKS(run_any(h, src, 1,
                     maxes ? (char *)maxes + e.base * di : nullptr, nullptr, offs + 2 * e.base,
                     coefs ? coefs + 6 * e.base : nullptr, m->stream));
     }
@@ -215,6 +277,7 @@ int emida_gb_multi_create(uint32_t src_w, uint32_t src_h, int32_t precision, emi
     std::vector<double> all(984);
     for (int s : {3, 5, 7, 9}) lstsq_matrix(s, all.data() + lstsq_offset(s));
     CK(cudaStreamCreateWithFlags(&m->stream, cudaStreamNonBlocking));
+    for (auto &ws : m->sets) CK(cudaEventCreateWithFlags(&ws.done, cudaEventDisableTiming));
     CK(cudaMalloc((void **)&m->d_lstsq_all, all.size() * sizeof(double)));
     CK(cudaMemcpy(m->d_lstsq_all, all.data(), all.size() * sizeof(double), cudaMemcpyHostToDevice));
     CK(cudaMalloc((void **)&m->d_err, sizeof(uint32_t)));
@@ -323,13 +386,18 @@ int emida_gb_multi_run(emida_gb_multi *m, const void *dev_patterns, uint32_t pat
     }
     plan pl;
     CKS(make_plan(m, patterns, layout_of, pl));
-    drop_graph(m);  // the work lists it reads are about to be overwritten
-    bool realloc = false;
-    CKS(upload_plan(m, pl, realloc));
-    if (!use_graph) return launch_plan(m, pl, dev_patterns, patterns, dev_offsets, dev_coefs, dev_maxes);
+    if (!use_graph) {
+        work_set &ws = next_ring_set(m);
+        CKS(upload_plan(m, pl, ws, false));
+        CKS(launch_plan(m, pl, ws, dev_patterns, patterns, dev_offsets, dev_coefs, dev_maxes));
+        return mark_used(m, ws);
+    }
+    drop_graph(m);  // the graph's work lists are about to be overwritten
+    work_set &gs = m->sets[emida_gb_multi::RING];
+    CKS(upload_plan(m, pl, gs, true));
     cudaGraph_t graph;
     CK(cudaStreamBeginCapture(m->stream, cudaStreamCaptureModeRelaxed));
-    int st = launch_plan(m, pl, dev_patterns, patterns, dev_offsets, dev_coefs, dev_maxes);
+    int st = launch_plan(m, pl, gs, dev_patterns, patterns, dev_offsets, dev_coefs, dev_maxes);
     cudaError_t e = cudaStreamEndCapture(m->stream, &graph);
     if (st != EMIDA_GB_OK) {
         if (e == cudaSuccess) cudaGraphDestroy(graph);
@@ -358,10 +426,30 @@ int emida_gb_multi_run_slots(emida_gb_multi *m, const void *dev_patterns, uint32
     std::lock_guard<std::mutex> lk(m->mu);
     plan pl;
     CKS(make_plan(m, patterns, layout_of, pl, slots, arena));
-    drop_graph(m);
-    bool realloc = false;
-    CKS(upload_plan(m, pl, realloc));
-    return launch_plan(m, pl, dev_patterns, arena, dev_offsets, dev_coefs, dev_maxes);
+    work_set &ws = next_ring_set(m);
+    CKS(upload_plan(m, pl, ws, false));
+    CKS(launch_plan(m, pl, ws, dev_patterns, arena, dev_offsets, dev_coefs, dev_maxes));
+    return mark_used(m, ws);
+}
+
+int emida_gb_multi_run_table(emida_gb_multi *m, const void *const *patterns, uint32_t n,
+                             const uint32_t *layout_of, double *dev_offsets, double *dev_coefs,
+                             void *dev_maxes)
+{
+    if (!m || !patterns || !layout_of || !dev_offsets)
+        return fail(EMIDA_GB_INVALID_ARGUMENT, "null argument");
+    for (uint32_t p = 0; p < n; ++p) {
+        bool on_device = true;
+        if (!patterns[p]) return fail(EMIDA_GB_INVALID_ARGUMENT, "pattern %u: null pointer", p);
+        CKS(pattern_location(patterns[p], on_device));
+    }
+    std::lock_guard<std::mutex> lk(m->mu);
+    plan pl;
+    CKS(make_plan(m, n, layout_of, pl));
+    work_set &ws = next_ring_set(m);
+    CKS(upload_plan(m, pl, ws, false, patterns, n));
+    CKS(launch_plan(m, pl, ws, nullptr, n, dev_offsets, dev_coefs, dev_maxes, -1, -1, patterns));
+    return mark_used(m, ws);
 }
 
 void *emida_gb_multi_stream(emida_gb_multi *m) { return m ? (void *)m->stream : nullptr; }
@@ -388,9 +476,8 @@ int emida_gb_multi_autotune(emida_gb_multi *m, const void *dev_patterns, uint32_
     std::lock_guard<std::mutex> lk(m->mu);
     plan pl;
     CKS(make_plan(m, patterns, layout_of, pl));
-    drop_graph(m);
-    bool realloc = false;
-    CKS(upload_plan(m, pl, realloc));
+    work_set &ws = next_ring_set(m);
+    CKS(upload_plan(m, pl, ws, false));
     int dev = 0, sms = 0;
     CK(cudaGetDevice(&dev));
     CK(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev));
@@ -405,10 +492,11 @@ int emida_gb_multi_autotune(emida_gb_multi *m, const void *dev_patterns, uint32_
         int best_grid = 0;
         for (int per_sm = 1; per_sm <= 4; ++per_sm) {
             const int grid = per_sm * sms;
-            CKS(launch_plan(m, pl, dev_patterns, patterns, dev_offsets, nullptr, nullptr, (int)c, grid));
+            CKS(launch_plan(m, pl, ws, dev_patterns, patterns, dev_offsets, nullptr, nullptr, (int)c, grid));
             CK(cudaEventRecord(a, m->stream));
             for (int r = 0; r < 3; ++r)
-                CKS(launch_plan(m, pl, dev_patterns, patterns, dev_offsets, nullptr, nullptr, (int)c, grid));
+                CKS(launch_plan(m, pl, ws, dev_patterns, patterns, dev_offsets, nullptr, nullptr, (int)c,
+                                grid));
             CK(cudaEventRecord(b, m->stream));
             CK(cudaEventSynchronize(b));
             float ms = 0;
@@ -426,7 +514,8 @@ int emida_gb_multi_autotune(emida_gb_multi *m, const void *dev_patterns, uint32_
     }
     cudaEventDestroy(a);
     cudaEventDestroy(b);
-    drop_graph(m);
+    CKS(mark_used(m, ws));
+    drop_graph(m);  // captured with the grids chosen before
     if (report && report_len) {
         std::strncpy(report, rep.c_str(), report_len - 1);
         report[report_len - 1] = 0;
@@ -442,7 +531,13 @@ void emida_gb_multi_destroy(emida_gb_multi *m)
     for (auto &k : m->classes) {
         if (k.d_begins) cudaFree(k.d_begins);
         if (k.d_spec) cudaFree(k.d_spec);
-        if (k.d_items) cudaFree(k.d_items);
+    }
+    for (auto &ws : m->sets) {
+        for (uint4 *p : ws.d_items)
+            if (p) cudaFree(p);
+        if (ws.d_ptrs) cudaFree(ws.d_ptrs);
+        if (ws.h_stage) cudaFreeHost(ws.h_stage);
+        if (ws.done) cudaEventDestroy(ws.done);
     }
     for (auto &L : m->layouts) emida_gb_destroy(L.h);
     if (m->d_lstsq_all) cudaFree(m->d_lstsq_all);

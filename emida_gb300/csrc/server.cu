@@ -26,6 +26,7 @@ using namespace emida_gb::host;
 namespace {
 
 using clock_t_ = std::chrono::steady_clock;
+constexpr uint32_t COPY_CHUNK = 16;
 
 struct request {
     uint64_t id = 0;
@@ -34,7 +35,13 @@ struct request {
     std::vector<uint32_t> slots;
     uint32_t next = 0, done = 0;  // patterns scheduled / finished
     std::vector<double> offsets, coefs;
-    cudaEvent_t copied = nullptr;
+    // one event per COPY_CHUNK patterns copied in: steps take a row's patterns
+    // as soon as their chunk has landed, not when the whole row has
+    std::vector<cudaEvent_t> chunks;
+    uint32_t landed_chunks = 0;
+    // read in place from the caller's pinned rows by the kernels: no arena
+    // slots, no copy, computable from the moment it is admitted
+    bool in_place = false;
     bool admitted = false, complete = false;
     int status = EMIDA_GB_OK;
     clock_t_::time_point t_submit, t_done;
@@ -64,7 +71,8 @@ struct pool {
     cudaStream_t copy = nullptr, out = nullptr;
     std::deque<request *> pending;
     std::vector<request *> active;
-    size_t rr = 0;  // round-robin cursor over active rows
+    size_t rr = 0;          // round-robin cursor over active rows
+    uint32_t max_rois = 0;  // largest layout of this pattern size
     step steps[2];
 };
 
@@ -77,6 +85,7 @@ struct emida_gb_server {
     std::vector<std::unique_ptr<pool>> pools;
     struct layout_ref {
         uint32_t pool, id, rois;
+        bool sparse;  // ROIs cover at most half of the pattern: rows may be read in place
     };
     std::vector<layout_ref> layouts;
     std::map<uint64_t, std::unique_ptr<request>> requests;
@@ -91,6 +100,7 @@ struct emida_gb_server {
     bool stop = false;
     int error = EMIDA_GB_OK;
     std::string error_msg;
+    bool zero_copy = true;  // pinned rows on sparse layouts are read in place
 };
 
 namespace {
@@ -99,16 +109,27 @@ int admit(emida_gb_server *sv, pool &p)
 {
     while (!p.pending.empty()) {
         request *r = p.pending.front();
+        if (r->in_place) {
+            p.pending.pop_front();
+            r->admitted = true;
+            p.active.push_back(r);
+            continue;
+        }
         if (p.free_slots.size() < r->n) break;  // wait for slots: rows are admitted whole
         p.pending.pop_front();
         r->slots.assign(p.free_slots.end() - r->n, p.free_slots.end());
         p.free_slots.resize(p.free_slots.size() - r->n);
         const size_t bytes = (size_t)p.w * p.h * 2;
-        for (uint32_t i = 0; i < r->n; ++i)
+        for (uint32_t i = 0; i < r->n; ++i) {
             CK(cudaMemcpyAsync(p.arena + (size_t)r->slots[i] * p.w * p.h, r->host + i * (size_t)p.w * p.h,
                                bytes, cudaMemcpyHostToDevice, p.copy));
-        CK(cudaEventCreateWithFlags(&r->copied, cudaEventDisableTiming));
-        CK(cudaEventRecord(r->copied, p.copy));
+            if ((i + 1) % COPY_CHUNK == 0 || i + 1 == r->n) {
+                cudaEvent_t e;
+                CK(cudaEventCreateWithFlags(&e, cudaEventDisableTiming));
+                r->chunks.push_back(e);
+                CK(cudaEventRecord(e, p.copy));
+            }
+        }
         r->admitted = true;
         p.active.push_back(r);
     }
@@ -140,30 +161,48 @@ int launch_step(emida_gb_server *sv, pool &p, step &st)
     st.parts.clear();
     st.slots.clear();
     std::vector<uint32_t> layout_of;
+    std::vector<const void *> ptrs;
+    bool any_in_place = false;
+    const size_t pat_elems = (size_t)p.w * p.h;
     st.rois = 0;
     uint32_t budget = sv->step_patterns;
     const size_t na = p.active.size();
     for (size_t k = 0; k < na && budget; ++k) {
         request *r = p.active[(p.rr + k) % na];
         if (r->next >= r->n) continue;
-        if (cudaEventQuery(r->copied) != cudaSuccess) continue;
+        while (r->landed_chunks < r->chunks.size() &&
+               cudaEventQuery(r->chunks[r->landed_chunks]) == cudaSuccess)
+            ++r->landed_chunks;
+        const uint32_t landed = r->in_place ? r->n : std::min(r->n, r->landed_chunks * COPY_CHUNK);
+        if (landed <= r->next) continue;
         // an even share per row keeps every row moving
-        uint32_t take = std::min(r->n - r->next, std::max(1u, sv->step_patterns / (uint32_t)na));
+        uint32_t take = std::min(landed - r->next, std::max(1u, sv->step_patterns / (uint32_t)na));
         take = std::min(take, budget);
         st.parts.push_back(step::part{r, r->next, take, st.rois});
         for (uint32_t i = 0; i < take; ++i) {
-            st.slots.push_back(r->slots[r->next + i]);
+            const uint32_t k = r->next + i;
+            const uint32_t slot = r->in_place ? 0 : r->slots[k];
+            st.slots.push_back(slot);
+            ptrs.push_back(r->in_place ? (const void *)(r->host + k * pat_elems)
+                                       : (const void *)(p.arena + slot * pat_elems));
             layout_of.push_back(sv->layouts[r->layout].id);
         }
+        any_in_place |= r->in_place;
         st.rois += (uint64_t)take * r->rois;
         r->next += take;
         budget -= take;
     }
     p.rr = na ? (p.rr + 1) % na : 0;
     if (st.parts.empty()) return EMIDA_GB_OK;
-    CKS(ensure_step_buffers(st, st.rois));
-    CKS(emida_gb_multi_run_slots(p.m, p.arena, p.slots, (uint32_t)st.slots.size(), st.slots.data(),
-                                 layout_of.data(), st.d_offs, st.d_coefs, nullptr));
+    // sized once for the largest step this pool can build (a regrow frees
+    // device memory, which waits for the whole device)
+    CKS(ensure_step_buffers(st, std::max<size_t>(st.rois, (size_t)sv->step_patterns * p.max_rois)));
+    if (any_in_place)
+        CKS(emida_gb_multi_run_table(p.m, ptrs.data(), (uint32_t)ptrs.size(), layout_of.data(), st.d_offs,
+                                     st.d_coefs, nullptr));
+    else
+        CKS(emida_gb_multi_run_slots(p.m, p.arena, p.slots, (uint32_t)st.slots.size(), st.slots.data(),
+                                     layout_of.data(), st.d_offs, st.d_coefs, nullptr));
     cudaStream_t ms = (cudaStream_t)emida_gb_multi_stream(p.m);
     CK(cudaEventRecord(st.done, ms));
     CK(cudaStreamWaitEvent(p.out, st.done, 0));
@@ -183,7 +222,8 @@ void retire_step(emida_gb_server *sv, pool &p, step &st)
         const size_t at = (size_t)part.first * r->rois;
         std::memcpy(r->offsets.data() + 2 * at, st.h_offs + 2 * part.out, n * 2 * sizeof(double));
         std::memcpy(r->coefs.data() + 6 * at, st.h_coefs + 6 * part.out, n * 6 * sizeof(double));
-        for (uint32_t i = 0; i < part.count; ++i) p.free_slots.push_back(r->slots[part.first + i]);
+        if (!r->in_place)
+            for (uint32_t i = 0; i < part.count; ++i) p.free_slots.push_back(r->slots[part.first + i]);
         r->done += part.count;
         sv->pairs_done += n;
         if (r->done == r->n) {
@@ -192,8 +232,8 @@ void retire_step(emida_gb_server *sv, pool &p, step &st)
             sv->latencies.push_back(
                 std::chrono::duration<double, std::milli>(r->t_done - r->t_submit).count());
             p.active.erase(std::find(p.active.begin(), p.active.end(), r));
-            cudaEventDestroy(r->copied);
-            r->copied = nullptr;
+            for (cudaEvent_t e : r->chunks) cudaEventDestroy(e);
+            r->chunks.clear();
         }
     }
     st.parts.clear();
@@ -283,7 +323,9 @@ int emida_gb_server_add_layout(emida_gb_server *sv, uint32_t src_w, uint32_t src
     }
     uint32_t id = 0;
     CKS(emida_gb_multi_add_layout(sv->pools[pi]->m, begins, n_rois, side, fitsize, ref, &id));
-    sv->layouts.push_back({pi, id, n_rois});
+    const bool sparse = 2 * (uint64_t)n_rois * side * side <= (uint64_t)src_w * src_h;
+    sv->layouts.push_back({pi, id, n_rois, sparse});
+    sv->pools[pi]->max_rois = std::max(sv->pools[pi]->max_rois, n_rois);
     *layout_id = (uint32_t)sv->layouts.size() - 1;
     return EMIDA_GB_OK;
 }
@@ -296,9 +338,16 @@ int emida_gb_server_submit(emida_gb_server *sv, uint32_t layout_id, const uint16
     if (layout_id >= sv->layouts.size()) return fail(EMIDA_GB_INVALID_ARGUMENT, "unknown layout %u", layout_id);
     const auto &L = sv->layouts[layout_id];
     pool &p = *sv->pools[L.pool];
-    if (n > p.slots)
+    bool in_place = false;
+    if (L.sparse && sv->zero_copy) {
+        cudaPointerAttributes pa{};
+        CK(cudaPointerGetAttributes(&pa, patterns));
+        in_place = pa.type == cudaMemoryTypeHost;
+    }
+    if (!in_place && n > p.slots)
         return fail(EMIDA_GB_INVALID_ARGUMENT, "a row of %u patterns exceeds the %u-pattern arena", n, p.slots);
     auto r = std::make_unique<request>();
+    r->in_place = in_place;
     r->id = sv->next_id++;
     r->layout = layout_id;
     r->pool = L.pool;
@@ -316,6 +365,14 @@ int emida_gb_server_submit(emida_gb_server *sv, uint32_t layout_id, const uint16
     *request_id = r->id;
     sv->requests[r->id] = std::move(r);
     sv->cv.notify_all();
+    return EMIDA_GB_OK;
+}
+
+int emida_gb_server_set_zero_copy(emida_gb_server *sv, int enable)
+{
+    if (!sv) return fail(EMIDA_GB_INVALID_ARGUMENT, "null argument");
+    std::lock_guard<std::mutex> lk(sv->mu);
+    sv->zero_copy = enable != 0;
     return EMIDA_GB_OK;
 }
 
@@ -384,7 +441,7 @@ void emida_gb_server_destroy(emida_gb_server *sv)
     for (auto &pp : sv->pools)
         if (pp->copy) cudaStreamSynchronize(pp->copy);
     for (auto &kv : sv->requests)
-        if (kv.second->copied) cudaEventDestroy(kv.second->copied);
+        for (cudaEvent_t e : kv.second->chunks) cudaEventDestroy(e);
     for (auto &pp : sv->pools) {
         pool &p = *pp;
         if (p.m) emida_gb_multi_synchronize(p.m);

@@ -109,7 +109,9 @@ int emida_gb_get_offset(emida_gb_handle *h, const void *batch, double *offsets, 
  * may be in flight; a ticket must be waited for before its slot is reused
  * (EMIDA_GB_INVALID_ARGUMENT otherwise).  The host batch must stay untouched
  * until its ticket is waited for.  The process_files pipeline of the reference
- * (src/process_files.hpp:98-233) does the same with threads and two streams. */
+ * (src/process_files.hpp:98-233) does the same with threads and two streams.
+ * A batch in device memory is used in place.  A batch in pinned host memory
+ * arrives as emida_gb_set_ingest chose (default EMIDA_GB_INGEST_COPY). */
 int emida_gb_submit(emida_gb_handle *h, const void *batch, uint32_t patterns, uint64_t *ticket);
 /* Waits for a ticket and copies its offsets [patterns*n_rois][2], coefficients
  * [..][6] and argmax indices [..] to the host (coefs, peaks may be NULL). */
@@ -118,14 +120,29 @@ int emida_gb_wait(emida_gb_handle *h, uint64_t ticket, double *offsets, double *
 
 /* Device-resident form for pipelines and benchmarks: `patterns` whole
  * patterns (any count, not limited to batch_size) already in device memory,
- * results to device memory, all on `stream` (NULL: the handle's compute
- * stream), no synchronisation.  coefs, maxes, neigh may be NULL. */
+ * or in pinned host memory that the kernels read in place (only the ROI
+ * pixels cross the host link), results to device memory, all on `stream`
+ * (NULL: the handle's compute stream), no synchronisation.  Pageable host
+ * memory is refused (EMIDA_GB_INVALID_ARGUMENT).  coefs, maxes, neigh may be
+ * NULL. */
 int emida_gb_run_device(emida_gb_handle *h, const void *dev_patterns, uint32_t patterns,
                         double *dev_offsets, double *dev_coefs, void *dev_maxes,
                         void *dev_neigh, void *stream);
 
 /* Which form the handle runs: EMIDA_GB_MODE_PLAIN, _FUSED or _TENSOR. */
 int emida_gb_resolved_mode(const emida_gb_handle *h);
+/* How emida_gb_submit brings a pinned host batch to the kernels:
+ *   COPY      a copy on the input stream, overlapping the previous batch's path;
+ *   IN_PLACE  no copy: the kernels read the batch's ROI pixels in place over the
+ *             host link (lowest latency per batch);
+ *   SPLIT     every other batch each way, so the copy engine and the kernels'
+ *             host reads work in parallel (highest throughput).
+ * IN_PLACE and SPLIT are taken only by a fused or tensor form whose ROIs cover
+ * at most half of each pattern; otherwise the mode stays COPY.
+ * emida_gb_ingest reports the mode in force. */
+enum { EMIDA_GB_INGEST_COPY = 0, EMIDA_GB_INGEST_IN_PLACE = 1, EMIDA_GB_INGEST_SPLIT = 2 };
+int emida_gb_set_ingest(emida_gb_handle *h, int mode);
+int emida_gb_ingest(const emida_gb_handle *h);
 /* The handle's compute stream (a cudaStream_t). */
 void *emida_gb_stream(emida_gb_handle *h);
 /* Number of kernel launches one emida_gb_run_device call makes. */
@@ -170,6 +187,13 @@ int emida_gb_multi_run(emida_gb_multi *m, const void *dev_patterns, uint32_t pat
 int emida_gb_multi_run_slots(emida_gb_multi *m, const void *dev_patterns, uint32_t arena,
                              uint32_t patterns, const uint32_t *slots, const uint32_t *layout_of,
                              double *dev_offsets, double *dev_coefs, void *dev_maxes);
+/* The same with one pointer per pattern: patterns[p] is pattern p in device
+ * memory or in pinned host memory, which the kernels then read in place (only
+ * the ROI pixels cross the host link).  The pointers and the memory behind
+ * them must stay valid until the run has completed; no graph. */
+int emida_gb_multi_run_table(emida_gb_multi *m, const void *const *patterns, uint32_t n,
+                             const uint32_t *layout_of, double *dev_offsets, double *dev_coefs,
+                             void *dev_maxes);
 /* The planner's stream (a cudaStream_t) and a wait for its work. */
 void *emida_gb_multi_stream(emida_gb_multi *m);
 int emida_gb_multi_synchronize(emida_gb_multi *m);
@@ -188,7 +212,10 @@ void emida_gb_multi_destroy(emida_gb_multi *m);
  * and computed in steps of up to step_patterns patterns drawn from every
  * admitted row in turn, so rows that arrive while others run share the next
  * steps.  The host patterns must stay valid until the request is waited for;
- * pinned memory lets the copies overlap.  Results are per row, pattern-major. */
+ * pinned memory lets the copies overlap.  A pinned row on a layout whose ROIs
+ * cover at most half of the pattern is not copied at all: the kernels read its
+ * ROI pixels in place (switch off with emida_gb_server_set_zero_copy).  Results
+ * are per row, pattern-major. */
 typedef struct emida_gb_server emida_gb_server;
 int emida_gb_server_create(int32_t precision, uint64_t hbm_bytes, uint32_t step_patterns,
                            emida_gb_server **out);
@@ -197,6 +224,8 @@ int emida_gb_server_add_layout(emida_gb_server *s, uint32_t src_w, uint32_t src_
                                int32_t fitsize, const uint16_t *ref, uint32_t *layout_id);
 int emida_gb_server_submit(emida_gb_server *s, uint32_t layout_id, const uint16_t *patterns,
                            uint32_t n, uint64_t *request_id);
+/* enable = 0: every row is copied into the arena (rows submitted later). */
+int emida_gb_server_set_zero_copy(emida_gb_server *s, int enable);
 /* Blocks until the row is done; offsets [n*rois][2], coefs [n*rois][6] may be
  * NULL; latency_ms = submission to completion. */
 int emida_gb_server_wait(emida_gb_server *s, uint64_t request_id, double *offsets, double *coefs,

@@ -1,0 +1,121 @@
+"""Patterns in pinned host memory read in place by the kernels (zero-copy):
+every entry that accepts them gives the same bits as the copied or
+device-resident run of the same patterns."""
+import numpy as np
+import pytest
+
+pytestmark = pytest.mark.gpu
+
+
+@pytest.fixture(scope="module", autouse=True)
+def built():
+    import __graft_entry__
+    __graft_entry__.build_library()
+
+
+@pytest.fixture(scope="module")
+def data():
+    from emida_gb300 import synth
+    ref = synth.reference_pattern(512, seed=41)
+    pics, _ = synth.deformed_patterns(512, 41, 6, sigma_eps=3e-3)
+    _, begins = synth.roi_grid(512, 4, 32, margin=48)
+    return ref, pics, begins
+
+
+@pytest.mark.parametrize("policy,mode", [("fft", "fused"), ("brute", "tensor"), ("fft", "plain")])
+def test_run_device_on_pinned_host_patterns(data, policy, mode):
+    from emida_gb300 import DeviceBuffer, GpuOffset, _lib, pinned_array
+    ref, pics, begins = data
+    n, S = len(pics), len(begins)
+    g = GpuOffset((512, 512), begins, (64, 64), (127, 127), n, policy, 5, 1, "float", np.uint16, mode)
+    g.allocate_memory(ref)
+    host = pinned_array(pics.shape)
+    host[:] = pics
+    d_pics = DeviceBuffer.from_array(pics)
+    o_dev, o_host = DeviceBuffer(n * S * 16), DeviceBuffer(n * S * 16)
+    g.run_device(d_pics, n, o_dev)
+    g.run_device(host.ctypes.data, n, o_host)
+    _lib.call("emida_gb_synchronize")
+    assert np.array_equal(o_dev.download(np.float64, (n * S, 2)), o_host.download(np.float64, (n * S, 2)))
+    g.close()
+
+
+def test_pageable_patterns_are_refused_by_run_device(data):
+    from emida_gb300 import DeviceBuffer, EmidaError, GpuOffset
+    ref, pics, begins = data
+    g = GpuOffset((512, 512), begins, (64, 64), (127, 127), 2, "fft", 5, 1, "float", np.uint16, "fused")
+    g.allocate_memory(ref)
+    pageable = np.ascontiguousarray(pics[:2])
+    with pytest.raises(EmidaError, match="pinned host memory"):
+        g.run_device(pageable.ctypes.data, 2, DeviceBuffer(2 * len(begins) * 16))
+    g.close()
+
+
+def test_submit_reads_pinned_batches_in_place(data):
+    from emida_gb300 import GpuOffset, pinned_array
+    ref, pics, begins = data
+    g = GpuOffset((512, 512), begins, (64, 64), (127, 127), 3, "fft", 5, 3, "float", np.uint16, "fused")
+    g.allocate_memory(ref)
+    assert g.ingest == "copy"  # the default
+    host = pinned_array(pics.shape)
+    host[:] = pics
+    expect = [g.get_offset(pics[k:k + 3]) for k in (0, 3)]
+    for mode in ("in_place", "split", "copy"):
+        g.ingest = mode
+        assert g.ingest == mode  # 16 ROIs of 64^2 cover a quarter of a 512^2 pattern
+        tickets = [g.submit(host[k:k + 3]) for k in (0, 3, 0)]
+        for t, (e_offs, e_coefs) in zip(tickets, expect + expect[:1]):
+            offs, coefs = g.wait(t)
+            assert np.array_equal(offs, e_offs) and np.array_equal(coefs, e_coefs)
+    g.close()
+    # ROIs that cover most of the pattern are copied, not read in place
+    _, dense = __import__("emida_gb300").synth.roi_grid(512, 7, 32, margin=32)
+    g = GpuOffset((512, 512), dense, (64, 64), (127, 127), 1, "fft", 5, 1, "float", np.uint16, "fused")
+    g.ingest = "split"
+    assert g.ingest == "copy"
+    g.close()
+
+
+def test_multi_run_table_mixes_device_and_host_patterns(data):
+    from emida_gb300 import DeviceBuffer, MultiLayout, pinned_array, synth
+    ref, pics, begins = data
+    m = MultiLayout((512, 512), "float")
+    lay = [(begins, 64, 5)]
+    for r, s, n in ((24, 3, 7), (48, 9, 3), (64, 5, 2)):  # 96-, 192-point fused, 256 staged
+        _, b = synth.random_layout(512, 60 + r, r, n, margin=4)
+        lay.append((b, 2 * r, s))
+    for b, side, s in lay:
+        m.add_layout(b, side, s, ref)
+    layout_of = np.array([0, 1, 2, 3, 1, 0], dtype=np.uint32)
+    total = m.count(layout_of)
+    d_pics = DeviceBuffer.from_array(pics)
+    o_arr, o_tab = DeviceBuffer(total * 16), DeviceBuffer(total * 16)
+    m.run(d_pics, layout_of, o_arr, graph=False)
+    host = pinned_array(pics.shape)
+    host[:] = pics
+    ptrs = [host[p] if p % 2 else d_pics.ptr.value + p * 512 * 512 * 2 for p in range(len(pics))]
+    m.run_table(ptrs, layout_of, o_tab)
+    m.synchronize()
+    assert np.array_equal(o_arr.download(np.float64, (total, 2)), o_tab.download(np.float64, (total, 2)))
+    m.close()
+
+
+def test_server_rows_in_place_equal_copied_rows(data):
+    from emida_gb300 import Server, pinned_array, synth
+    ref, pics, begins = data
+    _, wide = synth.roi_grid(512, 7, 32, margin=32)  # covers most of the pattern: copied
+    results = {}
+    for zero_copy in (False, True):
+        s = Server("float", hbm_bytes=8 * 512 * 512 * 2, step_patterns=4, zero_copy=zero_copy)
+        sparse = s.add_layout((512, 512), begins, 64, 5, ref)
+        dense = s.add_layout((512, 512), wide, 64, 3, ref)
+        rows = []
+        for k in range(4):
+            host = pinned_array((3, 512, 512))
+            host[:] = pics[k:k + 3]
+            rows.append((sparse if k % 2 == 0 else dense, host))
+        rids = [s.submit(lid, h) for lid, h in rows]
+        results[zero_copy] = [s.wait(r)[:2] for r in rids]
+        s.close()
+    for (a_offs, a_coefs), (b_offs, b_coefs) in zip(results[False], results[True]):
+        assert np.array_equal(a_offs, b_offs) and np.array_equal(a_coefs, b_coefs)
