@@ -215,14 +215,15 @@ fft_tables emida_gb::host::tables(const emida_gb_handle *h)
 // The staged pipeline for `pats` patterns from `pics` (<= B patterns):
 // src/gpu_offset.hpp:234-278 stage by stage.
 int emida_gb::host::run_plain_chunk(emida_gb_handle *h, const void *pics, uint32_t pats, void *maxes, void *neigh,
-                    double *offsets, double *coefs, cudaStream_t st)
+                    double *offsets, double *coefs, cudaStream_t st, const void *const *ptrs,
+                    const uint32_t *out_base, void *maxes_out)
 {
     const uint32_t n = pats * h->S;
     const int pol = h->fft ? POLICY_FFT : POLICY_BRUTE;
     CK(run_sums(pics, h->in_f64 ? IN_F64 : IN_U16, h->src, h->d_begins, h->S, h->slice, pats,
-                h->d_sums, st));
+                h->d_sums, st, ptrs));
     CK(run_prepare(pics, h->in_f64 ? IN_F64 : IN_U16, h->dbl, h->d_prep, h->d_hann, h->d_sums,
-                   h->d_begins, h->src, h->slice, h->prep_size(), h->S, pats, st));
+                   h->d_begins, h->src, h->slice, h->prep_size(), h->S, pats, st, ptrs));
     if (h->fft) {
         CK(run_fft_r2c(h->d_prep, h->d_spec, n, tables(h), h->dbl, st));
         CK(run_hadamard(h->d_spec, h->d_ref_spec, h->h2 * h->half, h->S, pats, h->dbl, st));
@@ -236,7 +237,8 @@ int emida_gb::host::run_plain_chunk(emida_gb_handle *h, const void *pics, uint32
     CK(run_maxarg(h->d_map, h->map_size(), n, mx, h->dbl, st));
     CK(run_extract_neighbors(h->d_map, mx, nb, h->p.fitsize, h->cross, n, pol, h->dbl, st));
     if (offsets)
-        CK(run_fit(nb, mx, n, h->p.fitsize, h->cross, pol, h->d_lstsq, h->dbl, offsets, coefs, st));
+        CK(run_fit(nb, mx, n, h->p.fitsize, h->cross, pol, h->d_lstsq, h->dbl, offsets, coefs, st,
+                   out_base, h->S, maxes_out));
     return EMIDA_GB_OK;
 }
 

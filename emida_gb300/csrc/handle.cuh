@@ -36,8 +36,13 @@ int upload_hann(emida_gb_handle *h, void **dst, uint32_t nx, uint32_t ny);
 int upload_twiddles(emida_gb_handle *h, void **dst, uint32_t n);
 fft_tables tables(const emida_gb_handle *h);
 // The staged pipeline for pats <= batch_size patterns (src/gpu_offset.hpp:234-278).
+// With `ptrs` (device table) pattern p is ptrs[p]; with `out_base` (device,
+// per pattern) its results land at output slots out_base[p] + roi, maxima in
+// maxes_out.
 int run_plain_chunk(emida_gb_handle *h, const void *pics, uint32_t pats, void *maxes, void *neigh,
-                    double *offsets, double *coefs, cudaStream_t st);
+                    double *offsets, double *coefs, cudaStream_t st,
+                    const void *const *ptrs = nullptr, const uint32_t *out_base = nullptr,
+                    void *maxes_out = nullptr);
 int run_fused(emida_gb_handle *h, const void *pics, uint32_t pats, void *maxes, void *neigh,
               double *offsets, double *coefs, cudaStream_t st);
 int run_tensor(emida_gb_handle *h, const void *pics, uint32_t pats, void *maxes, void *neigh,

@@ -45,6 +45,14 @@ struct emida_gb_multi {
         size_t h_cap = 0;              // bytes
         const void **d_ptrs = nullptr; // pattern pointer table of a table run
         size_t ptrs_cap = 0;           // bytes
+        // staged layouts: per layout a run of (pattern address, first output slot)
+        struct staged_group {
+            uint32_t layout, offset, count;
+        };
+        std::vector<staged_group> sgroups;
+        const void **d_sptrs = nullptr;
+        uint32_t *d_sbase = nullptr;
+        size_t sptrs_cap = 0, sbase_cap = 0;  // bytes
         cudaEvent_t done = nullptr;    // recorded after the launches that read this set
         bool pending = false;
     };
@@ -70,6 +78,8 @@ struct emida_gb_multi {
 };
 
 namespace {
+
+constexpr uint32_t STAGED_BATCH = 16;
 
 size_t spec_bytes_per_roi(uint32_t n, bool dbl) { return (size_t)(n / 2 + 1) * n * (dbl ? 16 : 8); }
 
@@ -136,7 +146,7 @@ using work_set = emida_gb_multi::work_set;
 // ahead of the launches that read them.  The set must not be read by work
 // still in flight: the graph's set waits for the stream (a replay may be
 // running), a ring set for the run that used it last.
-int upload_plan(emida_gb_multi *m, const plan &pl, work_set &ws, bool graph_set,
+int upload_plan(emida_gb_multi *m, const plan &pl, work_set &ws, bool graph_set, const void *pics,
                 const void *const *ptrs = nullptr, uint32_t n_ptrs = 0)
 {
     if (graph_set)
@@ -146,7 +156,30 @@ int upload_plan(emida_gb_multi *m, const plan &pl, work_set &ws, bool graph_set,
     ws.pending = false;
     ws.d_items.resize(m->classes.size(), nullptr);
     ws.cap.resize(m->classes.size(), 0);
-    size_t total = ((size_t)n_ptrs * sizeof(void *) + 15) / 16 * 16;
+    // staged patterns grouped by layout, in plan order within a layout
+    ws.sgroups.clear();
+    std::vector<const void *> sptrs;
+    std::vector<uint32_t> sbase;
+    if (!pl.staged.empty()) {
+        const size_t pat_bytes = (size_t)m->src_w * m->src_h * 2;
+        std::vector<std::vector<const staged_item *>> by_layout(m->layouts.size());
+        std::vector<uint32_t> order;
+        for (const auto &e : pl.staged) {
+            if (by_layout[e.layout].empty()) order.push_back(e.layout);
+            by_layout[e.layout].push_back(&e);
+        }
+        for (uint32_t l : order) {
+            ws.sgroups.push_back({l, (uint32_t)sptrs.size(), (uint32_t)by_layout[l].size()});
+            for (const staged_item *e : by_layout[l]) {
+                sptrs.push_back(ptrs ? ptrs[e->pattern]
+                                     : (const void *)((const char *)pics + e->pattern * pat_bytes));
+                sbase.push_back((uint32_t)e->base);
+            }
+        }
+    }
+    auto up16 = [](size_t v) { return (v + 15) / 16 * 16; };
+    size_t total = up16((size_t)n_ptrs * sizeof(void *)) + up16(sptrs.size() * sizeof(void *)) +
+                   up16(sbase.size() * sizeof(uint32_t));
     for (const auto &v : pl.items) total += v.size() * sizeof(uint4);
     if (total > ws.h_cap) {
         if (ws.h_stage) CK(cudaFreeHost(ws.h_stage));
@@ -156,13 +189,18 @@ int upload_plan(emida_gb_multi *m, const plan &pl, work_set &ws, bool graph_set,
         ws.h_cap = cap;
     }
     size_t off = 0;
-    if (n_ptrs) {
-        const size_t need = (size_t)n_ptrs * sizeof(void *);
-        CKS(grow((void **)&ws.d_ptrs, &ws.ptrs_cap, need, 0));
-        std::memcpy(ws.h_stage, ptrs, need);
-        CK(cudaMemcpyAsync(ws.d_ptrs, ws.h_stage, need, cudaMemcpyHostToDevice, m->stream));
-        off = (need + 15) / 16 * 16;
-    }
+    auto stage = [&](void **dst, size_t *cap, const void *src, size_t need) -> int {
+        if (!need) return EMIDA_GB_OK;
+        CKS(grow(dst, cap, need, 0));
+        char *s = reinterpret_cast<char *>(ws.h_stage) + off;
+        std::memcpy(s, src, need);
+        CK(cudaMemcpyAsync(*dst, s, need, cudaMemcpyHostToDevice, m->stream));
+        off += up16(need);
+        return EMIDA_GB_OK;
+    };
+    CKS(stage((void **)&ws.d_ptrs, &ws.ptrs_cap, ptrs, (size_t)n_ptrs * sizeof(void *)));
+    CKS(stage((void **)&ws.d_sptrs, &ws.sptrs_cap, sptrs.data(), sptrs.size() * sizeof(void *)));
+    CKS(stage((void **)&ws.d_sbase, &ws.sbase_cap, sbase.data(), sbase.size() * sizeof(uint32_t)));
     for (size_t c = 0; c < m->classes.size(); ++c) {
         const auto &v = pl.items[c];
         if (v.empty()) continue;
@@ -197,8 +235,6 @@ int launch_plan(emida_gb_multi *m, const plan &pl, const work_set &ws, const voi
                 uint32_t patterns, double *offs, double *coefs, void *maxes, int only_class = -1,
                 int grid_override = -1, const void *const *table = nullptr)
 {
-    const size_t pat_bytes = (size_t)m->src_w * m->src_h * 2;
-    const size_t di = m->dbl ? sizeof(data_index<double>) : sizeof(data_index<float>);
     CUtensorMap map;
     std::memset(&map, 0, sizeof map);
     bool on_device = false;
@@ -248,12 +284,15 @@ int launch_plan(emida_gb_multi *m, const plan &pl, const work_set &ws, const voi
         CK(launch_fused(k.n, m->dbl, false, a, &map, grid, m->stream));
     }
     if (only_class >= 0) return EMIDA_GB_OK;
-    for (const auto &e : pl.staged) {
-        emida_gb_handle *h = m->layouts[e.layout].h;
-        const void *src = table ? table[e.pattern] : (const char *)pics + e.pattern * pat_bytes;
-        CKS(run_any(h, src, 1,
-                    maxes ? (char *)maxes + e.base * di : nullptr, nullptr, offs + 2 * e.base,
-                    coefs ? coefs + 6 * e.base : nullptr, m->stream));
+    // staged layouts: batches of their patterns through the staged pipeline,
+    // results scattered to each pattern's output slots
+    for (const auto &sg : ws.sgroups) {
+        emida_gb_handle *h = m->layouts[sg.layout].h;
+        for (uint32_t k = 0; k < sg.count; k += h->B) {
+            const uint32_t c = std::min(h->B, sg.count - k);
+            CKS(run_plain_chunk(h, nullptr, c, nullptr, nullptr, offs, coefs, m->stream,
+                                ws.d_sptrs + sg.offset + k, ws.d_sbase + sg.offset + k, maxes));
+        }
     }
     return EMIDA_GB_OK;
 }
@@ -299,7 +338,9 @@ int emida_gb_multi_add_layout(emida_gb_multi *m, const uint32_t *begins, uint32_
     p.n_rois = n_rois;
     p.slice_w = p.slice_h = side;
     p.cross_w = p.cross_h = 2 * side - 1;
-    p.batch_size = 1;
+    // layouts without a fused kernel run the staged pipeline over up to
+    // STAGED_BATCH of their patterns per launch sequence
+    p.batch_size = fused_size_for(side, m->dbl) ? 1 : STAGED_BATCH;
     p.policy = EMIDA_GB_FFT;
     p.precision = m->precision;
     p.fitsize = fitsize;
@@ -388,13 +429,13 @@ int emida_gb_multi_run(emida_gb_multi *m, const void *dev_patterns, uint32_t pat
     CKS(make_plan(m, patterns, layout_of, pl));
     if (!use_graph) {
         work_set &ws = next_ring_set(m);
-        CKS(upload_plan(m, pl, ws, false));
+        CKS(upload_plan(m, pl, ws, false, dev_patterns));
         CKS(launch_plan(m, pl, ws, dev_patterns, patterns, dev_offsets, dev_coefs, dev_maxes));
         return mark_used(m, ws);
     }
     drop_graph(m);  // the graph's work lists are about to be overwritten
     work_set &gs = m->sets[emida_gb_multi::RING];
-    CKS(upload_plan(m, pl, gs, true));
+    CKS(upload_plan(m, pl, gs, true, dev_patterns));
     cudaGraph_t graph;
     CK(cudaStreamBeginCapture(m->stream, cudaStreamCaptureModeRelaxed));
     int st = launch_plan(m, pl, gs, dev_patterns, patterns, dev_offsets, dev_coefs, dev_maxes);
@@ -427,7 +468,7 @@ int emida_gb_multi_run_slots(emida_gb_multi *m, const void *dev_patterns, uint32
     plan pl;
     CKS(make_plan(m, patterns, layout_of, pl, slots, arena));
     work_set &ws = next_ring_set(m);
-    CKS(upload_plan(m, pl, ws, false));
+    CKS(upload_plan(m, pl, ws, false, dev_patterns));
     CKS(launch_plan(m, pl, ws, dev_patterns, arena, dev_offsets, dev_coefs, dev_maxes));
     return mark_used(m, ws);
 }
@@ -447,7 +488,7 @@ int emida_gb_multi_run_table(emida_gb_multi *m, const void *const *patterns, uin
     plan pl;
     CKS(make_plan(m, n, layout_of, pl));
     work_set &ws = next_ring_set(m);
-    CKS(upload_plan(m, pl, ws, false, patterns, n));
+    CKS(upload_plan(m, pl, ws, false, nullptr, patterns, n));
     CKS(launch_plan(m, pl, ws, nullptr, n, dev_offsets, dev_coefs, dev_maxes, -1, -1, patterns));
     return mark_used(m, ws);
 }
@@ -477,7 +518,7 @@ int emida_gb_multi_autotune(emida_gb_multi *m, const void *dev_patterns, uint32_
     plan pl;
     CKS(make_plan(m, patterns, layout_of, pl));
     work_set &ws = next_ring_set(m);
-    CKS(upload_plan(m, pl, ws, false));
+    CKS(upload_plan(m, pl, ws, false, dev_patterns));
     int dev = 0, sms = 0;
     CK(cudaGetDevice(&dev));
     CK(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev));
@@ -536,6 +577,8 @@ void emida_gb_multi_destroy(emida_gb_multi *m)
         for (uint4 *p : ws.d_items)
             if (p) cudaFree(p);
         if (ws.d_ptrs) cudaFree(ws.d_ptrs);
+        if (ws.d_sptrs) cudaFree(ws.d_sptrs);
+        if (ws.d_sbase) cudaFree(ws.d_sbase);
         if (ws.h_stage) cudaFreeHost(ws.h_stage);
         if (ws.done) cudaEventDestroy(ws.done);
     }

@@ -86,6 +86,7 @@ struct emida_gb_server {
     struct layout_ref {
         uint32_t pool, id, rois;
         bool sparse;  // ROIs cover at most half of the pattern: rows may be read in place
+        std::vector<std::pair<uint32_t, uint32_t>> bands;  // (first row, rows) holding ROI pixels
     };
     std::vector<layout_ref> layouts;
     std::map<uint64_t, std::unique_ptr<request>> requests;
@@ -119,16 +120,26 @@ int admit(emida_gb_server *sv, pool &p)
         p.pending.pop_front();
         r->slots.assign(p.free_slots.end() - r->n, p.free_slots.end());
         p.free_slots.resize(p.free_slots.size() - r->n);
-        const size_t bytes = (size_t)p.w * p.h * 2;
-        for (uint32_t i = 0; i < r->n; ++i) {
-            CK(cudaMemcpyAsync(p.arena + (size_t)r->slots[i] * p.w * p.h, r->host + i * (size_t)p.w * p.h,
-                               bytes, cudaMemcpyHostToDevice, p.copy));
-            if ((i + 1) % COPY_CHUNK == 0 || i + 1 == r->n) {
-                cudaEvent_t e;
-                CK(cudaEventCreateWithFlags(&e, cudaEventDisableTiming));
-                r->chunks.push_back(e);
-                CK(cudaEventRecord(e, p.copy));
+        std::sort(r->slots.begin(), r->slots.end());  // consecutive slots copy as one
+        const size_t row = (size_t)p.w * 2, pat = row * p.h;
+        const auto &bands = sv->layouts[r->layout].bands;
+        for (uint32_t c0 = 0; c0 < r->n; c0 += COPY_CHUNK) {
+            const uint32_t c1 = std::min(r->n, c0 + COPY_CHUNK);
+            for (uint32_t a = c0; a < c1;) {
+                uint32_t b = a + 1;
+                while (b < c1 && r->slots[b] == r->slots[b - 1] + 1) ++b;
+                // patterns a..b-1 go to consecutive slots: one pitched copy per ROI row band
+                const char *src = reinterpret_cast<const char *>(r->host) + a * pat;
+                char *dst = reinterpret_cast<char *>(p.arena) + r->slots[a] * pat;
+                for (const auto &bd : bands)
+                    CK(cudaMemcpy2DAsync(dst + bd.first * row, pat, src + bd.first * row, pat,
+                                         bd.second * row, b - a, cudaMemcpyHostToDevice, p.copy));
+                a = b;
             }
+            cudaEvent_t e;
+            CK(cudaEventCreateWithFlags(&e, cudaEventDisableTiming));
+            r->chunks.push_back(e);
+            CK(cudaEventRecord(e, p.copy));
         }
         r->admitted = true;
         p.active.push_back(r);
@@ -324,7 +335,18 @@ int emida_gb_server_add_layout(emida_gb_server *sv, uint32_t src_w, uint32_t src
     uint32_t id = 0;
     CKS(emida_gb_multi_add_layout(sv->pools[pi]->m, begins, n_rois, side, fitsize, ref, &id));
     const bool sparse = 2 * (uint64_t)n_rois * side * side <= (uint64_t)src_w * src_h;
-    sv->layouts.push_back({pi, id, n_rois, sparse});
+    // merged row bands of the ROIs: a copied row moves only these
+    std::vector<std::pair<uint32_t, uint32_t>> iv, bands;
+    for (uint32_t r = 0; r < n_rois; ++r) iv.push_back({begins[2 * r + 1], begins[2 * r + 1] + side});
+    std::sort(iv.begin(), iv.end());
+    for (const auto &v : iv) {
+        if (!bands.empty() && v.first <= bands.back().second)
+            bands.back().second = std::max(bands.back().second, v.second);
+        else
+            bands.push_back(v);
+    }
+    for (auto &b : bands) b.second -= b.first;
+    sv->layouts.push_back({pi, id, n_rois, sparse, bands});
     sv->pools[pi]->max_rois = std::max(sv->pools[pi]->max_rois, n_rois);
     *layout_id = (uint32_t)sv->layouts.size() - 1;
     return EMIDA_GB_OK;

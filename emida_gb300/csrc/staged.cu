@@ -33,13 +33,15 @@ __device__ __forceinline__ V block_sum(V v, V *scratch)
 template <typename IN>
 __global__ void __launch_bounds__(BLOCK) k_sums(const IN *__restrict__ pics, size2 src,
                                                 const uint2 *__restrict__ begins, uint32_t n_rois,
-                                                size2 slice, typename sum_of<IN>::type *sums)
+                                                size2 slice, typename sum_of<IN>::type *sums,
+                                                const void *const *__restrict__ ptrs)
 {
     using S = typename sum_of<IN>::type;
     __shared__ S scratch[32];
     const uint32_t pair = blockIdx.x, pic = pair / n_rois, roi = pair % n_rois;
     const uint2 b = begins[roi];
-    const IN *p = pics + (size_t)pic * src.x * src.y + (size_t)b.y * src.x + b.x;
+    const IN *base = ptrs ? reinterpret_cast<const IN *>(ptrs[pic]) : pics + (size_t)pic * src.x * src.y;
+    const IN *p = base + (size_t)b.y * src.x + b.x;
     S acc = 0;
     const uint32_t area = slice.x * slice.y;
     for (uint32_t i = threadIdx.x; i < area; i += BLOCK)
@@ -54,7 +56,7 @@ __global__ void __launch_bounds__(BLOCK)
     k_prepare(const IN *__restrict__ pics, T *__restrict__ out, const T *__restrict__ hann,
               const typename sum_of<IN>::type *__restrict__ sums,
               const uint2 *__restrict__ begins, size2 src, size2 slice, size2 out_size,
-              uint32_t n_rois, uint32_t n_pairs)
+              uint32_t n_rois, uint32_t n_pairs, const void *const *__restrict__ ptrs)
 {
     const uint64_t tid = (uint64_t)blockIdx.x * BLOCK + threadIdx.x;
     const uint32_t area = slice.x * slice.y;
@@ -63,7 +65,8 @@ __global__ void __launch_bounds__(BLOCK)
     const uint32_t within = (uint32_t)(tid % area), x = within % slice.x, y = within / slice.x;
     const uint32_t pic = (uint32_t)(pair / n_rois), roi = (uint32_t)(pair % n_rois);
     const uint2 b = begins[roi];
-    T pixel = (T)pics[(size_t)pic * src.x * src.y + (size_t)(b.y + y) * src.x + b.x + x];
+    const IN *base = ptrs ? reinterpret_cast<const IN *>(ptrs[pic]) : pics + (size_t)pic * src.x * src.y;
+    T pixel = (T)base[(size_t)(b.y + y) * src.x + b.x + x];
     pixel -= (T)sums[pair] / (T)area;
     pixel = pixel * hann[x] * hann[slice.x + y];
     out[pair * out_size.x * out_size.y + (size_t)y * out_size.x + x] = pixel;
@@ -329,7 +332,8 @@ template <typename T>
 __global__ void __launch_bounds__(BLOCK)
     k_fit(const T *__restrict__ neigh, const data_index<T> *__restrict__ mi, uint32_t n, int s,
           size2 cross, int policy, const double *__restrict__ lstsq, double *offsets,
-          double *coefs)
+          double *coefs, const uint32_t *__restrict__ out_base, uint32_t n_rois,
+          data_index<T> *maxes_out)
 {
     const uint64_t tid = (uint64_t)blockIdx.x * BLOCK + threadIdx.x;
     if (tid >= n) return;
@@ -342,10 +346,12 @@ __global__ void __launch_bounds__(BLOCK)
     shift_pos(mi[tid].index, policy, cross.x, cross.y, mx, my);
     double ox, oy;
     fit_offsets(c, mx, my, cross.x, cross.y, s, ox, oy);
-    offsets[2 * tid] = ox;
-    offsets[2 * tid + 1] = oy;
+    const uint64_t o = out_base ? (uint64_t)out_base[tid / n_rois] + tid % n_rois : tid;
+    offsets[2 * o] = ox;
+    offsets[2 * o + 1] = oy;
     if (coefs)
-        for (int j = 0; j < 6; ++j) coefs[6 * tid + j] = c[j];
+        for (int j = 0; j < 6; ++j) coefs[6 * o + j] = c[j];
+    if (maxes_out) maxes_out[o] = mi[tid];
 }
 
 template <typename T>
@@ -365,22 +371,24 @@ inline uint32_t grid_for(uint64_t n) { return (uint32_t)((n + BLOCK - 1) / BLOCK
 }  // namespace
 
 cudaError_t run_sums(const void *pics, int in_type, size2 src, const uint2 *begins,
-                     uint32_t n_rois, size2 slice, uint32_t batch, void *sums, cudaStream_t st)
+                     uint32_t n_rois, size2 slice, uint32_t batch, void *sums, cudaStream_t st,
+                     const void *const *ptrs)
 {
     const uint32_t n = n_rois * batch;
     if (n == 0) return cudaSuccess;
     if (in_type == IN_U16)
         k_sums<uint16_t><<<n, BLOCK, 0, st>>>(reinterpret_cast<const uint16_t *>(pics), src, begins,
-                                              n_rois, slice, reinterpret_cast<uint32_t *>(sums));
+                                              n_rois, slice, reinterpret_cast<uint32_t *>(sums), ptrs);
     else
         k_sums<double><<<n, BLOCK, 0, st>>>(reinterpret_cast<const double *>(pics), src, begins,
-                                            n_rois, slice, reinterpret_cast<double *>(sums));
+                                            n_rois, slice, reinterpret_cast<double *>(sums), ptrs);
     return cudaGetLastError();
 }
 
 cudaError_t run_prepare(const void *pics, int in_type, bool dbl, void *out, const void *hann,
                         const void *sums, const uint2 *begins, size2 src, size2 slice,
-                        size2 out_size, uint32_t n_rois, uint32_t batch, cudaStream_t st)
+                        size2 out_size, uint32_t n_rois, uint32_t batch, cudaStream_t st,
+                        const void *const *ptrs)
 {
     const uint32_t n = n_rois * batch;
     const uint32_t grid = grid_for((uint64_t)n * slice.x * slice.y);
@@ -389,7 +397,7 @@ cudaError_t run_prepare(const void *pics, int in_type, bool dbl, void *out, cons
     k_prepare<IN, T><<<grid, BLOCK, 0, st>>>(                                                   \
         reinterpret_cast<const IN *>(pics), reinterpret_cast<T *>(out),                         \
         reinterpret_cast<const T *>(hann), reinterpret_cast<const sum_of<IN>::type *>(sums),    \
-        begins, src, slice, out_size, n_rois, n)
+        begins, src, slice, out_size, n_rois, n, ptrs)
     if (in_type == IN_U16) {
         if (dbl) EMIDA_PREP(uint16_t, double);
         else EMIDA_PREP(uint16_t, float);
@@ -513,17 +521,19 @@ cudaError_t run_extract_neighbors(const void *maps, const void *maxes, void *nei
 
 cudaError_t run_fit(const void *neigh, const void *maxes, uint32_t n, int s, size2 cross,
                     int policy, const double *lstsq, bool dbl, double *offsets, double *coefs,
-                    cudaStream_t st)
+                    cudaStream_t st, const uint32_t *out_base, uint32_t n_rois, void *maxes_out)
 {
     if (n == 0) return cudaSuccess;
     if (dbl)
         k_fit<double><<<grid_for(n), BLOCK, 0, st>>>(
             reinterpret_cast<const double *>(neigh), reinterpret_cast<const data_index<double> *>(maxes),
-            n, s, cross, policy, lstsq, offsets, coefs);
+            n, s, cross, policy, lstsq, offsets, coefs, out_base, n_rois,
+            reinterpret_cast<data_index<double> *>(maxes_out));
     else
         k_fit<float><<<grid_for(n), BLOCK, 0, st>>>(
             reinterpret_cast<const float *>(neigh), reinterpret_cast<const data_index<float> *>(maxes),
-            n, s, cross, policy, lstsq, offsets, coefs);
+            n, s, cross, policy, lstsq, offsets, coefs, out_base, n_rois,
+            reinterpret_cast<data_index<float> *>(maxes_out));
     return cudaGetLastError();
 }
 

@@ -13,14 +13,18 @@ enum in_type_t : int32_t { IN_U16 = 0, IN_F64 = 1 };
 
 // src/sum.cu:109-167: sums[pair] over the ROI, pair = pattern * n_rois + roi.
 // u16 input sums into uint32 (wrapping like the reference), f64 into double.
+// With `ptrs` (a device table of pattern addresses), pattern p is ptrs[p]
+// instead of pics + p * src.x * src.y.
 cudaError_t run_sums(const void *pics, int in_type, size2 src, const uint2 *begins,
-                     uint32_t n_rois, size2 slice, uint32_t batch, void *sums, cudaStream_t st);
+                     uint32_t n_rois, size2 slice, uint32_t batch, void *sums, cudaStream_t st,
+                     const void *const *ptrs = nullptr);
 
 // src/prepare_pics.cu:11-63: out[pair][y*out.x + x] = (p - sum/area) * hx[x] * hy[y].
 // hann holds slice.x x-window values followed by slice.y y-window values.
 cudaError_t run_prepare(const void *pics, int in_type, bool dbl, void *out, const void *hann,
                         const void *sums, const uint2 *begins, size2 src, size2 slice,
-                        size2 out_size, uint32_t n_rois, uint32_t batch, cudaStream_t st);
+                        size2 out_size, uint32_t n_rois, uint32_t batch, cudaStream_t st,
+                        const void *const *ptrs = nullptr);
 
 // src/cross_corr.cu:11-74: brute-force lags, y-outer / x-inner sums with
 // separately rounded products and sums (same bits as the FP64 oracle).
@@ -53,10 +57,14 @@ cudaError_t run_extract_neighbors(const void *maps, const void *maxes, void *nei
                                   size2 cross, uint32_t n, int policy, bool dbl, cudaStream_t st);
 
 // On-device FP64 fit and finalisation (src/subpixel_max.hpp:76-97,
-// src/gpu_offset.hpp:289-298).  coefs may be null.
+// src/gpu_offset.hpp:289-298).  coefs may be null.  With `out_base` (device,
+// one entry per pattern of n_rois pairs) pair i lands in output slot
+// out_base[i / n_rois] + i % n_rois, and its maximum is copied to
+// maxes_out[slot] when maxes_out is given.
 cudaError_t run_fit(const void *neigh, const void *maxes, uint32_t n, int s, size2 cross,
                     int policy, const double *lstsq, bool dbl, double *offsets, double *coefs,
-                    cudaStream_t st);
+                    cudaStream_t st, const uint32_t *out_base = nullptr, uint32_t n_rois = 1,
+                    void *maxes_out = nullptr);
 
 // Reference spectra from cuFFT layout [S][h2][w2/2+1] to the fused kernel's
 // column-major layout [S][w2/2+1][h2].
