@@ -274,7 +274,7 @@ int emida_gb::host::run_fused(emida_gb_handle *h, const void *pics, uint32_t pat
             const cuuint64_t dims[3] = {h->src.x, h->src.y, pats};
             const cuuint64_t strides[2] = {(cuuint64_t)h->src.x * 2,
                                            (cuuint64_t)h->src.x * h->src.y * 2};
-            const cuuint32_t box[3] = {(h->slice.x + 14) & ~7u, h->slice.y, 1};
+            const cuuint32_t box[3] = {(h->slice.x + 14) & ~7u, fused_box_rows(h->w2, h->slice.y), 1};
             const cuuint32_t estr[3] = {1, 1, 1};
             if (enc(&map, CU_TENSOR_MAP_DATA_TYPE_UINT16, 3, const_cast<void *>(pics), dims,
                     strides, box, estr, CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_NONE,
@@ -499,12 +499,13 @@ int emida_gb_create(const emida_gb_params *p, emida_gb_handle **out)
     // The fused kernel takes square ROIs up to 96 pixels (64 in FP64); a ROI
     // whose 2*side is not one of its transform lengths is zero-padded into the
     // next one, which leaves every lag of the 2*side-1 window unchanged.
-    const uint32_t fn = h->fft ? fused_size_for(p->slice_w, h->dbl) : 0;
+    const uint32_t fn = h->fft ? fused_size_for(p->slice_w, h->dbl, h->in_f64) : 0;
     const bool fusable = fn != 0;
     if (p->mode == EMIDA_GB_MODE_FUSED && !fusable) {
         delete h;
         return fail(EMIDA_GB_UNSUPPORTED,
-                    "no fused kernel for this shape (FFT policy, ROI side <= 96 in FP32, <= 64 in FP64)");
+                    "no fused kernel for this shape (FFT policy; ROI side <= 64 in FP64, <= 96 in FP32, "
+                    "<= 128 in FP32 with uint16 input)");
     }
     h->mode = (p->mode == EMIDA_GB_MODE_PLAIN || !fusable) ? EMIDA_GB_MODE_PLAIN : EMIDA_GB_MODE_FUSED;
     if (p->mode == EMIDA_GB_MODE_TENSOR) h->mode = EMIDA_GB_MODE_TENSOR;

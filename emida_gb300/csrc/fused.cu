@@ -14,6 +14,7 @@
 // swizzled by row so that column and row accesses of the 8-lane FFT groups
 // spread over all banks.  The uint16 ROI tile is staged by TMA into the
 // spectrum's upper half, which is unused until the column pass.
+#include <cooperative_groups.h>
 #include <cuda.h>
 
 #include "device_fit.cuh"
@@ -498,6 +499,383 @@ __global__ void __launch_bounds__(N * G / 4, fused_min_blocks(N, sizeof(T)))
     }
 }
 
+
+// ---- 256-point transforms on a cluster of two CTAs ---------------------------
+// An FP32 256 x 128 half spectrum is 256 KB, more than one CTA's shared memory.
+// The two CTAs of a cluster split it by slots -- CTA r holds slots 64r..64r+63
+// of every spectrum row -- and exchange through distributed shared memory:
+//   sums          each CTA sums its half of the ROI rows; the partial sums cross;
+//   row pass      CTA r transforms ROI rows 64r..64r+63 (TMA box of 64 rows) and
+//                 writes every output slot into the CTA that owns it;
+//   column pass   local: forward FFT, conj product, inverse FFT of its 64 columns;
+//   inverse rows  CTA r produces map rows 128r..128r+127, reading the partner's
+//                 64 slots of each row; the real map goes back over the same
+//                 slots (map columns x < 128 in CTA 0, x >= 128 in CTA 1);
+//   peak, fit     CTA 0 merges both maxima, reads the neighbourhood from either
+//                 CTA and runs the batched FP64 fit.
+// Every thread of both CTAs passes the same cluster barriers in every pair and
+// none leaves the loop early, so a barrier cannot wait on a missing CTA; a TMA
+// wait that runs out only flags the error.
+namespace cl {
+
+constexpr int N = 256, G = 16, E = N / G, H = N / 2;
+constexpr int SLOTS = N / 4;        // slots of each spectrum row held per CTA
+constexpr int GROUPS = 16, THREADS = GROUPS * G, WARPS = THREADS / 32;
+constexpr int ROWS = H / 2;         // ROI rows staged per CTA
+
+template <typename C> __device__ __forceinline__ C *csp(C *S, int row, int slot)
+{
+    // XOR by the row's low 4 bits: a 16-lane group's column access (rows t + 16m)
+    // and row access (16 consecutive slots) both hit 16 distinct bank pairs
+    return S + row * SLOTS + (slot ^ (row & 15));
+}
+
+constexpr size_t up(size_t v, size_t a) { return (v + a - 1) / a * a; }
+
+struct layout {
+    static constexpr size_t spectrum = 0;                               // N x SLOTS float2
+    static constexpr size_t xch = spectrum + (size_t)N * SLOTS * 8;     // GROUPS x N float2
+    static constexpr size_t tw_fwd = xch + (size_t)GROUPS * N * 8;
+    static constexpr size_t tw_inv = tw_fwd + (size_t)N * 8;
+    static constexpr size_t hann = tw_inv + (size_t)N * 8;              // hx[side], hy[side]
+    static constexpr size_t red_val = hann + (size_t)N * 4;
+    static constexpr size_t red_idx = red_val + 32 * 4;
+    static constexpr size_t psum = red_idx + 32 * 4;                    // partial sums [2]
+    static constexpr size_t pbest_v = psum + 16;                        // CTA maxima [2]
+    static constexpr size_t pbest_i = pbest_v + 16;
+    static constexpr size_t barrier = pbest_i + 16;
+    static constexpr size_t fit_vals = barrier + 16;
+    static constexpr size_t fit_meta = fit_vals + 32 * 81 * 4;
+    static constexpr size_t fit_peak = fit_meta + 32 * 4 * 4;
+    static constexpr size_t tile = up(fit_peak + 32 * 4, 128);
+    static constexpr size_t bytes = tile + (size_t)ROWS * (H + 8) * 2;
+};
+static_assert(layout::bytes <= 227 * 1024, "cluster layout must fit one CTA's shared memory");
+
+}  // namespace cl
+
+__global__ void __cluster_dims__(2, 1, 1) __launch_bounds__(cl::THREADS, 1)
+    fused_cluster_kernel(const fused_args a, const __grid_constant__ CUtensorMap tmap)
+{
+    namespace cg = cooperative_groups;
+    using namespace cl;
+    using T = float;
+    using C = cplx<T>;
+    using L = cl::layout;
+    cg::cluster_group cluster = cg::this_cluster();
+    const int rank = (int)cluster.block_rank(), peer = rank ^ 1;
+    const uint32_t clusters = gridDim.x / 2, cid = blockIdx.x / 2;
+    const int side = a.side;
+    const int TW = (side + 14) & ~7;
+
+    extern __shared__ __align__(1024) unsigned char smem[];
+    C *S = reinterpret_cast<C *>(smem + L::spectrum);
+    C *Sp = cluster.map_shared_rank(S, peer);
+    C *X = reinterpret_cast<C *>(smem + L::xch);
+    C *twf = reinterpret_cast<C *>(smem + L::tw_fwd);
+    C *twi = reinterpret_cast<C *>(smem + L::tw_inv);
+    T *hx = reinterpret_cast<T *>(smem + L::hann);
+    T *hy = hx + side;
+    T *red_v = reinterpret_cast<T *>(smem + L::red_val);
+    uint32_t *red_i = reinterpret_cast<uint32_t *>(smem + L::red_idx);
+    uint32_t *psum = reinterpret_cast<uint32_t *>(smem + L::psum);
+    uint32_t *psum_p = cluster.map_shared_rank(psum, peer);
+    T *pbest_v = reinterpret_cast<T *>(smem + L::pbest_v);
+    uint32_t *pbest_i = reinterpret_cast<uint32_t *>(smem + L::pbest_i);
+    uint64_t *bar = reinterpret_cast<uint64_t *>(smem + L::barrier);
+    T *fbuf = reinterpret_cast<T *>(smem + L::fit_vals);
+    uint32_t *fmeta = reinterpret_cast<uint32_t *>(smem + L::fit_meta);
+    T *fval = reinterpret_cast<T *>(smem + L::fit_peak);
+    uint16_t *t16 = reinterpret_cast<uint16_t *>(smem + L::tile);
+
+    const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
+    const int t = lane & (G - 1), g = tid / G;
+    C *xg = X + g * N;  // this group's exchange line
+    struct xline {
+        C *p;
+        __device__ __forceinline__ C *operator()(int q) const { return p + q; }
+    };
+    const xline xl{xg};
+    // owner of slot k (0..127) of a spectrum row
+    auto owner = [&](int k) -> C * { return (k >> 6) == rank ? S : Sp; };
+
+    const C *gtw = reinterpret_cast<const C *>(a.twiddles);
+    for (int i = tid; i < G * E; i += THREADS) {
+        const C w = gtw[(i % G) * (i / G)];
+        twf[i] = w;
+        twi[i] = cconj(w);
+    }
+    const T *ghann = reinterpret_cast<const T *>(a.hann);
+    for (int i = tid; i < 2 * side; i += THREADS) hx[i] = ghann[i];
+    const bool tma = a.stage == STAGE_TMA;
+    if (tid == 0) {
+        mbar_init(bar, 1);
+        fence_proxy_async();
+    }
+    __syncthreads();
+
+    auto item = [&](uint32_t pair) -> uint4 {
+        if (a.items) return a.items[pair];
+        return make_uint4(pair / a.n_rois, pair % a.n_rois, pair, (uint32_t)a.fitsize);
+    };
+    auto pattern_base = [&](uint32_t pic) -> const uint16_t * {
+        if (a.pattern_ptrs) return reinterpret_cast<const uint16_t *>(a.pattern_ptrs[pic]);
+        return reinterpret_cast<const uint16_t *>(a.pics) + (size_t)pic * a.src_w * a.src_h;
+    };
+    auto issue_tile = [&](uint32_t pair) {
+        const uint4 it = item(pair);
+        const uint2 b = a.begins[it.y];
+        fence_proxy_async();
+        mbar_expect_tx(bar, TW * ROWS * 2);
+        tma_load_3d(t16, &tmap, (int)(b.x & ~7u), (int)b.y + ROWS * rank, (int)it.x, bar);
+    };
+    if (tma && tid == 0 && cid < a.n_pairs) issue_tile(cid);
+
+    uint32_t iter = 0;
+    for (uint32_t pair = cid; pair < a.n_pairs; pair += clusters, ++iter) {
+        const uint4 it = item(pair);
+        const uint32_t pic = it.x, roi = it.y, out = it.z;
+        const int s = (int)it.w, s2 = s * s;
+        const uint2 beg = a.begins[roi];
+        const int xo = (int)(beg.x & 7u);
+        const int r0 = ROWS * rank;                      // first ROI row of this CTA
+        const int nrows = max(0, min(ROWS, side - r0));  // live ROI rows of this CTA
+
+        // ---- this CTA's half of the ROI, its partial sum -------------------
+        if (tma) {
+            if (!mbar_wait(bar, iter & 1) && tid == 0) atomicOr(a.err, DEV_ERR_TMA_TIMEOUT);
+        } else {
+            const uint16_t *src = pattern_base(pic) + (size_t)(beg.y + r0) * a.src_w + beg.x;
+            for (int i = tid; i < nrows * side; i += THREADS)
+                t16[(i / side) * TW + xo + (i % side)] = src[(size_t)(i / side) * a.src_w + (i % side)];
+            __syncthreads();
+        }
+        uint32_t acc = 0;
+        for (int i = tid; i < nrows * side; i += THREADS) acc += t16[(i / side) * TW + xo + (i % side)];
+#pragma unroll
+        for (int o = 16; o; o >>= 1) acc += __shfl_xor_sync(0xffffffffu, acc, o);
+        if (lane == 0) red_i[warp] = acc;
+        __syncthreads();
+        if (tid == 0) {
+            uint32_t part = 0;
+            for (int w = 0; w < WARPS; ++w) part += red_i[w];
+            psum[rank] = part;
+            psum_p[rank] = part;
+        }
+        // B0: both partial sums are in place, and the previous pair's reads of
+        // the partner's map are finished
+        cluster.sync();
+        const T mean = (T)(psum[0] + psum[1]) / (T)(side * side);
+
+        // ---- forward rows: pairs of real rows as one complex FFT -----------
+#pragma unroll 1
+        for (int rnd = 0; rnd < ROWS / 2 / GROUPS; ++rnd) {
+            const int rl = 2 * (g + GROUPS * rnd), ra = r0 + rl, rb = ra + 1;
+            const bool live = ra < side;
+            C v[E];
+#pragma unroll
+            for (int m = 0; m < E / 2; ++m) {
+                const int x = t + G * m;
+                T pa = (T)0, pb = (T)0;
+                if (live && x < side) {
+                    pa = ((T)t16[rl * TW + xo + x] - mean) * hx[x] * hy[ra];
+                    pb = ((T)t16[(rl + 1) * TW + xo + x] - mean) * hx[x] * hy[rb];
+                }
+                v[m] = cmake<C>(pa, pb);
+            }
+            group_fft<N, -1, true, T, G>(v, t, xl, twf);
+            const int partner = (lane & ~(G - 1)) | ((G - t) & (G - 1));
+#pragma unroll
+            for (int j = 0; j < E / 2; ++j) {
+                C send = (t == 0) ? v[j == 0 ? 0 : E - j] : v[E - 1 - j];
+                C zm = cmake<C>(__shfl_sync(0xffffffffu, send.x, partner),
+                                __shfl_sync(0xffffffffu, send.y, partner));
+                C z = v[j];
+                const int k = t + G * j;
+                C *D = owner(k);
+                if (k == 0) {
+                    C zh = v[E / 2];
+                    *csp(D, ra, 0) = cmake<C>(z.x, zh.x);
+                    *csp(D, rb, 0) = cmake<C>(z.y, zh.y);
+                } else {
+                    *csp(D, ra, k & 63) = cmake<C>((z.x + zm.x) * (T)0.5, (z.y - zm.y) * (T)0.5);
+                    *csp(D, rb, k & 63) = cmake<C>((z.y + zm.y) * (T)0.5, (zm.x - z.x) * (T)0.5);
+                }
+            }
+        }
+        __syncthreads();
+        if (tma && tid == 0 && pair + clusters < a.n_pairs) issue_tile(pair + clusters);
+        cluster.sync();  // B1: every spectrum row is complete in both CTAs
+
+        // ---- columns: forward FFT, conj product, inverse FFT (local) -------
+        const C *R = reinterpret_cast<const C *>(a.ref_spec) + (size_t)roi * (H + 1) * N;
+#pragma unroll 1
+        for (int rnd = 0; rnd < SLOTS / GROUPS; ++rnd) {
+            const int c = g + rnd * GROUPS, kx = SLOTS * rank + c;
+            C v[E];
+#pragma unroll
+            for (int m = 0; m < E / 2; ++m) v[m] = *csp(S, t + G * m, c);
+            struct cline {
+                C *S;
+                int c;
+                __device__ __forceinline__ C *operator()(int q) const { return csp(S, q, c); }
+            } line{S, c};
+            group_fft<N, -1, true, T, G>(v, t, line, twf);
+            const C *Rc = R + (size_t)kx * N;
+            if (rank == 0 && warp == 0 && rnd == 0) {
+                // column 0 packs the DC and Nyquist columns (see the one-CTA kernel)
+#pragma unroll
+                for (int j = 0; j < E; ++j) *csp(S, t + G * j, c) = v[j];
+                __syncwarp();
+#pragma unroll
+                for (int j = 0; j < E; ++j) {
+                    const int ky = t + G * j;
+                    if (c == 0) {
+                        C x = v[j];
+                        C xm = *csp(S, ky == 0 ? 0 : N - ky, 0);
+                        C p0 = cmake<C>((x.x + xm.x) * (T)0.5, (x.y - xm.y) * (T)0.5);
+                        C pn = cmake<C>((x.y + xm.y) * (T)0.5, (xm.x - x.x) * (T)0.5);
+                        C q0 = cmulc(p0, __ldg(R + ky));
+                        C qn = cmulc(pn, __ldg(R + (size_t)H * N + ky));
+                        v[j] = cmake<C>(q0.x - qn.y, q0.y + qn.x);
+                    } else {
+                        v[j] = cmulc(v[j], __ldg(Rc + ky));
+                    }
+                }
+                __syncwarp();
+            } else {
+#pragma unroll
+                for (int j = 0; j < E; ++j) v[j] = cmulc(v[j], __ldg(Rc + t + G * j));
+            }
+            group_fft<N, +1, false, T, G>(v, t, line, twi);
+#pragma unroll
+            for (int j = 0; j < E; ++j) *csp(S, t + G * j, c) = v[j];
+        }
+        cluster.sync();  // B2: every column is back in the spectrum
+
+        // ---- inverse rows 128r..128r+127: two Hermitian rows per FFT -------
+        T bv = neg_inf<T>();
+        uint32_t bi = 0xffffffffu;
+#pragma unroll 1
+        for (int rnd = 0; rnd < H / 2 / GROUPS; ++rnd) {
+            const int ra = H * rank + 2 * (g + GROUPS * rnd), rb = ra + 1;
+            C v[E];
+#pragma unroll
+            for (int j = 0; j < E; ++j) {
+                const int n = t + G * j;
+                if (j < E / 2) {
+                    C *D = owner(n);
+                    C ga = *csp(D, ra, n & 63), gb = *csp(D, rb, n & 63);
+                    v[j] = (n == 0) ? cmake<C>(ga.x, gb.x) : cmake<C>(ga.x - gb.y, ga.y + gb.x);
+                } else {
+                    const int k = (n == H) ? 0 : N - n;
+                    C *D = owner(k);
+                    C ga = *csp(D, ra, k & 63), gb = *csp(D, rb, k & 63);
+                    v[j] = (n == H) ? cmake<C>(ga.y, gb.y) : cmake<C>(ga.x + gb.y, gb.x - ga.y);
+                }
+            }
+            group_fft<N, +1, false, T, G>(v, t, xl, twi);
+#pragma unroll
+            for (int j = 0; j < E; ++j) {
+                const int x = t + G * j, q = x >> 1;
+                reinterpret_cast<T *>(csp(owner(q), ra, q & 63))[x & 1] = v[j].x;
+                if (v[j].x > bv) {
+                    bv = v[j].x;
+                    bi = (uint32_t)(ra * N + x);
+                }
+            }
+#pragma unroll
+            for (int j = 0; j < E; ++j) {
+                const int x = t + G * j, q = x >> 1;
+                reinterpret_cast<T *>(csp(owner(q), rb, q & 63))[x & 1] = v[j].y;
+                if (v[j].y > bv) {
+                    bv = v[j].y;
+                    bi = (uint32_t)(rb * N + x);
+                }
+            }
+        }
+#pragma unroll
+        for (int o = 16; o; o >>= 1) {
+            T ov = __shfl_xor_sync(0xffffffffu, bv, o);
+            uint32_t oi = __shfl_xor_sync(0xffffffffu, bi, o);
+            better(bv, bi, ov, oi);
+        }
+        if (lane == 0) {
+            red_v[warp] = bv;
+            red_i[warp] = bi;
+        }
+        __syncthreads();
+        if (tid == 0) {
+            T cv = red_v[0];
+            uint32_t ci = red_i[0];
+            for (int w = 1; w < WARPS; ++w) better(cv, ci, red_v[w], red_i[w]);
+            // both CTAs' maxima meet in CTA 0
+            *cluster.map_shared_rank(pbest_v + rank, 0) = cv;
+            *cluster.map_shared_rank(pbest_i + rank, 0) = ci;
+        }
+        cluster.sync();  // B3: the map and both maxima are in place
+
+        // ---- neighbourhood and fit (CTA 0, warp 0) -------------------------
+        if (rank == 0 && warp == 0) {
+            T pv = pbest_v[0];
+            uint32_t pk = pbest_i[0];
+            better(pv, pk, pbest_v[1], pbest_i[1]);
+            if (pk >= (uint32_t)(N * N)) pk = 0;
+            uint32_t mx, my;
+            shift_pos(pk, POLICY_FFT, N - 1, N - 1, mx, my);
+            const uint32_t slot = iter & 31;
+            const T scale = (T)(4 * side * side) / (T)(N * N);
+            for (int l = lane; l < s2; l += 32) {
+                uint32_t x, y;
+                neighbour_pos(mx, my, l % s, l / s, s, N - 1, N - 1, x, y);
+                const uint32_t qm = (uint32_t)policy_index(POLICY_FFT, x, y, N - 1, N - 1);
+                const int qy = (int)(qm / N), qx = (int)(qm % N), q = qx >> 1;
+                T val = reinterpret_cast<T *>(csp(owner(q), qy, q & 63))[qx & 1];
+                if (2 * side != N) val *= scale;
+                fbuf[slot * 81 + l] = val;
+                if (a.neigh) reinterpret_cast<T *>(a.neigh)[(size_t)out * s2 + l] = val;
+            }
+            if (lane == 0) {
+                uint32_t pref = pk;
+                if (2 * side != N) {
+                    const int ns = 2 * side, c0 = N / 2 - 1;
+                    const int lx = (int)mx - c0, ly = (int)my - c0;
+                    pref = (uint32_t)(((ly % ns + ns) % ns) * ns + ((lx % ns + ns) % ns));
+                }
+                fmeta[4 * slot] = out;
+                fmeta[4 * slot + 1] = mx | (my << 16);
+                fmeta[4 * slot + 2] = pref | ((uint32_t)s << 24);
+                fval[slot] = 2 * side != N ? pv * scale : pv;
+            }
+            __syncwarp();
+            const bool last = pair + clusters >= a.n_pairs;
+            if (slot == 31 || last) fit_batch<T>(a, fbuf, fmeta, fval, (int)slot + 1, lane, N - 1);
+        }
+        __syncthreads();
+    }
+    // the partner may still read this CTA's shared memory: leave together
+    cluster.sync();
+}
+
+static cudaError_t launch_cluster(const fused_args &a, const CUtensorMap *tmap, int grid, cudaStream_t st)
+{
+    auto k = fused_cluster_kernel;
+    const size_t smem = cl::layout::bytes;
+    cudaError_t e = cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+    if (e != cudaSuccess) return e;
+    if (grid <= 0) {
+        int dev = 0, sms = 0;
+        cudaGetDevice(&dev);
+        cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+        grid = sms;  // one CTA per SM, two per cluster
+    }
+    grid &= ~1;
+    if ((uint32_t)grid > 2 * a.n_pairs) grid = (int)(2 * a.n_pairs);
+    if (grid < 2) return cudaSuccess;
+    k<<<grid, cl::THREADS, smem, st>>>(a, *tmap);
+    return cudaGetLastError();
+}
+
 template <int N, int G, typename T, typename IN>
 static cudaError_t launch_one(const fused_args &a, const CUtensorMap *tmap, int grid,
                               cudaStream_t st)
@@ -522,16 +900,22 @@ static cudaError_t launch_one(const fused_args &a, const CUtensorMap *tmap, int 
     return cudaGetLastError();
 }
 
-bool fused_supported(uint32_t fft_n, bool dbl)
+bool fused_supported(uint32_t fft_n, bool dbl, bool in_f64)
 {
-    return fft_n == 64 || fft_n == 96 || fft_n == 128 || (fft_n == 192 && !dbl);
+    return fft_n == 64 || fft_n == 96 || fft_n == 128 || (fft_n == 192 && !dbl) ||
+           (fft_n == 256 && !dbl && !in_f64);
 }
 
-uint32_t fused_size_for(uint32_t side, bool dbl)
+uint32_t fused_size_for(uint32_t side, bool dbl, bool in_f64)
 {
-    for (uint32_t n : {64u, 96u, 128u, 192u})
-        if (2 * side <= n && fused_supported(n, dbl)) return n;
+    for (uint32_t n : {64u, 96u, 128u, 192u, 256u})
+        if (2 * side <= n && fused_supported(n, dbl, in_f64)) return n;
     return 0;
+}
+
+uint32_t fused_box_rows(uint32_t fft_n, uint32_t side)
+{
+    return fft_n == 256 ? cl::ROWS : side;
 }
 
 template <int N, int G>
@@ -548,7 +932,8 @@ static cudaError_t launch_n(bool dbl, bool in_f64, const fused_args &a, const CU
 cudaError_t launch_fused(uint32_t fft_n, bool dbl, bool in_f64, const fused_args &a,
                          const CUtensorMap *tmap, int grid, cudaStream_t st)
 {
-    if (!fused_supported(fft_n, dbl)) return cudaErrorInvalidValue;
+    if (!fused_supported(fft_n, dbl, in_f64)) return cudaErrorInvalidValue;
+    if (fft_n == 256) return launch_cluster(a, tmap, grid, st);
     switch (fft_n) {
     case 64: return launch_n<64, 8>(dbl, in_f64, a, tmap, grid, st);
     case 96: return launch_n<96, 4>(dbl, in_f64, a, tmap, grid, st);

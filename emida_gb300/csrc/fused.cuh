@@ -50,10 +50,14 @@ __host__ __device__ inline int lstsq_offset(int s)
     return s == 3 ? 0 : s == 5 ? 54 : s == 7 ? 204 : 498;
 }
 
-// Transform sizes with a fused kernel: 64, 96, 128 and, in FP32, 192.
-bool fused_supported(uint32_t fft_n, bool dbl);
+// Transform sizes with a fused kernel: 64, 96, 128 and, in FP32, 192 and 256
+// (256 on a cluster of two CTAs, uint16 input only).
+bool fused_supported(uint32_t fft_n, bool dbl, bool in_f64 = false);
 // The smallest fused transform that holds a zero-padded ROI of this side (0: none).
-uint32_t fused_size_for(uint32_t side, bool dbl);
+uint32_t fused_size_for(uint32_t side, bool dbl, bool in_f64 = false);
+// Rows of the TMA box a CTA stages per ROI (the 256-point kernel's CTAs each
+// stage half of the ROI).
+uint32_t fused_box_rows(uint32_t fft_n, uint32_t side);
 
 // grid <= 0: one wave of resident CTAs (occupancy x SM count).
 cudaError_t launch_fused(uint32_t fft_n, bool dbl, bool in_f64, const fused_args &a,

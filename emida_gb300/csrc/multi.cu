@@ -272,7 +272,7 @@ int launch_plan(emida_gb_multi *m, const plan &pl, const work_set &ws, const voi
             const uint32_t side = k.side;
             const cuuint64_t dims[3] = {m->src_w, m->src_h, patterns};
             const cuuint64_t strides[2] = {(cuuint64_t)m->src_w * 2, (cuuint64_t)m->src_w * m->src_h * 2};
-            const cuuint32_t box[3] = {(side + 14) & ~7u, side, 1};
+            const cuuint32_t box[3] = {(side + 14) & ~7u, fused_box_rows(k.n, side), 1};
             const cuuint32_t estr[3] = {1, 1, 1};
             if (get_encoder()(&map, CU_TENSOR_MAP_DATA_TYPE_UINT16, 3, const_cast<void *>(pics), dims,
                               strides, box, estr, CU_TENSOR_MAP_INTERLEAVE_NONE,

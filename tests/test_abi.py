@@ -91,15 +91,19 @@ def test_no_cpu_fallback_when_library_missing(tmp_path, monkeypatch):
 
 
 def test_fused_form_availability(lib):
-    # FP64 192-point spectra do not fit in shared memory and no fused
-    # transform holds a 100-pixel ROI: the fused form is refused explicitly,
-    # "auto" takes the staged form there (a GPU path)
+    # FP64 192-point spectra do not fit in shared memory, the 256-point
+    # cluster kernel takes uint16 FP32 input only, and no fused transform
+    # holds a 130-pixel ROI: the fused form is refused explicitly, "auto"
+    # takes the staged form there (a GPU path)
     from emida_gb300 import EmidaError, GpuOffset
     with pytest.raises(EmidaError, match="no fused kernel"):
         GpuOffset((256, 256), [(0, 0)], (96, 96), (191, 191), 1, "fft", 3, 1, "double",
                   mode="fused")
     with pytest.raises(EmidaError, match="no fused kernel"):
         GpuOffset((256, 256), [(0, 0)], (100, 100), (199, 199), 1, "fft", 3, 1, "float",
+                  np.float64, mode="fused")
+    with pytest.raises(EmidaError, match="no fused kernel"):
+        GpuOffset((256, 256), [(0, 0)], (130, 130), (259, 259), 1, "fft", 3, 1, "float",
                   mode="fused")
 
 

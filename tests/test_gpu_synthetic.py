@@ -139,6 +139,36 @@ def test_fused_zero_padded_sides(data512, side, precision, tol):
     assert np.array_equal(p[2], o_peaks)
 
 
+@pytest.mark.parametrize("side", [128, 100, 116])
+def test_fused_256_point_cluster_kernel(data512, side):
+    # ROI sides 98..128 (FP32, uint16) run 256-point transforms on a cluster of
+    # two CTAs that split the half spectrum; 100 and 116 are zero-padded
+    from emida_gb300 import synth
+    ref, pics = data512
+    _, begins = synth.roi_grid(512, 3, side // 2, margin=side // 2 + 8)
+    offs, coefs, peaks = run(ref, pics[:3], begins, side, "fft", 5, "float", "fused")
+    o_offs, o_coefs, o_peaks = oracle(ref, pics[:3], begins, side, "fft", 5)
+    assert np.array_equal(peaks, o_peaks)
+    assert_offsets(offs, coefs, o_offs, o_coefs, 5, 1e-3)
+    p = run(ref, pics[:3], begins, side, "fft", 5, "float", "plain")
+    assert np.array_equal(p[2], o_peaks)
+
+
+def test_fused_256_many_pairs_and_border_rois(data512):
+    # more pairs than clusters (each cluster walks several), ROIs at the
+    # borders, x not a multiple of 8, and a repeat that must give the same bits
+    ref, pics = data512
+    begins = np.array([(0, 0), (384, 0), (0, 384), (384, 384), (3, 5), (201, 77), (383, 13)] * 4,
+                      dtype=np.uint32)
+    f = run(ref, pics, begins, 128, "fft", 3, "float", "fused")
+    g = run(ref, pics, begins, 128, "fft", 3, "float", "fused")
+    assert all(np.array_equal(x, y) for x, y in zip(f, g))
+    o = oracle(ref, pics, begins[:7], 128, "fft", 3)
+    per = len(begins)
+    for p in range(len(pics)):
+        assert np.array_equal(f[2][p * per:p * per + 7], o[2][p * 7:(p + 1) * 7])
+
+
 def test_fused_equals_plain_peaks_and_border_rois(data512):
     # ROIs touching every border and with x not a multiple of 8 (TMA x rounding)
     ref, pics = data512
