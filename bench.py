@@ -576,6 +576,22 @@ def main():
     sm_max = 2070.0
     fp32_peak = 152 * 128 * 2 * sm_max * 1e6 / 1e12
 
+    # the deformation fit after the path (python/process_offsets.py:83-104) on
+    # this job's offsets, with the fit-quality mask: one projective map per pattern
+    mids = (np.asarray(begins, dtype=np.float64) + 32.0)
+    d_mids = DeviceBuffer.from_array(np.ascontiguousarray(mids))
+    d_f = DeviceBuffer(P * 9 * 8)
+    centre = (ctypes.c_double * 3)(512.0, 512.0, 512.0)
+    g.run_device(d_pics, P, d_offs, d_coefs)
+    _lib.call("emida_gb_synchronize")
+    fit_args = (d_mids.ptr, d_offs.ptr, S, P, centre, d_coefs.ptr, 1e-6, d_f.ptr)
+    _lib.call("emida_gb_time_fit_homography", *fit_args, 2, ctypes.byref(ctypes.c_float()))
+    fit_ms = ctypes.c_float()
+    _lib.call("emida_gb_time_fit_homography", *fit_args, 10, ctypes.byref(fit_ms))
+    deformation = {"patterns_per_s": P / (fit_ms.value / 10 / 1000.0), "ms_per_step": fit_ms.value / 10,
+                   "what": "per pattern a 3x3 projective map from its 100 ROI offsets "
+                           "(FP64 one-sided Jacobi SVD of the 200 x 9 system, one warp per pattern)"}
+
     # plain form on the same data for the fused-vs-plain ratio
     plain = None
     if args.mode == "fused" and not args.no_plain:
@@ -667,6 +683,7 @@ def main():
                         "frac": flop / (ms_step / 1000.0) / 1e12 / fp32_peak,
                         "flop_per_pair": flop // pairs_per_step},
             "plain": plain,
+            "deformation_fit": deformation,
             "cpu_baseline": cpu,
             "e2e": {"value": e2e_value, "unit": "ROI pairs/s",
                     "h2d_bytes_per_step": int(P * roi_rows(begins, 64) * 1024 * 2),

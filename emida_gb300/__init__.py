@@ -7,13 +7,13 @@ include/emida_gb.h); this package is its Python host side.
 from ._lib import EmidaError, LIB_PATH  # noqa: F401
 from .api import (  # noqa: F401
     CROSS_POLICY_BRUTE, CROSS_POLICY_FFT, DATA_INDEX_F32, DATA_INDEX_F64, DeviceBuffer,
-    GpuOffset, MultiLayout, Server, device_count, get_offset, lstsq_matrix, pinned_array,
-    subpixel_max,
+    GpuOffset, MultiLayout, Server, device_count, fit_homography, get_offset, lstsq_matrix,
+    pinned_array, subpixel_max,
 )
 
 __all__ = [
     "EmidaError", "GpuOffset", "MultiLayout", "Server", "get_offset", "DeviceBuffer", "device_count", "lstsq_matrix",
-    "subpixel_max", "pinned_array", "CROSS_POLICY_BRUTE", "CROSS_POLICY_FFT", "DATA_INDEX_F32",
+    "subpixel_max", "pinned_array", "fit_homography", "CROSS_POLICY_BRUTE", "CROSS_POLICY_FFT", "DATA_INDEX_F32",
     "DATA_INDEX_F64",
     "LIB_PATH",
 ]

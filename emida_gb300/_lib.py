@@ -90,6 +90,9 @@ SIGNATURES = {
     "emida_gb_lstsq_matrix": [_I32, _DP],
     "emida_gb_device_count": [ctypes.POINTER(_I32)],
     "emida_gb_set_device": [_I32],
+    "emida_gb_fit_homography": [_VP, _VP, _U32, _U32, _DP, _VP, ctypes.c_double, _VP, _VP],
+    "emida_gb_time_fit_homography": [_VP, _VP, _U32, _U32, _DP, _VP, ctypes.c_double, _VP, _I32,
+                                     ctypes.POINTER(ctypes.c_float)],
     "emida_gb_malloc": [ctypes.POINTER(_VP), _SZ],
     "emida_gb_free": [_VP],
     "emida_gb_memset": [_VP, _I32, _SZ],

@@ -484,3 +484,27 @@ class Server:
             self.close()
         except Exception:
             pass
+
+
+def fit_homography(mids, offsets, centre, coefs=None, min_det=1e-6):
+    """The deformation fit after the path (python/process_offsets.py:83-104),
+    batched on the GPU: per pattern, the 3x3 projective map carrying the ROI
+    centres `mids` ([S][2], x, y) to their displaced positions, from the
+    offsets ([P][S][2]) about `centre` = (cx, cy, z), divided by its [2][2]
+    entry.  With `coefs` ([P][S][6] fit coefficients of the path), ROIs whose
+    peak is not a clear maximum are left out as jove/analyze.py:44-56 does,
+    and a pattern with ten or fewer kept ROIs gives NaN.  Returns [P][3][3]."""
+    mids = np.ascontiguousarray(mids, dtype=np.float64).reshape(-1, 2)
+    n = len(mids)
+    offsets = np.ascontiguousarray(offsets, dtype=np.float64).reshape(-1, n, 2)
+    p = len(offsets)
+    d_mids, d_offs = DeviceBuffer.from_array(mids), DeviceBuffer.from_array(offsets)
+    d_coefs = None
+    if coefs is not None:
+        d_coefs = DeviceBuffer.from_array(np.ascontiguousarray(coefs, dtype=np.float64).reshape(p, n, 6))
+    d_out = DeviceBuffer(p * 9 * 8)
+    c = (ctypes.c_double * 3)(*[float(v) for v in centre])
+    _lib.call("emida_gb_fit_homography", d_mids.ptr, d_offs.ptr, n, p, c,
+              d_coefs.ptr if d_coefs is not None else None, float(min_det), d_out.ptr, None)
+    _lib.call("emida_gb_synchronize")
+    return d_out.download(np.float64, (p, 3, 3))

@@ -14,9 +14,10 @@ CSRC = os.path.join(HERE, "csrc")
 OBJ = os.path.join(HERE, "_build")
 LIB = os.path.join(HERE, "libemida_gb.so")
 CLI = os.path.join(HERE, "bin", "emida")
-SOURCES = ["fused.cu", "brute_tc.cu", "staged.cu", "capi.cu", "multi.cu", "server.cu"]
+SOURCES = ["fused.cu", "brute_tc.cu", "staged.cu", "capi.cu", "multi.cu", "server.cu",
+           "deformation.cu"]
 HEADERS = ["common.cuh", "fft.cuh", "device_fit.cuh", "fused.cuh", "staged.cuh", "handle.cuh",
-           "ptx.cuh", "brute_tc.cuh"]
+           "ptx.cuh", "brute_tc.cuh", "deformation.cuh"]
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 FLAGS = ["-O3", "-lineinfo", "-std=c++17", "-Xcompiler", "-fPIC", "-Xcompiler",
          "-ffp-contract=off", "-Xcompiler", "-O2", "--expt-relaxed-constexpr",

@@ -13,6 +13,7 @@
 #include <string>
 #include <vector>
 
+#include "deformation.cuh"
 #include "fft.cuh"
 #include "handle.cuh"
 
@@ -871,6 +872,48 @@ void emida_gb_destroy(emida_gb_handle *h)
 }
 
 // ---- memory helpers -----------------------------------------------------------
+// ---- deformation fit downstream of the path ----------------------------------
+static int check_homography(const double *mids, const double *offsets, uint32_t n_rois,
+                            const double *centre, double *out)
+{
+    if (!mids || !offsets || !centre || !out) return fail(EMIDA_GB_INVALID_ARGUMENT, "null argument");
+    if (n_rois < HOMOGRAPHY_MIN_ROIS || n_rois > HOMOGRAPHY_MAX_ROIS)
+        return fail(EMIDA_GB_INVALID_ARGUMENT, "the deformation fit takes %u..%u ROIs per pattern (got %u)",
+                    HOMOGRAPHY_MIN_ROIS, HOMOGRAPHY_MAX_ROIS, n_rois);
+    return EMIDA_GB_OK;
+}
+
+int emida_gb_fit_homography(const double *mids, const double *offsets, uint32_t n_rois,
+                            uint32_t patterns, const double *centre, const double *coefs,
+                            double min_det, double *out, void *stream)
+{
+    CKS(check_homography(mids, offsets, n_rois, centre, out));
+    CK(launch_homography(mids, offsets, n_rois, patterns, centre[0], centre[1], centre[2], coefs, min_det,
+                         out, (cudaStream_t)stream));
+    return EMIDA_GB_OK;
+}
+
+int emida_gb_time_fit_homography(const double *mids, const double *offsets, uint32_t n_rois,
+                                 uint32_t patterns, const double *centre, const double *coefs,
+                                 double min_det, double *out, int repeats, float *ms)
+{
+    CKS(check_homography(mids, offsets, n_rois, centre, out));
+    if (repeats < 1 || !ms) return fail(EMIDA_GB_INVALID_ARGUMENT, "repeats must be >= 1");
+    cudaEvent_t a, b;
+    CK(cudaEventCreate(&a));
+    CK(cudaEventCreate(&b));
+    CK(cudaEventRecord(a, 0));
+    for (int r = 0; r < repeats; ++r)
+        CK(launch_homography(mids, offsets, n_rois, patterns, centre[0], centre[1], centre[2], coefs,
+                             min_det, out, 0));
+    CK(cudaEventRecord(b, 0));
+    CK(cudaEventSynchronize(b));
+    CK(cudaEventElapsedTime(ms, a, b));
+    cudaEventDestroy(a);
+    cudaEventDestroy(b);
+    return EMIDA_GB_OK;
+}
+
 int emida_gb_set_device(int device)
 {
     CK(cudaSetDevice(device));

@@ -1,0 +1,141 @@
+// deformation.cu -- the step after the path: per pattern, the projective map
+// (the deformation gradient up to scale) that carries the ROI centres to their
+// displaced positions, as python/process_offsets.py:83-104 computes it.  The
+// 2S x 9 homogeneous system built from the ROI offsets is solved for the unit
+// vector minimising |A x|: the right singular vector of the smallest singular
+// value, reshaped to 3 x 3 and divided by its [2][2] entry.
+//
+// One warp per pattern.  The system sits in shared memory column by column and
+// a one-sided (Hestenes) Jacobi SVD in FP64 orthogonalises its nine columns by
+// plane rotations; the accumulated rotations are the right singular vectors
+// and the column norms the singular values.  Optionally a quality mask drops
+// ROIs whose fitted peak is not a clear maximum, as jove/analyze.py:44-56 does
+// (det of the negated quadratic's Hessian <= min_det), and a pattern with ten
+// or fewer good ROIs yields NaN.
+#include <cmath>
+
+#include "deformation.cuh"
+
+namespace emida_gb {
+namespace {
+
+constexpr int NC = 9;          // unknowns
+constexpr int MAX_SWEEPS = 40;
+
+__device__ __forceinline__ double warp_sum(double v)
+{
+#pragma unroll
+    for (int o = 16; o; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
+    return v;
+}
+
+__global__ void __launch_bounds__(32)
+    k_homography(const double *__restrict__ mids, const double *__restrict__ offsets, uint32_t n_rois,
+                 double cx, double cy, double cz, const double *__restrict__ coefs, double min_det,
+                 double *__restrict__ out)
+{
+    extern __shared__ double sm[];
+    const uint32_t rows = 2 * n_rois;
+    double *A = sm;                  // column j: A[j * rows + i]
+    double *V = sm + NC * rows;      // V[r * NC + c], starts as the identity
+    const int lane = threadIdx.x;
+    const uint32_t pat = blockIdx.x;
+    const double *off = offsets + (size_t)pat * n_rois * 2;
+    const double *q = coefs ? coefs + (size_t)pat * n_rois * 6 : nullptr;
+
+    // the system of process_offsets.py:85-99, masked rows left at zero
+    uint32_t kept = 0;
+    for (uint32_t r = lane; r < n_rois; r += 32) {
+        bool keep = true;
+        if (q) {
+            const double a = -q[6 * r + 3], b = -q[6 * r + 4] / 2, c = -q[6 * r + 5];
+            keep = a * c - b * b > min_det;
+        }
+        kept += keep;
+        const double a = mids[2 * r] - cx, b = mids[2 * r + 1] - cy, z = cz;
+        const double c = a + off[2 * r], d = b + off[2 * r + 1];
+        const double e0[NC] = {-a * z, -b * z, -z * z, 0, 0, 0, a * c, b * c, z * c};
+        const double e1[NC] = {0, 0, 0, -a * z, -b * z, -z * z, a * d, b * d, z * d};
+#pragma unroll
+        for (int j = 0; j < NC; ++j) {
+            A[j * rows + 2 * r] = keep ? e0[j] : 0.0;
+            A[j * rows + 2 * r + 1] = keep ? e1[j] : 0.0;
+        }
+    }
+    for (int i = lane; i < NC * NC; i += 32) V[i] = (i / NC == i % NC) ? 1.0 : 0.0;
+#pragma unroll
+    for (int o = 16; o; o >>= 1) kept += __shfl_xor_sync(0xffffffffu, kept, o);
+    __syncwarp();
+
+    // cyclic one-sided Jacobi sweeps
+    for (int sweep = 0; sweep < MAX_SWEEPS; ++sweep) {
+        bool rotated = false;
+        for (int p = 0; p < NC - 1; ++p) {
+            for (int r = p + 1; r < NC; ++r) {
+                double al = 0, be = 0, ga = 0;
+                for (uint32_t i = lane; i < rows; i += 32) {
+                    const double x = A[p * rows + i], y = A[r * rows + i];
+                    al += x * x;
+                    be += y * y;
+                    ga += x * y;
+                }
+                al = warp_sum(al);
+                be = warp_sum(be);
+                ga = warp_sum(ga);
+                if (al == 0.0 || be == 0.0 || fabs(ga) <= 1e-15 * sqrt(al * be)) continue;
+                rotated = true;
+                const double zeta = (be - al) / (2.0 * ga);
+                const double t = copysign(1.0, zeta) / (fabs(zeta) + sqrt(1.0 + zeta * zeta));
+                const double c = 1.0 / sqrt(1.0 + t * t), s = c * t;
+                for (uint32_t i = lane; i < rows; i += 32) {
+                    const double x = A[p * rows + i], y = A[r * rows + i];
+                    A[p * rows + i] = c * x - s * y;
+                    A[r * rows + i] = s * x + c * y;
+                }
+                if (lane < NC) {
+                    const double x = V[lane * NC + p], y = V[lane * NC + r];
+                    V[lane * NC + p] = c * x - s * y;
+                    V[lane * NC + r] = s * x + c * y;
+                }
+                __syncwarp();
+            }
+        }
+        if (!rotated) break;
+    }
+
+    // smallest singular value's column of V
+    int jmin = 0;
+    double smin = INFINITY;
+    for (int j = 0; j < NC; ++j) {
+        double n2 = 0;
+        for (uint32_t i = lane; i < rows; i += 32) n2 += A[j * rows + i] * A[j * rows + i];
+        n2 = warp_sum(n2);
+        if (n2 < smin) {
+            smin = n2;
+            jmin = j;
+        }
+    }
+    if (lane < NC) {
+        const bool enough = !coefs || kept > 10;
+        const double v = V[lane * NC + jmin], v22 = V[8 * NC + jmin];
+        out[(size_t)pat * NC + lane] = enough ? v / v22 : NAN;
+    }
+}
+
+}  // namespace
+
+size_t homography_smem(uint32_t n_rois) { return (size_t)(NC * 2 * n_rois + NC * NC) * sizeof(double); }
+
+cudaError_t launch_homography(const double *mids, const double *offsets, uint32_t n_rois,
+                              uint32_t patterns, double cx, double cy, double cz, const double *coefs,
+                              double min_det, double *out, cudaStream_t st)
+{
+    if (patterns == 0) return cudaSuccess;
+    const size_t smem = homography_smem(n_rois);
+    cudaError_t e = cudaFuncSetAttribute(k_homography, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+    if (e != cudaSuccess) return e;
+    k_homography<<<patterns, 32, smem, st>>>(mids, offsets, n_rois, cx, cy, cz, coefs, min_det, out);
+    return cudaGetLastError();
+}
+
+}  // namespace emida_gb

@@ -238,6 +238,25 @@ void emida_gb_server_destroy(emida_gb_server *s);
 
 /* ---- device memory helpers (for callers without a CUDA runtime binding) --- */
 int emida_gb_device_count(int *count);
+
+/* ---- the step after the path: deformation fit (python/process_offsets.py:83-104) ----
+ * Per pattern, the projective map that carries the ROI centres to their
+ * displaced positions, up to scale: the unit 9-vector minimising |A x| for the
+ * 2S x 9 system built from centres (x, y) about centre = {cx, cy, z} and the
+ * offsets, as a row-major 3x3 divided by its [2][2] entry.  mids [n_rois][2],
+ * offsets [patterns][n_rois][2] and out [patterns][9] in device (or pinned host)
+ * memory; 5 <= n_rois <= 1600.  coefs ([patterns][n_rois][6], the fit
+ * coefficients of the path) may be NULL; when given, ROIs whose peak is not a
+ * clear maximum (det of the negated quadratic <= min_det) are left out, and a
+ * pattern with ten or fewer kept ROIs gives NaN (jove/analyze.py:44-56).
+ * Queued on `stream` (NULL: the legacy stream), no synchronisation. */
+int emida_gb_fit_homography(const double *mids, const double *offsets, uint32_t n_rois,
+                            uint32_t patterns, const double *centre, const double *coefs,
+                            double min_det, double *out, void *stream);
+/* CUDA-event time of `repeats` fits (ms, all repeats together). */
+int emida_gb_time_fit_homography(const double *mids, const double *offsets, uint32_t n_rois,
+                                 uint32_t patterns, const double *centre, const double *coefs,
+                                 double min_det, double *out, int repeats, float *ms);
 /* Device for this thread's subsequent handles and helpers (one process per GPU). */
 int emida_gb_set_device(int device);
 int emida_gb_malloc(void **dev_ptr, size_t bytes);

@@ -220,3 +220,41 @@ def get_offsets(ref_pattern, pics, begins, slice_w, slice_h, policy=POLICY_FFT,
     if rc != 0:
         raise ValueError(f"oracle rejected the parameters (code {rc})")
     return offs, coefs, peaks
+
+
+def homography_system(mids, offsets, centre):
+    """The 2S x 9 homogeneous system of python/process_offsets.py:85-99 for one
+    pattern: ROI centres (x, y) about the pattern centre, their offsets, and the
+    centre's distance z; rows [-a z, -b z, -z^2, 0, 0, 0, a c, b c, z c] and
+    [0, 0, 0, -a z, -b z, -z^2, a d, b d, z d] with c = a + dx, d = b + dy."""
+    mids = np.asarray(mids, dtype=np.float64)
+    offsets = np.asarray(offsets, dtype=np.float64)
+    a = mids[:, 0] - centre[0]
+    b = mids[:, 1] - centre[1]
+    z = float(centre[2])
+    c = a + offsets[:, 0]
+    d = b + offsets[:, 1]
+    A = np.zeros((2 * len(mids), 9))
+    A[0::2, 0] = -a * z
+    A[0::2, 1] = -b * z
+    A[0::2, 2] = -z * z
+    A[1::2, 3] = -a * z
+    A[1::2, 4] = -b * z
+    A[1::2, 5] = -z * z
+    A[0::2, 6] = a * c
+    A[0::2, 7] = b * c
+    A[0::2, 8] = z * c
+    A[1::2, 6] = a * d
+    A[1::2, 7] = b * d
+    A[1::2, 8] = z * d
+    return A
+
+
+def homography_fit(mids, offsets, centre):
+    """python/process_offsets.py:83-104: the unit vector minimising |A x| (the
+    right singular vector of the smallest singular value, from scipy's SVD as
+    the reference calls it), as a 3x3 matrix divided by its [2, 2] entry."""
+    from scipy.linalg import svd
+    v = svd(homography_system(mids, offsets, centre))[2][8]
+    uu = v.reshape((3, 3))
+    return uu / uu[2, 2]

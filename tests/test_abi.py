@@ -122,3 +122,14 @@ def test_tensor_form_shape_limits(lib, kw):
     args.update(kw)
     with pytest.raises(EmidaError, match="tensor-core form"):
         GpuOffset(**args)
+
+
+def test_deformation_fit_roi_count_limits(lib):
+    # checked before any device work
+    import ctypes
+    from emida_gb300 import EmidaError, _lib
+    dummy = (ctypes.c_double * 4)()
+    centre = (ctypes.c_double * 3)(1.0, 1.0, 1.0)
+    for n in (4, 1601):
+        with pytest.raises(EmidaError, match="ROIs per pattern"):
+            _lib.call("emida_gb_fit_homography", dummy, dummy, n, 1, centre, None, 0.0, dummy, None)

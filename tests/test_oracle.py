@@ -207,3 +207,12 @@ def test_reference_lib_agrees_where_built():
         m = np.zeros(6 * s * s)
         assert ref.ref_lstsq_matrix(s, m.ctypes.data_as(ctypes.POINTER(ctypes.c_double))) == 0
         assert np.array_equal(m, eo.lstsq_matrix(s).ravel())
+
+
+def test_homography_fit_matches_reference_script():
+    # python/process_offsets.py run on seeded offsets (tests/golden/make_homography_golden.py)
+    from oracle import oracle as eo
+    g = np.load(os.path.join(GOLDEN, "homography_golden.npz"))
+    for off, uu in zip(g["offsets"], g["uu"]):
+        got = eo.homography_fit(g["mids"], off, g["centre"])
+        assert np.allclose(got, uu, rtol=1e-12, atol=1e-15)
