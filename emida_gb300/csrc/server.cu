@@ -1,13 +1,16 @@
 // server.cu -- a request loop over the multi-layout planner.  A request is a
 // scan row: n patterns of one size on one registered ROI layout (reference
-// spectra resident per layout).  Rows are admitted while the device pattern
-// arena of their size has room for all their patterns (admission by free
-// HBM), copied in on their own stream, and computed in steps that take
-// patterns from every admitted row in turn (continuous batching): a row that
-// arrives while others run joins the next step.  Each pattern size has its
-// own planner and streams, so their steps overlap on the device.  The
-// reference's counterpart is the load / GPU / finalize thread pipeline of
-// src/process_files.hpp:79-237, which runs one layout and one row at a time.
+// spectra resident per layout).  A pinned row on a layout whose ROIs cover at
+// most half of the pattern is read in place by the kernels; any other row is
+// admitted while the device pattern arena of its size has room for all its
+// patterns (admission by free HBM) and copied in on its own stream, chunk by
+// chunk, only its ROI row bands.  Steps of up to step_patterns patterns are
+// filled from the oldest admitted rows first (continuous batching): a row that
+// arrives while others run joins the next step that has room, so its work
+// overlaps theirs on the device.  Each pattern size has its own planner and
+// streams, so their steps overlap too.  The reference's counterpart is the
+// load / GPU / finalize thread pipeline of src/process_files.hpp:79-237, which
+// runs one layout and one row at a time.
 #include <algorithm>
 #include <chrono>
 #include <condition_variable>
@@ -71,7 +74,6 @@ struct pool {
     cudaStream_t copy = nullptr, out = nullptr;
     std::deque<request *> pending;
     std::vector<request *> active;
-    size_t rr = 0;          // round-robin cursor over active rows
     uint32_t max_rois = 0;  // largest layout of this pattern size
     step steps[2];
 };
@@ -177,18 +179,17 @@ int launch_step(emida_gb_server *sv, pool &p, step &st)
     const size_t pat_elems = (size_t)p.w * p.h;
     st.rois = 0;
     uint32_t budget = sv->step_patterns;
-    const size_t na = p.active.size();
-    for (size_t k = 0; k < na && budget; ++k) {
-        request *r = p.active[(p.rr + k) % na];
+    // oldest admitted rows first: a row's latency is its own work plus the
+    // rows ahead of it, and a row that arrives meanwhile fills what is left
+    for (size_t k = 0; k < p.active.size() && budget; ++k) {
+        request *r = p.active[k];
         if (r->next >= r->n) continue;
         while (r->landed_chunks < r->chunks.size() &&
                cudaEventQuery(r->chunks[r->landed_chunks]) == cudaSuccess)
             ++r->landed_chunks;
         const uint32_t landed = r->in_place ? r->n : std::min(r->n, r->landed_chunks * COPY_CHUNK);
         if (landed <= r->next) continue;
-        // an even share per row keeps every row moving
-        uint32_t take = std::min(landed - r->next, std::max(1u, sv->step_patterns / (uint32_t)na));
-        take = std::min(take, budget);
+        const uint32_t take = std::min(landed - r->next, budget);
         st.parts.push_back(step::part{r, r->next, take, st.rois});
         for (uint32_t i = 0; i < take; ++i) {
             const uint32_t k = r->next + i;
@@ -203,7 +204,6 @@ int launch_step(emida_gb_server *sv, pool &p, step &st)
         r->next += take;
         budget -= take;
     }
-    p.rr = na ? (p.rr + 1) % na : 0;
     if (st.parts.empty()) return EMIDA_GB_OK;
     // sized once for the largest step this pool can build (a regrow frees
     // device memory, which waits for the whole device)
