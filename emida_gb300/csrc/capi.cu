@@ -1058,7 +1058,7 @@ constexpr uint32_t NOALLOC_MAX_SIDE = 1024;
 constexpr size_t NOALLOC_COL_OFFSET = NOALLOC_MAX_SIDE * sizeof(double2);
 constexpr int NOALLOC_MAX_DEVICES = 64;
 
-__device__ __align__(256) unsigned char g_noalloc_twiddles[2 * NOALLOC_COL_OFFSET];
+static __device__ __align__(256) unsigned char g_noalloc_twiddles[2 * NOALLOC_COL_OFFSET];
 
 std::mutex g_noalloc_mutex;
 void *g_noalloc_ptr[NOALLOC_MAX_DEVICES];  // device address of the array, per device

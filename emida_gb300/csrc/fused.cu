@@ -274,12 +274,15 @@ __global__ void __launch_bounds__(N * G / 4, fused_min_blocks(N, sizeof(T)))
             } else {
                 const uint16_t *src = reinterpret_cast<const uint16_t *>(pattern_base(pic)) +
                                       (size_t)beg.y * a.src_w + beg.x;
-                for (int i = tid; i < side * side; i += THREADS)
-                    t16[(i / side) * TW + xo + (i % side)] = src[(size_t)(i / side) * a.src_w + (i % side)];
+                // a warp per tile row, lanes along x: coalesced, and no division
+                // by the runtime side
+                for (int r = warp; r < side; r += WARPS)
+                    for (int x = lane; x < side; x += 32) t16[r * TW + xo + x] = src[(size_t)r * a.src_w + x];
                 __syncthreads();
             }
-            uint32_t acc = 0;
-            for (int i = tid; i < side * side; i += THREADS) acc += t16[(i / side) * TW + xo + (i % side)];
+            uint32_t acc = 0;  // exact, so any summation order gives the same total
+            for (int r = tid >> 2; r < side; r += THREADS >> 2)
+                for (int x = tid & 3; x < side; x += 4) acc += t16[r * TW + xo + x];
 #pragma unroll
             for (int o = 16; o; o >>= 1) acc += __shfl_xor_sync(0xffffffffu, acc, o);
             if (lane == 0) red_i[warp] = acc;
@@ -646,12 +649,13 @@ __global__ void __cluster_dims__(2, 1, 1) __launch_bounds__(cl::THREADS, 1)
             if (!mbar_wait(bar, iter & 1) && tid == 0) atomicOr(a.err, DEV_ERR_TMA_TIMEOUT);
         } else {
             const uint16_t *src = pattern_base(pic) + (size_t)(beg.y + r0) * a.src_w + beg.x;
-            for (int i = tid; i < nrows * side; i += THREADS)
-                t16[(i / side) * TW + xo + (i % side)] = src[(size_t)(i / side) * a.src_w + (i % side)];
+            for (int r = warp; r < nrows; r += WARPS)
+                for (int x = lane; x < side; x += 32) t16[r * TW + xo + x] = src[(size_t)r * a.src_w + x];
             __syncthreads();
         }
         uint32_t acc = 0;
-        for (int i = tid; i < nrows * side; i += THREADS) acc += t16[(i / side) * TW + xo + (i % side)];
+        for (int r = tid >> 2; r < nrows; r += THREADS >> 2)
+            for (int x = tid & 3; x < side; x += 4) acc += t16[r * TW + xo + x];
 #pragma unroll
         for (int o = 16; o; o >>= 1) acc += __shfl_xor_sync(0xffffffffu, acc, o);
         if (lane == 0) red_i[warp] = acc;
