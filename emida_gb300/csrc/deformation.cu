@@ -5,10 +5,12 @@
 // vector minimising |A x|: the right singular vector of the smallest singular
 // value, reshaped to 3 x 3 and divided by its [2][2] entry.
 //
-// One warp per pattern.  The system sits in shared memory column by column and
-// a one-sided (Hestenes) Jacobi SVD in FP64 orthogonalises its nine columns by
-// plane rotations; the accumulated rotations are the right singular vectors
-// and the column norms the singular values.  Optionally a quality mask drops
+// One warp per pattern, FP64.  The system sits in shared memory column by
+// column; a Householder QR reduces it to a 9 x 9 triangle R with the same right
+// singular vectors, and a one-sided (Hestenes) Jacobi SVD orthogonalises R's
+// nine columns by plane rotations: the accumulated rotations are the right
+// singular vectors and the column norms the singular values.  The QR costs
+// about a tenth of the FP64 work of running the rotations over all 2S rows.  Optionally a quality mask drops
 // ROIs whose fitted peak is not a clear maximum, as jove/analyze.py:44-56 does
 // (det of the negated quadratic's Hessian <= min_det), and a pattern with ten
 // or fewer good ROIs yields NaN.
@@ -38,6 +40,7 @@ __global__ void __launch_bounds__(32)
     const uint32_t rows = 2 * n_rois;
     double *A = sm;                  // column j: A[j * rows + i]
     double *V = sm + NC * rows;      // V[r * NC + c], starts as the identity
+    double *B = V + NC * NC;         // R of A = QR, column-major, B[c * NC + r]
     const int lane = threadIdx.x;
     const uint32_t pat = blockIdx.x;
     const double *off = offsets + (size_t)pat * n_rois * 2;
@@ -67,35 +70,57 @@ __global__ void __launch_bounds__(32)
     for (int o = 16; o; o >>= 1) kept += __shfl_xor_sync(0xffffffffu, kept, o);
     __syncwarp();
 
-    // cyclic one-sided Jacobi sweeps
+    // Householder QR, A = QR: the right singular vectors of A are those of the
+    // 9 x 9 triangle R, so the iterative part below works on nine rows only
+    for (int k = 0; k < NC; ++k) {
+        double *ak = A + k * rows;
+        double n2 = 0;
+        for (uint32_t i = k + lane; i < rows; i += 32) n2 += ak[i] * ak[i];
+        n2 = warp_sum(n2);
+        const double x0 = ak[k];
+        __syncwarp();
+        if (n2 == 0.0) continue;  // the column is zero from row k down: R[k][k] = 0
+        const double alpha = x0 >= 0 ? -sqrt(n2) : sqrt(n2);
+        const double vtv = 2.0 * (n2 - alpha * x0);  // |x - alpha e_k|^2
+        if (lane == 0) ak[k] = x0 - alpha;          // the reflector v, in place
+        __syncwarp();
+        for (int j = k + 1; j < NC; ++j) {
+            double *aj = A + j * rows;
+            double w = 0;
+            for (uint32_t i = k + lane; i < rows; i += 32) w += ak[i] * aj[i];
+            w = warp_sum(w);
+            const double f = 2.0 * w / vtv;
+            for (uint32_t i = k + lane; i < rows; i += 32) aj[i] -= f * ak[i];
+            __syncwarp();
+        }
+        if (lane == 0) ak[k] = alpha;
+        __syncwarp();
+    }
+    for (int i = lane; i < NC * NC; i += 32) {
+        const int c = i / NC, r = i % NC;
+        B[i] = r <= c ? A[c * rows + r] : 0.0;
+    }
+    __syncwarp();
+
+    // cyclic one-sided Jacobi sweeps on R: lane r < 9 holds row r
     for (int sweep = 0; sweep < MAX_SWEEPS; ++sweep) {
         bool rotated = false;
         for (int p = 0; p < NC - 1; ++p) {
             for (int r = p + 1; r < NC; ++r) {
-                double al = 0, be = 0, ga = 0;
-                for (uint32_t i = lane; i < rows; i += 32) {
-                    const double x = A[p * rows + i], y = A[r * rows + i];
-                    al += x * x;
-                    be += y * y;
-                    ga += x * y;
-                }
-                al = warp_sum(al);
-                be = warp_sum(be);
-                ga = warp_sum(ga);
+                const double x = lane < NC ? B[p * NC + lane] : 0.0;
+                const double y = lane < NC ? B[r * NC + lane] : 0.0;
+                const double al = warp_sum(x * x), be = warp_sum(y * y), ga = warp_sum(x * y);
                 if (al == 0.0 || be == 0.0 || fabs(ga) <= 1e-15 * sqrt(al * be)) continue;
                 rotated = true;
                 const double zeta = (be - al) / (2.0 * ga);
                 const double t = copysign(1.0, zeta) / (fabs(zeta) + sqrt(1.0 + zeta * zeta));
                 const double c = 1.0 / sqrt(1.0 + t * t), s = c * t;
-                for (uint32_t i = lane; i < rows; i += 32) {
-                    const double x = A[p * rows + i], y = A[r * rows + i];
-                    A[p * rows + i] = c * x - s * y;
-                    A[r * rows + i] = s * x + c * y;
-                }
                 if (lane < NC) {
-                    const double x = V[lane * NC + p], y = V[lane * NC + r];
-                    V[lane * NC + p] = c * x - s * y;
-                    V[lane * NC + r] = s * x + c * y;
+                    B[p * NC + lane] = c * x - s * y;
+                    B[r * NC + lane] = s * x + c * y;
+                    const double vx = V[lane * NC + p], vy = V[lane * NC + r];
+                    V[lane * NC + p] = c * vx - s * vy;
+                    V[lane * NC + r] = s * vx + c * vy;
                 }
                 __syncwarp();
             }
@@ -103,13 +128,12 @@ __global__ void __launch_bounds__(32)
         if (!rotated) break;
     }
 
-    // smallest singular value's column of V
+    // the smallest singular value's column of V
     int jmin = 0;
     double smin = INFINITY;
     for (int j = 0; j < NC; ++j) {
-        double n2 = 0;
-        for (uint32_t i = lane; i < rows; i += 32) n2 += A[j * rows + i] * A[j * rows + i];
-        n2 = warp_sum(n2);
+        const double x = lane < NC ? B[j * NC + lane] : 0.0;
+        const double n2 = warp_sum(x * x);
         if (n2 < smin) {
             smin = n2;
             jmin = j;
@@ -124,7 +148,7 @@ __global__ void __launch_bounds__(32)
 
 }  // namespace
 
-size_t homography_smem(uint32_t n_rois) { return (size_t)(NC * 2 * n_rois + NC * NC) * sizeof(double); }
+size_t homography_smem(uint32_t n_rois) { return (size_t)(NC * 2 * n_rois + 2 * NC * NC) * sizeof(double); }
 
 cudaError_t launch_homography(const double *mids, const double *offsets, uint32_t n_rois,
                               uint32_t patterns, double cx, double cy, double cz, const double *coefs,
