@@ -61,6 +61,9 @@ def parse():
     ap.add_argument("--patterns", type=int, default=256)
     ap.add_argument("--profile-case", type=int, default=0,
                     help="run only N patterns through the chosen form a few times (for ncu)")
+    ap.add_argument("--profile-target", default="fused", choices=["fused", "cluster", "homography"],
+                    help="profile case: the detector's fused kernel; the 256-point cluster kernel "
+                         "(1024^2, 6 x 6 ROIs of 128^2); the deformation fit (N patterns x 100 ROIs)")
     ap.add_argument("--no-plain", action="store_true", help="skip the plain-form comparison")
     ap.add_argument("--config", default="detector",
                     choices=["detector", "batching", "serving", "precision"],
@@ -493,6 +496,45 @@ def run_precision(args):
     print(json.dumps(line), flush=True)
 
 
+def run_profile_target(args):
+    """Small cases of the 256-point cluster kernel and of the deformation fit
+    for ncu: a few launches, then one CUDA-event timing line."""
+    import ctypes
+    import __graft_entry__
+    __graft_entry__.build_library()
+    from emida_gb300 import DeviceBuffer, GpuOffset, _lib, synth
+    n = args.profile_case
+    if args.profile_target == "cluster":
+        ref = synth.reference_pattern(1024, 5)
+        uniq, _ = synth.deformed_patterns(1024, 5, 8, sigma_eps=5e-3)
+        _, begins = synth.roi_grid(1024, 6, 64, margin=80)
+        pics = np.ascontiguousarray(np.resize(uniq, (n, 1024, 1024)))
+        g = GpuOffset((1024, 1024), begins, (128, 128), (255, 255), 8, "fft", 5, 1, "float",
+                      np.uint16, "fused")
+        g.allocate_memory(ref)
+        d, o = DeviceBuffer.from_array(pics), DeviceBuffer(n * len(begins) * 16)
+        for _ in range(3):
+            g.run_device(d, n, o)
+        _lib.call("emida_gb_synchronize")
+        ms = g.time_device(d, n, o, 5) / 5
+        print(json.dumps({"profile_target": "cluster", "pairs": n * len(begins), "ms": ms}))
+        g.close()
+        return
+    rng = np.random.default_rng(1)
+    axis = np.linspace(60, 964, 10)
+    mids = np.array([(x, y) for y in axis for x in axis])
+    offs = rng.normal(0, 1.0, (n, len(mids), 2))
+    dm, do, dout = DeviceBuffer.from_array(mids), DeviceBuffer.from_array(offs), DeviceBuffer(n * 72)
+    c = (ctypes.c_double * 3)(512.0, 512.0, 512.0)
+    args_c = (dm.ptr, do.ptr, len(mids), n, c, None, 0.0, dout.ptr)
+    for _ in range(2):
+        _lib.call("emida_gb_fit_homography", *args_c, None)
+    _lib.call("emida_gb_synchronize")
+    ms = ctypes.c_float()
+    _lib.call("emida_gb_time_fit_homography", *args_c, 5, ctypes.byref(ms))
+    print(json.dumps({"profile_target": "homography", "patterns": n, "ms": ms.value / 5}))
+
+
 def main():
     args = parse()
     rank, world, local = dist_env()
@@ -504,6 +546,8 @@ def main():
         return run_serving(args)
     if args.config == "precision":
         return run_precision(args)
+    if args.profile_case and args.profile_target != "fused":
+        return run_profile_target(args)
 
     import __graft_entry__
     __graft_entry__.build_library()
