@@ -634,7 +634,8 @@ def main():
     _lib.call("emida_gb_time_fit_homography", *fit_args, 10, ctypes.byref(fit_ms))
     deformation = {"patterns_per_s": P / (fit_ms.value / 10 / 1000.0), "ms_per_step": fit_ms.value / 10,
                    "what": "per pattern a 3x3 projective map from its 100 ROI offsets "
-                           "(FP64 one-sided Jacobi SVD of the 200 x 9 system, one warp per pattern)"}
+                           "(FP64 Householder QR of the 200 x 9 system and a one-sided Jacobi SVD of "
+                           "its 9 x 9 triangle, one warp per pattern)"}
 
     # plain form on the same data for the fused-vs-plain ratio
     plain = None

@@ -1,5 +1,5 @@
 """The deformation fit after the path (python/process_offsets.py:83-104) on the
-GPU: FP64 one-sided Jacobi SVD per pattern against the reference script's own
+GPU: FP64 QR and one-sided Jacobi SVD per pattern against the reference script's own
 output, against the oracle (scipy's SVD, as the reference calls it), with the
 quality mask of jove/analyze.py, and on offsets computed by the path."""
 import os
