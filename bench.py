@@ -619,6 +619,9 @@ def main():
     flop = pairs_per_step * (5 * 128 * 128 * 14 + 6 * 65 * 128 + 3 * 64 * 64)
     sm_max = 2070.0
     fp32_peak = 152 * 128 * 2 * sm_max * 1e6 / 1e12
+    # the arithmetic pipe of the chosen precision: FP32 lanes at the maximum SM
+    # clock, or GB300's nominal FP64 rate (no measured FP64 peak is available)
+    fpu, fpu_peak = ("fp32", fp32_peak) if args.precision == "float" else ("fp64", 1.25)
 
     # the deformation fit after the path (python/process_offsets.py:83-104) on
     # this job's offsets, with the fit-quality mask: one projective map per pattern
@@ -723,9 +726,9 @@ def main():
                          "traffic": (TRAFFIC_PER_PAIR * pairs_per_step + TRAFFIC_PER_LAUNCH
                                      if g.mode == "fused" and args.precision == "float" else None),
                          "note": "FP32 pipe / shared memory bound; see compute"},
-            "compute": {"fp32_tflops": flop / (ms_step / 1000.0) / 1e12,
-                        "fp32_peak_tflops_nominal": fp32_peak,
-                        "frac": flop / (ms_step / 1000.0) / 1e12 / fp32_peak,
+            "compute": {f"{fpu}_tflops": flop / (ms_step / 1000.0) / 1e12,
+                        f"{fpu}_peak_tflops_nominal": fpu_peak,
+                        "frac": flop / (ms_step / 1000.0) / 1e12 / fpu_peak,
                         "flop_per_pair": flop // pairs_per_step},
             "plain": plain,
             "deformation_fit": deformation,
