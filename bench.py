@@ -65,6 +65,8 @@ def parse():
                     help="profile case: the detector's fused kernel; the 256-point cluster kernel "
                          "(1024^2, 6 x 6 ROIs of 128^2); the deformation fit (N patterns x 100 ROIs)")
     ap.add_argument("--no-plain", action="store_true", help="skip the plain-form comparison")
+    ap.add_argument("--in-flight", type=int, default=3,
+                    help="e2e: batches in flight through submit/wait (device input buffers)")
     ap.add_argument("--config", default="detector",
                     choices=["detector", "batching", "serving", "precision"],
                     help="detector: 256 x 1024^2, 100 ROIs r=32 (default); batching: patterns on "
@@ -567,7 +569,7 @@ def main():
     S = len(begins)
     pics = np.ascontiguousarray(np.resize(uniq, (P, 1024, 1024)))
     pairs_per_step = P * S
-    g = GpuOffset((1024, 1024), begins, (64, 64), (127, 127), 32, "fft", 5, 3, args.precision,
+    g = GpuOffset((1024, 1024), begins, (64, 64), (127, 127), 32, "fft", 5, args.in_flight, args.precision,
                   np.uint16, args.mode)
     g.allocate_memory(ref)
     d_pics = DeviceBuffer.from_array(pics)
@@ -661,7 +663,7 @@ def main():
     host_offs = np.zeros((pairs_per_step, 2))
     e2e_steps = max(2, args.steps // 4)
     nb = P // 32
-    in_flight = 3
+    in_flight = args.in_flight
 
     def e2e_step():
         pending = []

@@ -714,6 +714,7 @@ static int ring_init(emida_gb_handle *h)
         CK(cudaMallocHost((void **)&r.h_offsets, 2 * sizeof(double) * h->N));
         CK(cudaMallocHost((void **)&r.h_coefs, 6 * sizeof(double) * h->N));
         CK(cudaMallocHost(&r.h_maxes, h->di_elem * h->N));
+        CK(cudaMallocHost((void **)&r.h_err, sizeof(uint32_t)));
         CK(cudaEventCreateWithFlags(&r.h2d, cudaEventDisableTiming));
         CK(cudaEventCreateWithFlags(&r.comp, cudaEventDisableTiming));
         CK(cudaEventCreateWithFlags(&r.done, cudaEventDisableTiming));
@@ -761,6 +762,8 @@ int emida_gb_submit(emida_gb_handle *h, const void *batch, uint32_t patterns, ui
     CK(cudaMemcpyAsync(r.h_offsets, r.d_offsets, 2 * sizeof(double) * n, cudaMemcpyDeviceToHost, h->out_stream));
     CK(cudaMemcpyAsync(r.h_coefs, r.d_coefs, 6 * sizeof(double) * n, cudaMemcpyDeviceToHost, h->out_stream));
     CK(cudaMemcpyAsync(r.h_maxes, r.d_maxes, h->di_elem * n, cudaMemcpyDeviceToHost, h->out_stream));
+    // the error word travels with the results: wait() reads it without a synchronous copy
+    CK(cudaMemcpyAsync(r.h_err, h->d_err, sizeof(uint32_t), cudaMemcpyDeviceToHost, h->out_stream));
     CK(cudaEventRecord(r.done, h->out_stream));
     r.busy = true;
     r.ticket = t;
@@ -783,7 +786,7 @@ int emida_gb_wait(emida_gb_handle *h, uint64_t ticket, double *offsets, double *
             return fail(EMIDA_GB_INVALID_ARGUMENT, "unknown ticket %llu", (unsigned long long)ticket);
     }
     CK(cudaEventSynchronize(r->done));
-    CKS(check_device_error(h));
+    if (*r->h_err) CKS(check_device_error(h));  // reports the flags and clears the word
     const size_t n = (size_t)r->patterns * h->S;
     std::memcpy(offsets, r->h_offsets, 2 * sizeof(double) * n);
     if (coefs) std::memcpy(coefs, r->h_coefs, 6 * sizeof(double) * n);
@@ -858,6 +861,7 @@ void emida_gb_destroy(emida_gb_handle *h)
         if (r.h_offsets) cudaFreeHost(r.h_offsets);
         if (r.h_coefs) cudaFreeHost(r.h_coefs);
         if (r.h_maxes) cudaFreeHost(r.h_maxes);
+        if (r.h_err) cudaFreeHost(r.h_err);
         for (cudaEvent_t e : {r.h2d, r.comp, r.done})
             if (e) cudaEventDestroy(e);
     }

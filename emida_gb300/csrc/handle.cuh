@@ -127,6 +127,7 @@ struct emida_gb_handle {
         void *d_maxes = nullptr;
         double *h_offsets = nullptr, *h_coefs = nullptr;
         void *h_maxes = nullptr;
+        uint32_t *h_err = nullptr;  // the device error word as it stood after this slot's path
         cudaEvent_t h2d = nullptr, comp = nullptr, done = nullptr;
         uint64_t ticket = 0;
         uint32_t patterns = 0;
