@@ -586,10 +586,13 @@ def main():
 
     # parity gate on the bench data: the first pattern against the FP64 oracle
     from oracle import oracle as eo
-    g.run_device(d_pics, P, d_offs, d_coefs)
+    d_maxes = DeviceBuffer(pairs_per_step * 16)
+    g.run_device(d_pics, P, d_offs, d_coefs, d_maxes)
     _lib.call("emida_gb_synchronize")
     offs = d_offs.download(np.float64, (pairs_per_step, 2))
-    o_offs, o_coefs, _ = eo.get_offsets(ref, pics[:2], begins, 64, 64, eo.POLICY_FFT, 5)
+    peaks = d_maxes.download(g.data_index, pairs_per_step)["index"][:2 * S]
+    o_offs, o_coefs, o_peaks = eo.get_offsets(ref, pics[:2], begins, 64, 64, eo.POLICY_FFT, 5)
+    peak_match = float(np.mean(peaks == o_peaks))
     ok = well_posed(o_coefs, 5)
     d = np.abs(offs[:2 * S] - o_offs)
     err = float(d[ok].max())
@@ -721,6 +724,7 @@ def main():
                        "l2": "inputs larger than L2 (512 MB of patterns)",
                        "parallelism": f"patterns sharded over {world} GPU(s)"},
             "parity": {"max_abs_err_px": err, "rms_err_px": rms, "tol_px": tol,
+                       "peak_match_rate": peak_match,
                        "vs": "FP64 oracle, first two patterns", "well_posed_fits": int(ok.sum()),
                        "extrapolated_fits": int((~ok).sum())},
             "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
