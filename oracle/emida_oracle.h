@@ -8,7 +8,7 @@
  * Parity is pinned against the reference's own golden vectors
  * (test/get_offset_test.cpp:10-27 and :120-200, test/cross_corr_test.cpp,
  * test/maxarg_test.cpp, test/subpixel_max_test.cpp, test/prepare_test.cpp,
- * test/sum_test.cpp) and, where /root/reference is mounted, against the
+ * test/sum_test.cpp) and, where the reference's sources are mounted, against the
  * reference's CPU code compiled by oracle/Makefile into oracle/_ref/.
  *
  * Layouts follow the reference (src/gpu_offset.hpp:41-45): patterns are
