@@ -195,8 +195,13 @@ __device__ void mma_issuer(const brute_tc_args &a, unsigned char *smem, const ba
                            uint64_t q0, uint64_t q1, uint32_t tmem)
 {
     constexpr uint32_t idesc = idesc_bf16_f32(TM, TN);
-    const uint32_t b_hi = smem_u32(smem + L::b_hi), b_lo = smem_u32(smem + L::b_lo);
-    const uint32_t ring = smem_u32(smem + L::a_ring);
+    // Every operand address is a base plus a constant, and a descriptor's low
+    // 14 bits are the address / 16, so each descriptor below is a base
+    // descriptor plus a small integer: the single issuing thread spends a few
+    // adds per MMA instead of rebuilding four 64-bit descriptors.
+    const uint64_t dA0 = smem_desc(smem_u32(smem + L::a_ring), 128, 128);
+    const uint64_t dBh0 = smem_desc(smem_u32(smem + L::b_hi) + 64 * 16, B_KBLK, 128);  // pattern row 0
+    const uint64_t dBl0 = smem_desc(smem_u32(smem + L::b_lo) + 64 * 16, B_KBLK, 128);
     uint32_t g = 0, k = 0;
     bool ok = true;
     for (uint64_t q = q0; q < q1 && ok; ++q, ++k) {
@@ -208,17 +213,16 @@ __device__ void mma_issuer(const brute_tc_args &a, unsigned char *smem, const ba
             const int s = (int)(g % NST);
             if (!(ok = mbar_wait(&bar.full[s], (g / NST) & 1))) break;
             tc_fence_after();
+            const uint64_t dAs = dA0 + (uint64_t)((s * STAGE) >> 4);
 #pragma unroll
             for (int rr = 0; rr < RPS; ++rr) {
-                const int row = st * RPS + rr;
-                const uint32_t ahi = ring + s * STAGE + rr * 2 * A_ROW, alo = ahi + A_ROW;
-                const uint32_t boff = (uint32_t)(64 - row) * 16;
+                const uint64_t row = (uint64_t)(st * RPS + rr);  // B starts row rows earlier
 #pragma unroll
                 for (int ks = 0; ks < SIDE / 16; ++ks) {
-                    const uint64_t dah = smem_desc(ahi + ks * 256, 128, 128);
-                    const uint64_t dal = smem_desc(alo + ks * 256, 128, 128);
-                    const uint64_t dbh = smem_desc(b_hi + ks * 2 * B_KBLK + boff, B_KBLK, 128);
-                    const uint64_t dbl = smem_desc(b_lo + ks * 2 * B_KBLK + boff, B_KBLK, 128);
+                    const uint64_t dah = dAs + ((rr * 2 * A_ROW + ks * 256) >> 4);
+                    const uint64_t dal = dah + (A_ROW >> 4);
+                    const uint64_t dbh = dBh0 - row + ((ks * 2 * B_KBLK) >> 4);
+                    const uint64_t dbl = dBl0 - row + ((ks * 2 * B_KBLK) >> 4);
                     mma_bf16(d, dah, dbh, idesc, (st | rr | ks) != 0);
                     mma_bf16(d, dah, dbl, idesc, 1);
                     mma_bf16(d, dal, dbh, idesc, 1);
