@@ -8,12 +8,12 @@ from ._lib import EmidaError, LIB_PATH  # noqa: F401
 from .api import (  # noqa: F401
     CROSS_POLICY_BRUTE, CROSS_POLICY_FFT, DATA_INDEX_F32, DATA_INDEX_F64, DeviceBuffer,
     GpuOffset, MultiLayout, Server, device_count, fit_homography, get_offset, lstsq_matrix,
-    pinned_array, subpixel_max,
+    pinned_array, read_results, subpixel_max,
 )
 
 __all__ = [
     "EmidaError", "GpuOffset", "MultiLayout", "Server", "get_offset", "DeviceBuffer", "device_count", "lstsq_matrix",
-    "subpixel_max", "pinned_array", "fit_homography", "CROSS_POLICY_BRUTE", "CROSS_POLICY_FFT", "DATA_INDEX_F32",
+    "subpixel_max", "pinned_array", "fit_homography", "read_results", "CROSS_POLICY_BRUTE", "CROSS_POLICY_FFT", "DATA_INDEX_F32",
     "DATA_INDEX_F64",
     "LIB_PATH",
 ]

@@ -508,3 +508,24 @@ def fit_homography(mids, offsets, centre, coefs=None, min_det=1e-6):
               d_coefs.ptr if d_coefs is not None else None, float(min_det), d_out.ptr, None)
     _lib.call("emida_gb_synchronize")
     return d_out.download(np.float64, (p, 3, 3))
+
+
+def read_results(path):
+    """Reads the CLI's --binary results file: a list of per-pattern dicts with
+    x, y, name, mids [S][2] (uint32), offsets [S][2] and coefs [S][6]."""
+    import struct
+    out = []
+    with open(path, "rb") as f:
+        data = f.read()
+    pos = 0
+    rec = np.dtype([("mid", "<u4", 2), ("offset", "<f8", 2), ("coefs", "<f8", 6)])
+    while pos < len(data):
+        x, y, n, ln = struct.unpack_from("<ddII", data, pos)
+        pos += 24
+        name = data[pos:pos + ln].decode()
+        pos += ln
+        r = np.frombuffer(data, dtype=rec, count=n, offset=pos)
+        pos += n * rec.itemsize
+        out.append({"x": x, "y": y, "name": name, "mids": r["mid"].copy(),
+                    "offsets": r["offset"].copy(), "coefs": r["coefs"].copy()})
+    return out

@@ -45,6 +45,7 @@ struct params {
     cross_policy policy = CROSS_POLICY_FFT;
     esize_t batch = 1, workers = 1;
     int mode = EMIDA_GB_MODE_AUTO;
+    std::string binary;  // results as binary records instead of text
 };
 
 const char *usage =
@@ -65,6 +66,10 @@ const char *usage =
     "  --loadworkers N            pattern loading threads (default 1)\n"
     "  --mode auto|plain|fused|tensor  execution form (default auto; tensor: brute\n"
     "                             policy on the tensor cores, float, 64x64 ROIs)\n"
+    "  --binary FILE              write the results to FILE as binary records (full\n"
+    "                             precision) instead of text: per pattern f64 x, f64 y,\n"
+    "                             u32 rois, u32 name bytes, name; per ROI u32 mid x,\n"
+    "                             u32 mid y, f64 dx, f64 dy, f64 coefs[6] (little-endian)\n"
     "  -h,--help\n";
 
 bool parse_pair(const std::string &v, size2_t &out)
@@ -242,6 +247,7 @@ bool parse(int argc, char **argv, params &a, bool &help)
                  : m == "tensor" ? EMIDA_GB_MODE_TENSOR
                                  : EMIDA_GB_MODE_AUTO;
     }
+    if (v.count("binary")) a.binary = v["binary"];
     a.analysis = v.count("analysis") > 0;
     a.write_coefs = v.count("writecoefs") > 0;
     std::string err;
@@ -405,6 +411,13 @@ int process(const params &a)
             order_cv.notify_all();
         }
     };
+    // the binary results file is opened before any worker starts, so a failure
+    // leaves no thread running
+    FILE *bin = nullptr;
+    if (!a.binary.empty() && !(bin = fopen(a.binary.c_str(), "wb"))) {
+        std::cerr << "Error: cannot open " << a.binary << " for writing\n";
+        return 1;
+    }
     // GPU stage (src/process_files.hpp:184-216)
     std::thread gpu([&]() {
         for (esize_t b = 0; b < n_batches; ++b) {
@@ -432,6 +445,24 @@ int process(const params &a)
             if (f->files == 0) continue;  // a batch that failed to load is skipped
             auto r = offs.finalize(f->maxes.data(), f->neigh.data());
             for (esize_t j = f->first; j < f->first + f->files; ++j) {
+                if (bin) {
+                    // the same content, unrounded: pattern header, then one record per ROI
+                    const uint32_t n = (uint32_t)S, len = (uint32_t)work[j].fname.size();
+                    fwrite(&work[j].x, sizeof(double), 1, bin);
+                    fwrite(&work[j].y, sizeof(double), 1, bin);
+                    fwrite(&n, sizeof n, 1, bin);
+                    fwrite(&len, sizeof len, 1, bin);
+                    fwrite(work[j].fname.data(), 1, len, bin);
+                    const esize_t it = j - f->first;
+                    for (esize_t i = it * S; i < (it + 1) * S; ++i) {
+                        const uint32_t mid[2] = {(uint32_t)a.mids[i % S].x, (uint32_t)a.mids[i % S].y};
+                        const double o[2] = {r.offsets[i].x, r.offsets[i].y};
+                        fwrite(mid, sizeof mid, 1, bin);
+                        fwrite(o, sizeof o, 1, bin);
+                        fwrite(r.coefs[i].data(), sizeof(double), 6, bin);
+                    }
+                    continue;
+                }
                 printf("%f %f %llu %s\n", work[j].x, work[j].y, (unsigned long long)S,
                        work[j].fname.c_str());
                 const esize_t it = j - f->first;
@@ -458,6 +489,10 @@ int process(const params &a)
     for (auto &t : loaders) t.join();
     gpu.join();
     fin.join();
+    if (bin && fclose(bin) != 0) {
+        std::cerr << "Error: writing " << a.binary << " failed\n";
+        return 1;
+    }
     for (auto p : pinned) emida_gb_free_host(p);
     fflush(stdout);
     return 0;

@@ -75,3 +75,31 @@ def test_cli_end_to_end_matches_oracle(tmp_path, policy, precision, fit, tol):
             scale = np.abs(o_coefs[k]).max()
             rel = 1e-5 if precision == "float" else 1e-9
             assert np.abs(np.array([float(v) for v in row[4:]]) - o_coefs[k]).max() <= rel * scale + 1e-6
+
+
+@pytest.mark.gpu
+@pytest.mark.parametrize("mode,policy,precision", [("fused", "fft", "float"), ("tensor", "brute", "float")])
+def test_cli_binary_results_match_text(tmp_path, mode, policy, precision):
+    # --binary writes the same results unrounded; the text form rounds them to %f
+    from emida_gb300 import read_results, synth
+    ref = synth.reference_pattern(256, seed=43)
+    pics, _ = synth.deformed_patterns(256, 43, 3, 3e-3)
+    mids, begins = synth.roi_grid(256, 3, 32, margin=40)
+    paths = write_inputs(str(tmp_path), ref, pics, mids, 32, big_endian=False)
+    common = ["-i", paths[0], "-d", paths[1], "-b", paths[2], "--precision", precision, "-f", 5,
+              "--crosspolicy", policy, "--batchsize", 2, "--mode", mode]
+    text = run_cli(*common, "-q")
+    assert text.returncode == 0, text.stdout + text.stderr
+    out = tmp_path / "results.bin"
+    r = run_cli(*common, "--binary", out)
+    assert r.returncode == 0, r.stdout + r.stderr
+    assert r.stdout.strip() == ""  # the results went to the file
+    got = read_results(out)
+    expect = parse_output(text.stdout)
+    assert len(got) == len(expect) == 3
+    for g, (hdr, rows) in zip(got, expect):
+        assert (g["x"], g["y"], len(g["mids"]), g["name"]) == (hdr[0], hdr[1], hdr[2], hdr[3])
+        vals = np.array([[float(v) for v in row] for row in rows])
+        assert np.array_equal(g["mids"], vals[:, :2].astype(np.uint32))
+        assert np.abs(g["offsets"] - vals[:, 2:4]).max() <= 5e-7
+        assert np.abs(g["coefs"] - vals[:, 4:]).max() <= 5e-7 * max(1.0, np.abs(g["coefs"]).max())
