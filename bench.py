@@ -65,6 +65,8 @@ def parse():
                     help="profile case: the detector's fused kernel; the 256-point cluster kernel "
                          "(1024^2, 6 x 6 ROIs of 128^2); the deformation fit (N patterns x 100 ROIs)")
     ap.add_argument("--no-plain", action="store_true", help="skip the plain-form comparison")
+    ap.add_argument("--sample-seconds", type=float, default=0.0,
+                    help="reference arm: seconds of host work per step (default: ~20 s in all)")
     ap.add_argument("--in-flight", type=int, default=3,
                     help="e2e: batches in flight through submit/wait (device input buffers)")
     ap.add_argument("--config", default="detector",
@@ -190,7 +192,7 @@ def run_reference(args, rank, world):
         return
     ref, uniq, begins = workload()
     threads = os.cpu_count() or 1
-    per_step = max(2.0, 20.0 / max(1, args.steps + args.warmup))
+    per_step = args.sample_seconds or max(2.0, 20.0 / max(1, args.steps + args.warmup))
     vals = []
     for i in range(args.warmup + args.steps):
         v, pairs, dt = cpu_reference(ref, uniq, begins, per_step, threads)
