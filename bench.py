@@ -61,9 +61,12 @@ def parse():
     ap.add_argument("--patterns", type=int, default=256)
     ap.add_argument("--profile-case", type=int, default=0,
                     help="run only N patterns through the chosen form a few times (for ncu)")
-    ap.add_argument("--profile-target", default="fused", choices=["fused", "cluster", "homography"],
+    ap.add_argument("--profile-target", default="fused",
+                    choices=["fused", "cluster", "homography", "ingest"],
                     help="profile case: the detector's fused kernel; the 256-point cluster kernel "
-                         "(1024^2, 6 x 6 ROIs of 128^2); the deformation fit (N patterns x 100 ROIs)")
+                         "(1024^2, 6 x 6 ROIs of 128^2); the deformation fit (N patterns x 100 ROIs); "
+                         "N detector patterns from pinned host memory through submit/wait, copied "
+                         "and then gathered, three batches of 32 in flight")
     ap.add_argument("--no-plain", action="store_true", help="skip the plain-form comparison")
     ap.add_argument("--sample-seconds", type=float, default=0.0,
                     help="reference arm: seconds of host work per step (default: ~20 s in all)")
@@ -501,13 +504,35 @@ def run_precision(args):
 
 
 def run_profile_target(args):
-    """Small cases of the 256-point cluster kernel and of the deformation fit
-    for ncu: a few launches, then one CUDA-event timing line."""
+    """Small cases of the 256-point cluster kernel, of the deformation fit and
+    of the ingest modes for ncu: a few launches, then one timing line."""
     import ctypes
     import __graft_entry__
     __graft_entry__.build_library()
-    from emida_gb300 import DeviceBuffer, GpuOffset, _lib, synth
+    from emida_gb300 import DeviceBuffer, GpuOffset, _lib, pinned_array, synth
     n = args.profile_case
+    if args.profile_target == "ingest":
+        ref, uniq, begins = workload()
+        host = pinned_array((n, 1024, 1024))
+        host[:] = np.resize(uniq, (n, 1024, 1024))
+        g = GpuOffset((1024, 1024), begins, (64, 64), (127, 127), 32, "fft", 5, 3, "float",
+                      np.uint16, "fused")
+        g.allocate_memory(ref)
+        out = {"profile_target": "ingest", "patterns": n}
+        for mode in ("copy", "gather"):
+            g.ingest = mode
+            t0 = time.perf_counter()
+            pending = []
+            for b in range(0, n, 32):
+                if len(pending) == 3:
+                    g.wait(pending.pop(0))
+                pending.append(g.submit(host[b:b + 32]))
+            for t in pending:
+                g.wait(t)
+            out[mode + "_ms"] = (time.perf_counter() - t0) * 1000
+        print(json.dumps(out))
+        g.close()
+        return
     if args.profile_target == "cluster":
         ref = synth.reference_pattern(1024, 5)
         uniq, _ = synth.deformed_patterns(1024, 5, 8, sigma_eps=5e-3)
@@ -690,9 +715,10 @@ def main():
     e2e_ms = max_over_ranks((time.perf_counter() - t0) * 1000 / e2e_steps, dist, device="cuda")
     e2e_value = whole_job_rate(pairs_per_step, e2e_ms / 1000.0, world)
     # the other ingest modes: kernels reading the ROI pixels in place (no
-    # copy), and every other batch each way
+    # copy), every other batch each way, and a gather kernel packing the ROI
+    # rows beside the path
     ingest = {}
-    for mode in ("in_place", "split"):
+    for mode in ("in_place", "split", "gather"):
         g.ingest = mode
         if g.ingest != mode:
             continue

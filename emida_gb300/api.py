@@ -164,6 +164,7 @@ class GpuOffset:
         _lib.call("emida_gb_create", ctypes.byref(p), ctypes.byref(h))
         self._h = h
         self._pinned = []
+        self._submitted = {}  # ticket -> patterns
 
     @property
     def handle(self):
@@ -226,21 +227,35 @@ class GpuOffset:
 
     def submit(self, pic, patterns=None):
         """Queue one batch (host memory, pinned for overlap) and return a ticket.
-        `pic` must stay alive and unchanged until wait(ticket)."""
-        patterns = self.batch_size if patterns is None else int(patterns)
+        `pic` must stay alive and unchanged until wait(ticket).  An array
+        batch holds len(pic) patterns unless `patterns` says fewer; an address
+        holds batch_size patterns unless `patterns` says otherwise."""
+        if isinstance(pic, int):
+            patterns = self.batch_size if patterns is None else int(patterns)
+            ptr = pic
+        else:
+            have = pic.size * pic.itemsize // (self.src_size[0] * self.src_size[1] * self.in_dtype.itemsize)
+            patterns = have if patterns is None else int(patterns)
+            if not pic.flags.c_contiguous or pic.dtype != self.in_dtype or patterns > have:
+                raise ValueError(f"submit needs {patterns} contiguous {self.in_dtype} patterns")
+            ptr = pic.ctypes.data
         t = ctypes.c_uint64()
-        ptr = pic if isinstance(pic, int) else pic.ctypes.data
         _lib.call("emida_gb_submit", self._h, ctypes.c_void_p(ptr), patterns, ctypes.byref(t))
+        self._submitted[t.value] = patterns
         return t.value
 
     def wait(self, ticket, patterns=None, with_peaks=False):
-        """Results of a submitted batch: (offsets, coefs[, peaks])."""
-        n = (self.batch_size if patterns is None else int(patterns)) * len(self.begins)
+        """Results of a submitted batch: (offsets, coefs[, peaks]), one row per
+        ROI of each of its patterns."""
+        if patterns is None:
+            patterns = self._submitted.get(ticket, self.batch_size)
+        n = int(patterns) * len(self.begins)
         offs = np.zeros((n, 2))
         coefs = np.zeros((n, 6))
         peaks = np.zeros(n, dtype=np.uint32)
         _lib.call("emida_gb_wait", self._h, ctypes.c_uint64(ticket), _dptr(offs), _dptr(coefs),
                   peaks.ctypes.data_as(ctypes.POINTER(ctypes.c_uint32)))
+        self._submitted.pop(ticket, None)
         return (offs, coefs, peaks) if with_peaks else (offs, coefs)
 
     def run_device(self, dev_pics, patterns, dev_offsets, dev_coefs=None, dev_maxes=None,
@@ -261,19 +276,23 @@ class GpuOffset:
     def stream(self):
         return _lib.lib().emida_gb_stream(self._h)
 
-    INGEST = ("copy", "in_place", "split")
+    INGEST = ("copy", "in_place", "split", "gather")
 
     @property
     def ingest(self):
         """How submit() brings pinned host batches to the kernels: "copy",
-        "in_place" (kernels read the ROI pixels over the host link, no copy) or
-        "split" (alternate batches, copy engine and host reads in parallel)."""
+        "in_place" (kernels read the ROI pixels over the host link, no copy),
+        "split" (alternate batches, copy engine and host reads in parallel) or
+        "gather" (a gather kernel on a few SMs packs only the ROI rows into
+        device memory beside the previous batch's path)."""
         return self.INGEST[_lib.lib().emida_gb_ingest(self._h)]
 
     @ingest.setter
     def ingest(self, mode):
         """In-place modes are honoured only when the ROIs cover at most half
-        of each pattern (a fused or tensor form); otherwise "copy" stays."""
+        of each pattern (a fused or tensor form); "gather" only for a fused or
+        tensor form with uint16 input, a width divisible by 8 and a compact
+        ROI layout no larger than a pattern; otherwise "copy" stays."""
         _lib.call("emida_gb_set_ingest", self._h, self.INGEST.index(mode))
 
     def launches_per_run(self):

@@ -405,10 +405,12 @@ cudaError_t launch_brute_tc(const brute_tc_args &a, int grid, cudaStream_t st)
     if (e == cudaSuccess)
         e = cudaFuncSetAttribute(brute_tc_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, L::bytes);
     if (e != cudaSuccess) return e;
-    if (grid <= 0) grid = sms;
+    if (grid <= 0) grid = sms + grid > 1 ? sms + grid : 1;
     if ((uint64_t)grid > total) grid = (int)total;
     brute_tc_kernel<<<grid, THREADS, L::bytes, st>>>(a);
     return cudaGetLastError();
 }
+
+size_t brute_tc_smem_bytes() { return L::bytes; }
 
 }  // namespace emida_gb

@@ -28,7 +28,9 @@ struct brute_tc_args {
 constexpr uint32_t BRUTE_TC_SIDE = 64;
 constexpr uint32_t BRUTE_TC_CROSS = 2 * BRUTE_TC_SIDE - 1;
 
-// grid <= 0: one CTA per SM.
+// grid <= 0: one CTA per SM, less -grid CTAs.
 cudaError_t launch_brute_tc(const brute_tc_args &a, int grid, cudaStream_t st);
+// Dynamic shared memory of one CTA.
+size_t brute_tc_smem_bytes();
 
 }  // namespace emida_gb

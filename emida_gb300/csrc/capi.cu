@@ -244,13 +244,14 @@ int emida_gb::host::run_plain_chunk(emida_gb_handle *h, const void *pics, uint32
 }
 
 int emida_gb::host::run_fused(emida_gb_handle *h, const void *pics, uint32_t pats, void *maxes, void *neigh,
-              double *offsets, double *coefs, cudaStream_t st)
+              double *offsets, double *coefs, cudaStream_t st, const batch_view *view, int grid)
 {
+    const size2 src = view ? view->src : h->src;
     fused_args a{};
     a.pics = pics;
-    a.src_w = h->src.x;
-    a.src_h = h->src.y;
-    a.begins = h->d_begins;
+    a.src_w = src.x;
+    a.src_h = src.y;
+    a.begins = view ? view->begins : h->d_begins;
     a.n_rois = h->S;
     a.n_pairs = pats * h->S;
     a.side = h->slice.x;
@@ -270,11 +271,10 @@ int emida_gb::host::run_fused(emida_gb_handle *h, const void *pics, uint32_t pat
     a.stage = STAGE_PLAIN;
     bool on_device = true;
     CKS(pattern_location(pics, on_device));
-    if (on_device && !h->in_f64 && (h->src.x % 8) == 0 && ((uintptr_t)pics % 16) == 0) {
+    if (on_device && !h->in_f64 && (src.x % 8) == 0 && ((uintptr_t)pics % 16) == 0) {
         if (encode_fn enc = get_encoder()) {
-            const cuuint64_t dims[3] = {h->src.x, h->src.y, pats};
-            const cuuint64_t strides[2] = {(cuuint64_t)h->src.x * 2,
-                                           (cuuint64_t)h->src.x * h->src.y * 2};
+            const cuuint64_t dims[3] = {src.x, src.y, pats};
+            const cuuint64_t strides[2] = {(cuuint64_t)src.x * 2, (cuuint64_t)src.x * src.y * 2};
             const cuuint32_t box[3] = {(h->slice.x + 14) & ~7u, fused_box_rows(h->w2, h->slice.y), 1};
             const cuuint32_t estr[3] = {1, 1, 1};
             if (enc(&map, CU_TENSOR_MAP_DATA_TYPE_UINT16, 3, const_cast<void *>(pics), dims,
@@ -284,18 +284,18 @@ int emida_gb::host::run_fused(emida_gb_handle *h, const void *pics, uint32_t pat
                 a.stage = STAGE_TMA;
         }
     }
-    CK(launch_fused(h->w2, h->dbl, h->in_f64, a, &map, 0, st));
+    CK(launch_fused(h->w2, h->dbl, h->in_f64, a, &map, grid, st));
     return EMIDA_GB_OK;
 }
 
 int emida_gb::host::run_tensor(emida_gb_handle *h, const void *pics, uint32_t pats, void *maxes, void *neigh,
-               double *offsets, double *coefs, cudaStream_t st)
+               double *offsets, double *coefs, cudaStream_t st, const batch_view *view, int grid)
 {
     brute_tc_args a{};
     a.pics = static_cast<const uint16_t *>(pics);
-    a.src_w = h->src.x;
-    a.src_h = h->src.y;
-    a.begins = h->d_begins;
+    a.src_w = view ? view->src.x : h->src.x;
+    a.src_h = view ? view->src.y : h->src.y;
+    a.begins = view ? view->begins : h->d_begins;
     a.n_rois = h->S;
     a.n_patterns = pats;
     a.ref_prep = h->d_ref_prep64;
@@ -307,15 +307,18 @@ int emida_gb::host::run_tensor(emida_gb_handle *h, const void *pics, uint32_t pa
     a.maxes = maxes;
     a.neigh = static_cast<float *>(neigh);
     a.err = h->d_err;
-    CK(launch_brute_tc(a, 0, st));
+    CK(launch_brute_tc(a, grid, st));
     return EMIDA_GB_OK;
 }
 
 int emida_gb::host::run_any(emida_gb_handle *h, const void *pics, uint32_t pats, void *maxes, void *neigh,
-            double *offsets, double *coefs, cudaStream_t st)
+            double *offsets, double *coefs, cudaStream_t st, const batch_view *view, int grid)
 {
-    if (h->mode == EMIDA_GB_MODE_FUSED) return run_fused(h, pics, pats, maxes, neigh, offsets, coefs, st);
-    if (h->mode == EMIDA_GB_MODE_TENSOR) return run_tensor(h, pics, pats, maxes, neigh, offsets, coefs, st);
+    if (h->mode == EMIDA_GB_MODE_FUSED)
+        return run_fused(h, pics, pats, maxes, neigh, offsets, coefs, st, view, grid);
+    if (h->mode == EMIDA_GB_MODE_TENSOR)
+        return run_tensor(h, pics, pats, maxes, neigh, offsets, coefs, st, view, grid);
+    if (view) return fail(EMIDA_GB_UNSUPPORTED, "the staged form reads whole patterns only");
     const size_t pat_bytes = (size_t)h->src.x * h->src.y * h->in_elem;
     const size_t s2 = (size_t)h->p.fitsize * h->p.fitsize;
     for (uint32_t done = 0; done < pats; done += h->B) {
@@ -513,6 +516,9 @@ int emida_gb_create(const emida_gb_params *p, emida_gb_handle **out)
     row_bands(h);
     h->in_place_allowed = h->mode != EMIDA_GB_MODE_PLAIN &&
                           2 * (uint64_t)p->n_rois * p->slice_w * p->slice_h <= (uint64_t)p->src_w * p->src_h;
+    h->gather_allowed = h->mode != EMIDA_GB_MODE_PLAIN && !h->in_f64 && p->src_w % 8 == 0 &&
+                        (uint64_t)p->n_rois * p->slice_h * gather_width(p->slice_w) <=
+                            (uint64_t)p->src_w * p->src_h;
     if (h->mode == EMIDA_GB_MODE_FUSED) {
         // the resident reference spectra are computed at the fused length
         h->w2 = h->h2 = fn;
@@ -545,6 +551,19 @@ int emida_gb_create(const emida_gb_params *p, emida_gb_handle **out)
         CK(cudaMemcpy(h->d_begins, h->begins.data(), sizeof(uint2) * h->S, cudaMemcpyHostToDevice));
         return EMIDA_GB_OK;
     }());
+    if (h->gather_allowed) {
+        std::vector<uint32_t> compact(2 * (size_t)h->S);
+        for (uint32_t r = 0; r < h->S; ++r) {
+            compact[2 * r] = h->begins[2 * r] & 7u;
+            compact[2 * r + 1] = r * h->slice.y;
+        }
+        TRY(h->alloc((void **)&h->d_begins_compact, sizeof(uint2) * h->S));
+        TRY([&]() -> int {
+            CK(cudaMemcpy(h->d_begins_compact, compact.data(), sizeof(uint2) * h->S,
+                          cudaMemcpyHostToDevice));
+            return EMIDA_GB_OK;
+        }());
+    }
     TRY(upload_hann(h, &h->d_hann, h->slice.x, h->slice.y));
     const size_t sum_elem = h->in_f64 ? 8 : 4;
     TRY(h->alloc(&h->d_sums_ref, sum_elem * h->S));
@@ -703,6 +722,12 @@ int emida_gb_get_offset(emida_gb_handle *h, const void *batch, double *offsets, 
     return EMIDA_GB_OK;
 }
 
+// CTAs of the gather ingest: host reads over NVLink-C2C top out near 15 GB/s
+// per SM, so 16 CTAs of 256 threads reach the link's rate for ROI rows
+// (about 145 GB/s of ROI pixels against 211 GB/s for contiguous reads) when
+// they run alone; beside the path's CTAs they run slower.
+constexpr int GATHER_CTAS = 16;
+
 static int ring_init(emida_gb_handle *h)
 {
     if (!h->ring.empty()) return EMIDA_GB_OK;
@@ -746,8 +771,29 @@ int emida_gb_submit(emida_gb_handle *h, const void *batch, uint32_t patterns, ui
     const bool in_place_host = pa.type == cudaMemoryTypeHost &&
                                (h->ingest == EMIDA_GB_INGEST_IN_PLACE ||
                                 (h->ingest == EMIDA_GB_INGEST_SPLIT && (t & 1)));
+    const bool gather = pa.type == cudaMemoryTypeHost && h->ingest == EMIDA_GB_INGEST_GATHER &&
+                        (uintptr_t)batch % 16 == 0;
     const void *src = batch;
-    if (!(pa.type == cudaMemoryTypeDevice || pa.type == cudaMemoryTypeManaged || in_place_host)) {
+    batch_view compact{size2{gather_width(h->slice.x), h->S * h->slice.y}, h->d_begins_compact};
+    const batch_view *view = nullptr;
+    int grid = 0;
+    if (gather) {
+        // only the ROI rows cross the host link, packed by a gather kernel on
+        // GATHER_CTAS CTAs of the path's footprint; the path launches that
+        // many CTAs short of a full wave, so the gather of the next batch runs
+        // beside it
+        const size_t smem = h->mode == EMIDA_GB_MODE_FUSED ? fused_smem_bytes(h->w2, h->dbl)
+                                                           : brute_tc_smem_bytes();
+        CK(cudaStreamWaitEvent(h->in_stream, r.comp, 0));
+        CK(run_gather_rois(static_cast<const uint16_t *>(batch), h->src, h->d_begins, h->S, h->slice,
+                           patterns, static_cast<uint16_t *>(h->d_in[si]), GATHER_CTAS, smem,
+                           h->in_stream));
+        CK(cudaEventRecord(r.h2d, h->in_stream));
+        CK(cudaStreamWaitEvent(h->comp, r.h2d, 0));
+        src = h->d_in[si];
+        view = &compact;
+        grid = -GATHER_CTAS;
+    } else if (!(pa.type == cudaMemoryTypeDevice || pa.type == cudaMemoryTypeManaged || in_place_host)) {
         // the input buffer is free once the slot's previous computation ran
         CK(cudaStreamWaitEvent(h->in_stream, r.comp, 0));
         CKS(copy_patterns(h, h->d_in[si], batch, patterns, h->in_stream));
@@ -755,7 +801,7 @@ int emida_gb_submit(emida_gb_handle *h, const void *batch, uint32_t patterns, ui
         CK(cudaStreamWaitEvent(h->comp, r.h2d, 0));
         src = h->d_in[si];
     }
-    CKS(run_any(h, src, patterns, r.d_maxes, h->d_neigh, r.d_offsets, r.d_coefs, h->comp));
+    CKS(run_any(h, src, patterns, r.d_maxes, h->d_neigh, r.d_offsets, r.d_coefs, h->comp, view, grid));
     CK(cudaEventRecord(r.comp, h->comp));
     CK(cudaStreamWaitEvent(h->out_stream, r.comp, 0));
     const size_t n = (size_t)patterns * h->S;
@@ -837,10 +883,13 @@ int emida_gb_ingest(const emida_gb_handle *h) { return h ? h->ingest : -1; }
 int emida_gb_set_ingest(emida_gb_handle *h, int mode)
 {
     if (!h) return fail(EMIDA_GB_INVALID_ARGUMENT, "null handle");
-    if (mode < EMIDA_GB_INGEST_COPY || mode > EMIDA_GB_INGEST_SPLIT)
+    if (mode < EMIDA_GB_INGEST_COPY || mode > EMIDA_GB_INGEST_GATHER)
         return fail(EMIDA_GB_INVALID_ARGUMENT, "invalid ingest mode %d", mode);
     std::lock_guard<std::mutex> lk(h->mu);
-    h->ingest = h->in_place_allowed ? mode : EMIDA_GB_INGEST_COPY;
+    const bool ok = mode == EMIDA_GB_INGEST_GATHER ? h->gather_allowed
+                    : mode == EMIDA_GB_INGEST_COPY ? true
+                                                   : h->in_place_allowed;
+    h->ingest = ok ? mode : EMIDA_GB_INGEST_COPY;
     return EMIDA_GB_OK;
 }
 void *emida_gb_stream(emida_gb_handle *h) { return h ? (void *)h->comp : nullptr; }

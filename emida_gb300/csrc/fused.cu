@@ -871,7 +871,8 @@ static cudaError_t launch_cluster(const fused_args &a, const CUtensorMap *tmap, 
         int dev = 0, sms = 0;
         cudaGetDevice(&dev);
         cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
-        grid = sms;  // one CTA per SM, two per cluster
+        grid += sms;  // one CTA per SM, two per cluster, less the CTAs left free
+        if (grid < 2) grid = 2;
     }
     grid &= ~1;
     if ((uint32_t)grid > 2 * a.n_pairs) grid = (int)(2 * a.n_pairs);
@@ -896,7 +897,8 @@ static cudaError_t launch_one(const fused_args &a, const CUtensorMap *tmap, int 
         e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k, threads, smem);
         if (e != cudaSuccess) return e;
         if (per_sm < 1) per_sm = 1;
-        grid = per_sm * sms;
+        grid += per_sm * sms;  // less the CTAs left free
+        if (grid < 1) grid = 1;
     }
     if ((uint32_t)grid > a.n_pairs) grid = (int)a.n_pairs;
     if (grid < 1) return cudaSuccess;
@@ -915,6 +917,18 @@ uint32_t fused_size_for(uint32_t side, bool dbl, bool in_f64)
     for (uint32_t n : {64u, 96u, 128u, 192u, 256u})
         if (2 * side <= n && fused_supported(n, dbl, in_f64)) return n;
     return 0;
+}
+
+size_t fused_smem_bytes(uint32_t fft_n, bool dbl)
+{
+    switch (fft_n) {
+    case 64: return dbl ? fused_layout<64, 8, double>::bytes : fused_layout<64, 8, float>::bytes;
+    case 96: return dbl ? fused_layout<96, 4, double>::bytes : fused_layout<96, 4, float>::bytes;
+    case 128: return dbl ? fused_layout<128, 8, double>::bytes : fused_layout<128, 8, float>::bytes;
+    case 192: return fused_layout<192, 8, float>::bytes;
+    case 256: return cl::layout::bytes;
+    default: return 0;
+    }
 }
 
 uint32_t fused_box_rows(uint32_t fft_n, uint32_t side)

@@ -55,11 +55,15 @@ __host__ __device__ inline int lstsq_offset(int s)
 bool fused_supported(uint32_t fft_n, bool dbl, bool in_f64 = false);
 // The smallest fused transform that holds a zero-padded ROI of this side (0: none).
 uint32_t fused_size_for(uint32_t side, bool dbl, bool in_f64 = false);
+// Dynamic shared memory of one CTA of the fused kernel for this length.
+size_t fused_smem_bytes(uint32_t fft_n, bool dbl);
 // Rows of the TMA box a CTA stages per ROI (the 256-point kernel's CTAs each
 // stage half of the ROI).
 uint32_t fused_box_rows(uint32_t fft_n, uint32_t side);
 
-// grid <= 0: one wave of resident CTAs (occupancy x SM count).
+// grid <= 0: one wave of resident CTAs (occupancy x SM count) less -grid CTAs,
+// which leaves room for a kernel that runs beside it (the gather of the next
+// batch).
 cudaError_t launch_fused(uint32_t fft_n, bool dbl, bool in_f64, const fused_args &a,
                          const CUtensorMap *tmap, int grid, cudaStream_t st);
 

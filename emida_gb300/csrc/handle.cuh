@@ -43,13 +43,24 @@ int run_plain_chunk(emida_gb_handle *h, const void *pics, uint32_t pats, void *m
                     double *offsets, double *coefs, cudaStream_t st,
                     const void *const *ptrs = nullptr, const uint32_t *out_base = nullptr,
                     void *maxes_out = nullptr);
+// The pattern geometry a fused or tensor launch reads: the patterns as given,
+// or the compact ROI layout that the gather ingest writes (patterns of
+// gather_width(side) x n_rois * side pixels, ROI r at (x_r & 7, r * side)).
+struct batch_view {
+    size2 src;
+    const uint2 *begins;
+};
+// `grid` as launch_fused and launch_brute_tc take it (<= 0: one wave less -grid CTAs).
 int run_fused(emida_gb_handle *h, const void *pics, uint32_t pats, void *maxes, void *neigh,
-              double *offsets, double *coefs, cudaStream_t st);
+              double *offsets, double *coefs, cudaStream_t st, const batch_view *view = nullptr,
+              int grid = 0);
 int run_tensor(emida_gb_handle *h, const void *pics, uint32_t pats, void *maxes, void *neigh,
-               double *offsets, double *coefs, cudaStream_t st);
-// Either form, any number of patterns.
+               double *offsets, double *coefs, cudaStream_t st, const batch_view *view = nullptr,
+               int grid = 0);
+// Either form, any number of patterns (a view only for the fused and tensor forms).
 int run_any(emida_gb_handle *h, const void *pics, uint32_t pats, void *maxes, void *neigh,
-            double *offsets, double *coefs, cudaStream_t st);
+            double *offsets, double *coefs, cudaStream_t st, const batch_view *view = nullptr,
+            int grid = 0);
 int check_device_error(emida_gb_handle *h);
 // Host -> device copy of `patterns` whole patterns as the kernels need them:
 // only the row bands that hold ROI pixels (one pitched copy per band over all
@@ -119,6 +130,11 @@ struct emida_gb_handle {
     // rows [first, first + second) of a pattern that hold ROI pixels, merged
     std::vector<std::pair<uint32_t, uint32_t>> bands;
     int ingest = EMIDA_GB_INGEST_COPY;
+    // The gather ingest: allowed for the fused and tensor forms with uint16
+    // input, src_w % 8 == 0 and a compact layout no larger than the patterns;
+    // d_begins_compact holds each ROI's place in the compact layout.
+    bool gather_allowed = false;
+    uint2 *d_begins_compact = nullptr;
     std::mutex mu;
     std::vector<void *> allocs;
     // submit/wait ring: one slot per input buffer

@@ -3,6 +3,8 @@
 // HBM buffers laid out as the reference lays them out.  It is the baseline the
 // fused kernel is measured against and the path for every size the fused kernel
 // does not cover (any ROI size, brute policy, odd FFT lengths).
+#include <algorithm>
+
 #include "device_fit.cuh"
 #include "fft.cuh"
 #include "staged.cuh"
@@ -366,9 +368,66 @@ __global__ void __launch_bounds__(BLOCK) k_to_colmajor(const cplx<T> *__restrict
     out[map * per + (uint64_t)kx * h2 + ky] = in[i];
 }
 
+// One thread per ROI row: the 16-byte chunks of the source row that hold the
+// row's pixels (CH at most), all loads issued before the stores, so that a
+// row costs one round trip (over the host link a read takes microseconds).
+template <int CH>
+__global__ void __launch_bounds__(256) k_gather_rois(const uint16_t *__restrict__ pics, size2 src,
+                                                     const uint2 *__restrict__ begins, uint32_t n_rois,
+                                                     size2 slice, uint32_t cw, uint32_t rows,
+                                                     uint16_t *__restrict__ out)
+{
+    for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < rows; i += gridDim.x * blockDim.x) {
+        const uint32_t pr = i / slice.y, y = i - pr * slice.y;
+        const uint32_t p = pr / n_rois;
+        const uint2 b = begins[pr - p * n_rois];
+        // chunks [x & ~7, roundup(x + side, 8)) stay inside the row: src.x % 8 == 0
+        const uint32_t chunks = ((b.x & 7u) + slice.x + 7) / 8;
+        const int4 *s = reinterpret_cast<const int4 *>(
+            pics + ((size_t)p * src.y + b.y + y) * src.x + (b.x & ~7u));
+        int4 *d = reinterpret_cast<int4 *>(out + (size_t)i * cw);
+        int4 v[CH];
+#pragma unroll
+        for (uint32_t k = 0; k < CH; ++k)
+            if (k < chunks) v[k] = s[k];
+#pragma unroll
+        for (uint32_t k = 0; k < CH; ++k)
+            if (k < chunks) d[k] = v[k];
+    }
+}
+
 inline uint32_t grid_for(uint64_t n) { return (uint32_t)((n + BLOCK - 1) / BLOCK); }
 
 }  // namespace
+
+uint32_t gather_width(uint32_t side) { return (side + 14) & ~7u; }
+
+cudaError_t run_gather_rois(const uint16_t *pics, size2 src, const uint2 *begins, uint32_t n_rois,
+                            size2 slice, uint32_t patterns, uint16_t *out, int ctas, size_t smem,
+                            cudaStream_t st)
+{
+    if (src.x % 8 || (uintptr_t)pics % 16 || (uintptr_t)out % 16) return cudaErrorInvalidValue;
+    const uint32_t cw = gather_width(slice.x), ch = cw / 8;
+    if (ch > 17) return cudaErrorInvalidValue;  // ROI sides up to 128
+    const size_t pat_out = (size_t)n_rois * slice.y * cw;
+    // launches of at most 2^31 rows, so that row indices stay 32-bit
+    const uint32_t per = (uint32_t)std::max<uint64_t>(1, (1u << 31) / ((uint64_t)n_rois * slice.y));
+    for (uint32_t p0 = 0; p0 < patterns; p0 += per) {
+        const uint32_t np = std::min(per, patterns - p0);
+        const uint32_t rows = np * n_rois * slice.y;
+        if (rows == 0) return cudaSuccess;
+        const uint32_t grid = std::min<uint32_t>((rows + 255) / 256, (uint32_t)ctas);
+        const uint16_t *in = pics + (size_t)p0 * src.x * src.y;
+        uint16_t *o = out + p0 * pat_out;
+        auto k = ch <= 4 ? k_gather_rois<4> : ch <= 9 ? k_gather_rois<9> : k_gather_rois<17>;
+        cudaError_t e = cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+        if (e != cudaSuccess) return e;
+        k<<<grid, 256, smem, st>>>(in, src, begins, n_rois, slice, cw, rows, o);
+        e = cudaGetLastError();
+        if (e != cudaSuccess) return e;
+    }
+    return cudaSuccess;
+}
 
 cudaError_t run_sums(const void *pics, int in_type, size2 src, const uint2 *begins,
                      uint32_t n_rois, size2 slice, uint32_t batch, void *sums, cudaStream_t st,

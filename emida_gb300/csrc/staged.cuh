@@ -66,6 +66,21 @@ cudaError_t run_fit(const void *neigh, const void *maxes, uint32_t n, int s, siz
                     cudaStream_t st, const uint32_t *out_base = nullptr, uint32_t n_rois = 1,
                     void *maxes_out = nullptr);
 
+// Compact ROI layout for a batch that crosses the host link: row y of ROI r of
+// pattern p lands at out + ((p * n_rois + r) * slice.y + y) * cw, cw =
+// gather_width(slice.x) pixels from source pixel (x_r & ~7), so the ROI
+// starts at column x_r & 7 of its compact rows.  Only the 16-byte chunks that
+// hold ROI pixels are read; pics may be pinned host memory (read over
+// NVLink-C2C) or device memory.  Needs src.x % 8 == 0 and 16-byte aligned
+// pics and out; `ctas` bounds the grid (256 threads each).  Each CTA reserves
+// `smem` bytes of (unused) dynamic shared memory: given the footprint of the
+// kernel it runs beside, a gather CTA takes exactly one of that kernel's CTA
+// slots, so the two fill one wave together whichever is dispatched first.
+uint32_t gather_width(uint32_t side);
+cudaError_t run_gather_rois(const uint16_t *pics, size2 src, const uint2 *begins, uint32_t n_rois,
+                            size2 slice, uint32_t patterns, uint16_t *out, int ctas, size_t smem,
+                            cudaStream_t st);
+
 // Reference spectra from cuFFT layout [S][h2][w2/2+1] to the fused kernel's
 // column-major layout [S][w2/2+1][h2].
 cudaError_t run_spec_to_colmajor(const void *spec, void *out, uint32_t maps, uint32_t w2,

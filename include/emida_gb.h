@@ -136,11 +136,25 @@ int emida_gb_resolved_mode(const emida_gb_handle *h);
  *   IN_PLACE  no copy: the kernels read the batch's ROI pixels in place over the
  *             host link (lowest latency per batch);
  *   SPLIT     every other batch each way, so the copy engine and the kernels'
- *             host reads work in parallel (highest throughput).
+ *             host reads work in parallel;
+ *   GATHER    a gather kernel on a few SMs reads only the 16-byte chunks that
+ *             hold ROI pixels over the host link into a compact device layout,
+ *             beside the previous batch's path (the fewest bytes over the link
+ *             and the lowest latency per batch; with several batches in flight
+ *             the copy engine keeps up better, as the gather's host reads slow
+ *             down beside the path's CTAs).
  * IN_PLACE and SPLIT are taken only by a fused or tensor form whose ROIs cover
- * at most half of each pattern; otherwise the mode stays COPY.
+ * at most half of each pattern; GATHER by a fused or tensor form with uint16
+ * input, src_w a multiple of 8 and a compact layout (n_rois ROIs of side x
+ * ((side + 14) & ~7) pixels) no larger than a pattern, and only for 16-byte
+ * aligned batches (others are copied).  Otherwise the mode stays COPY.
  * emida_gb_ingest reports the mode in force. */
-enum { EMIDA_GB_INGEST_COPY = 0, EMIDA_GB_INGEST_IN_PLACE = 1, EMIDA_GB_INGEST_SPLIT = 2 };
+enum {
+    EMIDA_GB_INGEST_COPY = 0,
+    EMIDA_GB_INGEST_IN_PLACE = 1,
+    EMIDA_GB_INGEST_SPLIT = 2,
+    EMIDA_GB_INGEST_GATHER = 3
+};
 int emida_gb_set_ingest(emida_gb_handle *h, int mode);
 int emida_gb_ingest(const emida_gb_handle *h);
 /* The handle's compute stream (a cudaStream_t). */

@@ -119,3 +119,73 @@ def test_server_rows_in_place_equal_copied_rows(data):
         s.close()
     for (a_offs, a_coefs), (b_offs, b_coefs) in zip(results[False], results[True]):
         assert np.array_equal(a_offs, b_offs) and np.array_equal(a_coefs, b_coefs)
+
+
+def _ragged_begins(w, h, side, n, seed):
+    # x at every remainder mod 8, the right and bottom edges included
+    rng = np.random.default_rng(seed)
+    xs = list(rng.integers(0, w - side + 1, n - 2)) + [w - side, 0]
+    ys = list(rng.integers(0, h - side + 1, n - 2)) + [h - side, h - side]
+    return np.array(list(zip(xs, ys)), dtype=np.int64)
+
+
+@pytest.mark.parametrize("side,precision,mode", [(32, "float", "fused"), (24, "float", "fused"),
+                                                 (48, "float", "fused"), (96, "float", "fused"),
+                                                 (128, "float", "fused"), (32, "double", "fused"),
+                                                 (64, "float", "tensor")])
+def test_submit_gather_ingest_equals_copy(side, precision, mode):
+    # the gather kernel packs only the ROI rows of a pinned batch; the path then
+    # reads the compact layout and gives the bits of the copied batch
+    from emida_gb300 import GpuOffset, pinned_array, synth
+    w, h, batch = 520, 384, 3
+    ref = synth.reference_pattern((w, h), seed=side)
+    pics, _ = synth.deformed_patterns((w, h), side, 2 * batch, sigma_eps=3e-3)
+    # the compact layout (ROIs of side x ((side + 14) & ~7) pixels) fits in a pattern
+    begins = _ragged_begins(w, h, side, 8 if side == 128 else 12, seed=side)
+    assert {int(x) % 8 for x, _ in begins} != {0}
+    policy = "brute" if mode == "tensor" else "fft"
+    g = GpuOffset((w, h), begins, (side, side), (2 * side - 1, 2 * side - 1), batch, policy, 5, 3,
+                  precision, np.uint16, mode)
+    g.allocate_memory(ref)
+    host = pinned_array(pics.shape)
+    host[:] = pics
+    expect = [g.get_offset(pics[k:k + batch]) for k in (0, batch)]
+    g.ingest = "gather"
+    assert g.ingest == "gather"
+    tickets = [g.submit(host[k:k + batch]) for k in (0, batch, 0)]
+    for t, (e_offs, e_coefs) in zip(tickets, expect + expect[:1]):
+        offs, coefs = g.wait(t)
+        assert np.array_equal(offs, e_offs) and np.array_equal(coefs, e_coefs)
+    # a partial batch, and a batch that is not 16-byte aligned (copied instead)
+    t = g.submit(host[:2])
+    offs, _ = g.wait(t)
+    assert np.array_equal(offs, expect[0][0][:2 * len(begins)])
+    flat = pinned_array((batch * w * h + 8,))
+    odd = flat[1:1 + batch * w * h].reshape(batch, h, w)
+    odd[:] = pics[:batch]
+    offs, coefs = g.wait(g.submit(odd))
+    assert np.array_equal(offs, expect[0][0]) and np.array_equal(coefs, expect[0][1])
+    g.close()
+
+
+def test_gather_ingest_needs_its_geometry():
+    from emida_gb300 import GpuOffset, synth
+    ref = synth.reference_pattern((260, 256), seed=3)
+    # a width that is not a multiple of 8
+    g = GpuOffset((260, 256), [(0, 0), (100, 90)], (64, 64), (127, 127), 1, "fft", 5, 1, "float",
+                  np.uint16, "fused")
+    g.ingest = "gather"
+    assert g.ingest == "copy"
+    g.close()
+    # a compact layout larger than the pattern (overlapping ROIs)
+    many = [(k % 190, k % 190) for k in range(40)]
+    g = GpuOffset((256, 256), many, (64, 64), (127, 127), 1, "fft", 5, 1, "float", np.uint16, "fused")
+    g.ingest = "gather"
+    assert g.ingest == "copy"
+    g.close()
+    # the staged form and FP64 input read whole patterns
+    for mode, in_type in (("plain", np.uint16), ("fused", np.float64)):
+        g = GpuOffset((256, 256), [(0, 0)], (64, 64), (127, 127), 1, "fft", 5, 1, "float", in_type, mode)
+        g.ingest = "gather"
+        assert g.ingest == "copy"
+        g.close()
