@@ -280,24 +280,29 @@ def run_batching(args):
     total = m.count(layout_of)
     d_offs, d_coefs = DeviceBuffer(total * 16), DeviceBuffer(total * 48)
     report = m.autotune(d_pics, layout_of, d_offs)
-    m.run(d_pics, layout_of, d_offs, d_coefs, graph=True)
+    d_maxes = DeviceBuffer(total * m.data_index.itemsize)
+    m.run(d_pics, layout_of, d_offs, d_coefs, d_maxes, graph=True)
     m.synchronize()
     # parity: the first pattern of every layout against the FP64 oracle
     offs = d_offs.download(np.float64, (total, 2))
     coefs = d_coefs.download(np.float64, (total, 6))
+    peaks = d_maxes.download(m.data_index, total)["index"]
     import concurrent.futures as cf
     starts = np.concatenate([[0], np.cumsum([len(layouts[l][0]) for l in layout_of])])
 
     def check(p):
         begins, side, fs = layouts[layout_of[p]]
-        o, c, _ = eo.get_offsets(ref, uniq[p:p + 1], begins, side, side, eo.POLICY_FFT, fs)
+        o, c, pk = eo.get_offsets(ref, uniq[p:p + 1], begins, side, side, eo.POLICY_FFT, fs)
         sl = slice(starts[p], starts[p + 1])
         ok = well_posed(c, fs)
-        d = np.abs(offs[sl] - o)
-        return float(d[ok].max()) if ok.any() else 0.0, int(ok.sum() // 2), len(o)
+        d = np.abs(offs[sl] - o)[ok]
+        return (float(d.max()) if d.size else 0.0, int(ok.sum() // 2), len(o), float((d ** 2).sum()),
+                d.size, int((peaks[sl] == pk).sum()))
     with cf.ThreadPoolExecutor(os.cpu_count()) as ex:
         res = list(ex.map(check, range(L)))
     err = max(r[0] for r in res)
+    rms = float(np.sqrt(sum(r[3] for r in res) / max(1, sum(r[4] for r in res))))
+    peak_match = sum(r[5] for r in res) / sum(r[2] for r in res)
     assert err <= 1e-2, f"offset error {err} px"
     for _ in range(args.warmup):
         m.run(d_pics, layout_of, d_offs, d_coefs, graph=True)
@@ -317,8 +322,9 @@ def run_batching(args):
         "config": {"workload": f"{P} x 1024^2 uint16 patterns on {L} seeded layouts, radius "
                                f"{radii}, 25-400 ROIs, fit 3-9", "patterns": P, "pairs": int(total)},
         "autotune": report.strip().splitlines(),
-        "parity": {"max_abs_err_px": err, "well_posed_fits": sum(r[1] for r in res),
-                   "checked_pairs": sum(r[2] for r in res), "vs": "FP64 oracle, one pattern per layout"},
+        "parity": {"max_abs_err_px": err, "rms_err_px": rms, "peak_match_rate": peak_match,
+                   "well_posed_fits": sum(r[1] for r in res), "checked_pairs": sum(r[2] for r in res),
+                   "vs": "FP64 oracle, one pattern per layout"},
         "clocks": clk.summary()}), flush=True)
     m.close()
 
@@ -354,14 +360,16 @@ def run_serving(args):
             lay = random_layouts(size, 8, size, (24, 48), (25, 225))
         layouts[size] = [(srv.add_layout((size, size), b, side, fs, ref), b, side, fs) for b, side, fs in lay]
     # parity of one row per size against the FP64 oracle (not timed)
-    errs = []
+    errs, sq = [], []
     for size in sizes:
         lid, begins, side, fs = layouts[size][0]
         ref, buf = rows_src[size]
         offs, coefs, _ = srv.wait(srv.submit(lid, buf[:2]))
         o, c, _ = eo.get_offsets(ref, buf[:2], begins, side, side, eo.POLICY_FFT, fs)
         ok = well_posed(c, fs)
-        errs.append(float(np.abs(offs - o)[ok].max()))
+        d = np.abs(offs - o)[ok]
+        errs.append(float(d.max()))
+        sq.append(d ** 2)
     srv.reset_stats()
     # arrivals
     pending, sent_pairs = [], 0
@@ -395,7 +403,9 @@ def run_serving(args):
                    "hbm_arena_bytes_per_size": 24 << 30, "step_patterns": args.step_patterns,
                    "rows": "copied into the device arena" if args.copy_rows else
                            "pinned rows read in place where ROIs cover <= half the pattern"},
-        "parity": {"max_abs_err_px": max(errs), "vs": "FP64 oracle, one row per size"},
+        "parity": {"max_abs_err_px": max(errs),
+                   "rms_err_px": float(np.sqrt(np.concatenate(sq).mean())),
+                   "vs": "FP64 oracle, one row per size"},
         "clocks": clk.summary()}), flush=True)
     srv.close()
 
