@@ -284,6 +284,9 @@ int emida_gb::host::run_fused(emida_gb_handle *h, const void *pics, uint32_t pat
                 a.stage = STAGE_TMA;
         }
     }
+    // pinned host patterns: cp.async chunks over the host link
+    if (a.stage == STAGE_PLAIN && !h->in_f64 && (src.x % 8) == 0 && ((uintptr_t)pics % 16) == 0)
+        a.stage = STAGE_ASYNC;
     CK(launch_fused(h->w2, h->dbl, h->in_f64, a, &map, grid, st));
     return EMIDA_GB_OK;
 }

@@ -80,6 +80,18 @@ __device__ __forceinline__ void tma_load_3d(void *dst, const CUtensorMap *map, i
         "l"((uint64_t)map), "r"(x), "r"(y), "r"(z), "r"(smem_u32(bar))
         : "memory");
 }
+// 16 bytes global -> shared, cached in L2 only; completion is tracked by
+// cp_async_arrive on an mbarrier.
+__device__ __forceinline__ void cp_async16(void *dst, const void *src)
+{
+    asm volatile("cp.async.cg.shared.global [%0], [%1], 16;" ::"r"(smem_u32(dst)), "l"(src) : "memory");
+}
+// The mbarrier counts one arrival of this thread once all its earlier
+// cp.async copies have landed (the barrier's expected count includes it).
+__device__ __forceinline__ void cp_async_arrive(uint64_t *bar)
+{
+    asm volatile("cp.async.mbarrier.arrive.noinc.shared::cta.b64 [%0];" ::"r"(smem_u32(bar)) : "memory");
+}
 // Bounded wait on an mbarrier phase: returns false when the budget ran out.
 __device__ __forceinline__ bool mbar_wait(uint64_t *bar, uint32_t parity)
 {
@@ -230,8 +242,10 @@ __global__ void __launch_bounds__(N * G / 4, fused_min_blocks(N, sizeof(T)))
     const T *ghann = reinterpret_cast<const T *>(a.hann);
     for (int i = tid; i < 2 * a.side; i += THREADS) hx[i] = ghann[i];  // hx then hy
     const bool tma = U16 && a.stage == STAGE_TMA;
+    const bool cpa = U16 && a.stage == STAGE_ASYNC;
     if (tid == 0) {
-        mbar_init(bar, 1);
+        // TMA: one arrival (with the byte count) per tile; cp.async: one per thread
+        mbar_init(bar, cpa ? THREADS : 1);
         fence_proxy_async();
     }
     __syncthreads();
@@ -253,7 +267,23 @@ __global__ void __launch_bounds__(N * G / 4, fused_min_blocks(N, sizeof(T)))
         mbar_expect_tx(bar, TW * side * 2);
         tma_load_3d(t16, &tmap, (int)(b.x & ~7u), (int)b.y, (int)pic, bar);
     };
+    // cp.async staging: every thread copies some of the tile's 16-byte chunks,
+    // [x & ~7, roundup(x + side, 8)) of each ROI row, to the layout TMA uses
+    // (the ROI starts at column x & 7), then arrives on the barrier
+    auto issue_chunks = [&](uint32_t pair) {
+        const uint4 it = item(pair);
+        const uint2 b = a.begins[it.y];
+        const uint16_t *src = reinterpret_cast<const uint16_t *>(pattern_base(it.x)) +
+                              (size_t)b.y * a.src_w + (b.x & ~7u);
+        const int nch = ((int)(b.x & 7u) + side + 7) >> 3;
+        for (int i = tid; i < side * nch; i += THREADS) {
+            const int r = i / nch, c = i - r * nch;
+            cp_async16(t16 + r * TW + 8 * c, src + (size_t)r * a.src_w + 8 * c);
+        }
+        cp_async_arrive(bar);
+    };
     if (tma && tid == 0 && blockIdx.x < a.n_pairs) issue_tile(blockIdx.x);
+    if (cpa && blockIdx.x < a.n_pairs) issue_chunks(blockIdx.x);
 
     uint32_t iter = 0;
     for (uint32_t pair = blockIdx.x; pair < a.n_pairs; pair += gridDim.x, ++iter) {
@@ -266,7 +296,7 @@ __global__ void __launch_bounds__(N * G / 4, fused_min_blocks(N, sizeof(T)))
         T mean;
         const int xo = U16 ? (int)(beg.x & 7u) : 0;
         if constexpr (U16) {
-            if (tma) {
+            if (tma || cpa) {
                 if (!mbar_wait(bar, iter & 1)) {
                     if (tid == 0) atomicOr(a.err, DEV_ERR_TMA_TIMEOUT);
                     return;
@@ -357,6 +387,7 @@ __global__ void __launch_bounds__(N * G / 4, fused_min_blocks(N, sizeof(T)))
         __syncthreads();
         // the tile is free: fetch the next pair's ROI behind the remaining passes
         if (tma && tid == 0 && pair + gridDim.x < a.n_pairs) issue_tile(pair + gridDim.x);
+        if (cpa && pair + gridDim.x < a.n_pairs) issue_chunks(pair + gridDim.x);
 
         // ---- columns: forward FFT, conj product, inverse FFT --------------
         const C *R = reinterpret_cast<const C *>(a.ref_spec) + (size_t)roi * (SL + 1) * N;

@@ -7,12 +7,15 @@
 
 namespace emida_gb {
 
-// How a uint16 ROI reaches shared memory.  Pinned host patterns are read in
-// place with plain loads: over the host link the ROI rows arrive at about
-// 100 GB/s either way, and plain loads fetch only the ROI's own pixels.
+// How a uint16 ROI reaches shared memory.  TMA reads device memory only, so
+// pinned host patterns (read in place over the host link) and pattern tables
+// are staged by cp.async in 16-byte chunks, which also prefetches the next
+// ROI behind the current one's column pass.
 enum fused_stage : int {
     STAGE_PLAIN = 0,  // synchronous loads by every thread
     STAGE_TMA = 1,    // one TMA box per ROI (device-resident patterns), next ROI prefetched
+    STAGE_ASYNC = 2,  // cp.async chunks of the ROI rows (src_w % 8 == 0, 16-byte aligned
+                      // patterns; any memory the GPU can address), next ROI prefetched
 };
 
 struct fused_args {

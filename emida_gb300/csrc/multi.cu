@@ -242,6 +242,13 @@ int launch_plan(emida_gb_multi *m, const plan &pl, const work_set &ws, const voi
     // one TMA map per size class (the box is the ROI side + 8 by the ROI side)
     const bool use_tma = on_device && (m->src_w % 8) == 0 && ((uintptr_t)pics % 16) == 0 &&
                          get_encoder() != nullptr;
+    // otherwise (host patterns, pattern tables) cp.async chunks, where every
+    // pattern starts on a 16-byte boundary
+    bool use_async = (m->src_w % 8) == 0;
+    if (table)
+        for (uint32_t p = 0; p < patterns && use_async; ++p) use_async = (uintptr_t)table[p] % 16 == 0;
+    else
+        use_async = use_async && (uintptr_t)pics % 16 == 0;
     for (size_t c = 0; c < m->classes.size(); ++c) {
         if (only_class >= 0 && (int)c != only_class) continue;
         auto &k = m->classes[c];
@@ -280,6 +287,7 @@ int launch_plan(emida_gb_multi *m, const plan &pl, const work_set &ws, const voi
                               CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE) == CUDA_SUCCESS)
                 a.stage = STAGE_TMA;
         }
+        if (a.stage == STAGE_PLAIN && use_async) a.stage = STAGE_ASYNC;
         const int grid = grid_override >= 0 ? grid_override : k.grid;
         CK(launch_fused(k.n, m->dbl, false, a, &map, grid, m->stream));
     }
