@@ -67,7 +67,7 @@ int check_device_error(emida_gb_handle *h);
 // patterns), or everything when the bands cover most of a pattern.
 int copy_patterns(emida_gb_handle *h, void *dst, const void *src, uint32_t patterns, cudaStream_t st);
 // Where a pattern array lives.  Device memory is staged through TMA; pinned
-// host memory is read in place by the kernels with plain loads (over the
+// host memory is read in place by the kernels (cp.async chunks over the
 // NVLink-C2C host link on Grace systems), which skips the host-to-device copy
 // of the pixels outside the ROIs.  Pageable memory is refused.
 int pattern_location(const void *patterns, bool &on_device);

@@ -96,7 +96,17 @@ def test_multi_run_table_mixes_device_and_host_patterns(data):
     ptrs = [host[p] if p % 2 else d_pics.ptr.value + p * 512 * 512 * 2 for p in range(len(pics))]
     m.run_table(ptrs, layout_of, o_tab)
     m.synchronize()
-    assert np.array_equal(o_arr.download(np.float64, (total, 2)), o_tab.download(np.float64, (total, 2)))
+    expect = o_arr.download(np.float64, (total, 2))
+    assert np.array_equal(expect, o_tab.download(np.float64, (total, 2)))
+    # a pattern that does not start on a 16-byte boundary: the table is staged
+    # with plain loads instead of 16-byte chunks, with the same bits
+    flat = pinned_array((pics.size + 8,))
+    odd = flat[1:1 + pics.size].reshape(pics.shape)
+    odd[:] = pics
+    o_odd = DeviceBuffer(total * 16)
+    m.run_table([odd[p] if p == 2 else host[p] for p in range(len(pics))], layout_of, o_odd)
+    m.synchronize()
+    assert np.array_equal(expect, o_odd.download(np.float64, (total, 2)))
     m.close()
 
 
