@@ -142,6 +142,32 @@ int make_plan(emida_gb_multi *m, uint32_t patterns, const uint32_t *layout_of, p
 
 using work_set = emida_gb_multi::work_set;
 
+// Host -> device copy of a work list by SM loads from the pinned staging
+// buffer (over NVLink-C2C), not by the copy engine: a copy engine runs its
+// copies in order, so a step's small lists would otherwise wait behind every
+// pattern copy queued before them (the request loop queues whole rows).
+// dst, src 16-byte aligned; bytes a multiple of 4.
+__global__ void __launch_bounds__(256) k_upload(unsigned char *__restrict__ dst,
+                                                const unsigned char *__restrict__ src, size_t bytes)
+{
+    const size_t stride = (size_t)gridDim.x * blockDim.x;
+    const size_t n16 = bytes / 16;
+    for (size_t i = (size_t)blockIdx.x * blockDim.x + threadIdx.x; i < n16; i += stride)
+        reinterpret_cast<int4 *>(dst)[i] = reinterpret_cast<const int4 *>(src)[i];
+    for (size_t j = n16 * 4 + (size_t)blockIdx.x * blockDim.x + threadIdx.x; j < bytes / 4; j += stride)
+        reinterpret_cast<uint32_t *>(dst)[j] = reinterpret_cast<const uint32_t *>(src)[j];
+}
+
+int upload(void *dst, const void *src, size_t bytes, cudaStream_t st)
+{
+    const size_t n16 = (bytes + 15) / 16;
+    const unsigned grid = (unsigned)std::min<size_t>(64, std::max<size_t>(1, (n16 + 255) / 256));
+    k_upload<<<grid, 256, 0, st>>>(static_cast<unsigned char *>(dst), static_cast<const unsigned char *>(src),
+                                   bytes);
+    CK(cudaGetLastError());
+    return EMIDA_GB_OK;
+}
+
 // Stages the plan's work lists in `ws` and queues their copies on m->stream,
 // ahead of the launches that read them.  The set must not be read by work
 // still in flight: the graph's set waits for the stream (a replay may be
@@ -194,7 +220,7 @@ int upload_plan(emida_gb_multi *m, const plan &pl, work_set &ws, bool graph_set,
         CKS(grow(dst, cap, need, 0));
         char *s = reinterpret_cast<char *>(ws.h_stage) + off;
         std::memcpy(s, src, need);
-        CK(cudaMemcpyAsync(*dst, s, need, cudaMemcpyHostToDevice, m->stream));
+        CKS(upload(*dst, s, need, m->stream));
         off += up16(need);
         return EMIDA_GB_OK;
     };
@@ -208,7 +234,7 @@ int upload_plan(emida_gb_multi *m, const plan &pl, work_set &ws, bool graph_set,
         CKS(grow((void **)&ws.d_items[c], &ws.cap[c], need, 0));
         char *stage = reinterpret_cast<char *>(ws.h_stage) + off;
         std::memcpy(stage, v.data(), need);
-        CK(cudaMemcpyAsync(ws.d_items[c], stage, need, cudaMemcpyHostToDevice, m->stream));
+        CKS(upload(ws.d_items[c], stage, need, m->stream));
         off += need;
     }
     return EMIDA_GB_OK;

@@ -30,6 +30,11 @@ namespace {
 
 using clock_t_ = std::chrono::steady_clock;
 constexpr uint32_t COPY_CHUNK = 16;
+// Chunks of copied rows queued on a pool's copy stream at a time (about 1 ms
+// of copies at 1024^2): enough to keep the copy engine busy between polls of
+// the loop, few enough that queuing them never blocks the loop (a full driver
+// queue would hold it, and with it every submit, for the copies' duration).
+constexpr uint32_t COPY_WINDOW = 8;
 
 struct request {
     uint64_t id = 0;
@@ -38,8 +43,8 @@ struct request {
     std::vector<uint32_t> slots;
     uint32_t next = 0, done = 0;  // patterns scheduled / finished
     std::vector<double> offsets, coefs;
-    // one event per COPY_CHUNK patterns copied in: steps take a row's patterns
-    // as soon as their chunk has landed, not when the whole row has
+    // one event per COPY_CHUNK patterns copied in (queued so far): steps take a
+    // row's patterns as soon as their chunk has landed, not when the whole row has
     std::vector<cudaEvent_t> chunks;
     uint32_t landed_chunks = 0;
     // read in place from the caller's pinned rows by the kernels: no arena
@@ -123,9 +128,29 @@ int admit(emida_gb_server *sv, pool &p)
         r->slots.assign(p.free_slots.end() - r->n, p.free_slots.end());
         p.free_slots.resize(p.free_slots.size() - r->n);
         std::sort(r->slots.begin(), r->slots.end());  // consecutive slots copy as one
-        const size_t row = (size_t)p.w * 2, pat = row * p.h;
+        r->admitted = true;
+        p.active.push_back(r);
+    }
+    return EMIDA_GB_OK;
+}
+
+// Queues the copies of admitted rows, oldest row first, chunk by chunk, while
+// fewer than COPY_WINDOW chunks are on their way.
+int issue_copies(emida_gb_server *sv, pool &p)
+{
+    uint32_t in_flight = 0;
+    for (request *r : p.active) {
+        while (r->landed_chunks < r->chunks.size() &&
+               cudaEventQuery(r->chunks[r->landed_chunks]) == cudaSuccess)
+            ++r->landed_chunks;
+        in_flight += (uint32_t)r->chunks.size() - r->landed_chunks;
+    }
+    const size_t row = (size_t)p.w * 2, pat = row * p.h;
+    for (request *r : p.active) {
+        if (r->in_place) continue;
         const auto &bands = sv->layouts[r->layout].bands;
-        for (uint32_t c0 = 0; c0 < r->n; c0 += COPY_CHUNK) {
+        while (in_flight < COPY_WINDOW && r->chunks.size() * COPY_CHUNK < r->n) {
+            const uint32_t c0 = (uint32_t)r->chunks.size() * COPY_CHUNK;
             const uint32_t c1 = std::min(r->n, c0 + COPY_CHUNK);
             for (uint32_t a = c0; a < c1;) {
                 uint32_t b = a + 1;
@@ -142,11 +167,10 @@ int admit(emida_gb_server *sv, pool &p)
             CK(cudaEventCreateWithFlags(&e, cudaEventDisableTiming));
             r->chunks.push_back(e);
             CK(cudaEventRecord(e, p.copy));
+            ++in_flight;
         }
-        r->admitted = true;
-        p.active.push_back(r);
+        if (in_flight >= COPY_WINDOW) break;
     }
-    (void)sv;
     return EMIDA_GB_OK;
 }
 
@@ -169,8 +193,26 @@ int ensure_step_buffers(step &st, size_t rois)
 }
 
 // Builds and queues one step from the rows whose patterns are on the device.
-int launch_step(emida_gb_server *sv, pool &p, step &st)
+// While the pool's other step keeps the GPU busy, a step that would be
+// short of step_patterns waits for more copied patterns to land (when more
+// are on their way), so that copies slower than the path do not cut the work
+// into small, tail-heavy launches.
+int launch_step(emida_gb_server *sv, pool &p, step &st, bool other_busy)
 {
+    if (other_busy) {
+        uint32_t avail = 0;
+        bool more_coming = false;
+        for (request *r : p.active) {
+            if (r->next >= r->n) continue;
+            while (r->landed_chunks < r->chunks.size() &&
+                   cudaEventQuery(r->chunks[r->landed_chunks]) == cudaSuccess)
+                ++r->landed_chunks;
+            const uint32_t landed = r->in_place ? r->n : std::min(r->n, r->landed_chunks * COPY_CHUNK);
+            if (landed > r->next) avail += landed - r->next;
+            more_coming |= landed < r->n;
+        }
+        if (more_coming && avail < sv->step_patterns) return EMIDA_GB_OK;
+    }
     st.parts.clear();
     st.slots.clear();
     std::vector<uint32_t> layout_of;
@@ -264,8 +306,12 @@ void server_loop(emida_gb_server *sv)
                     progress = true;
                 }
             int rc = admit(sv, p);
-            for (auto &st : p.steps)
-                if (rc == EMIDA_GB_OK && !st.busy && !p.active.empty()) rc = launch_step(sv, p, st);
+            if (rc == EMIDA_GB_OK) rc = issue_copies(sv, p);
+            for (int k = 0; k < 2; ++k) {
+                step &st = p.steps[k];
+                if (rc == EMIDA_GB_OK && !st.busy && !p.active.empty())
+                    rc = launch_step(sv, p, st, p.steps[1 - k].busy);
+            }
             if (rc != EMIDA_GB_OK) {
                 // a failed launch fails the rows it would have served
                 sv->error = rc;
