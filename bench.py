@@ -65,11 +65,12 @@ def parse():
     ap.add_argument("--profile-case", type=int, default=0,
                     help="run only N patterns through the chosen form a few times (for ncu)")
     ap.add_argument("--profile-target", default="fused",
-                    choices=["fused", "cluster", "homography", "ingest"],
+                    choices=["fused", "cluster", "homography", "ingest", "inplace"],
                     help="profile case: the detector's fused kernel; the 256-point cluster kernel "
                          "(1024^2, 6 x 6 ROIs of 128^2); the deformation fit (N patterns x 100 ROIs); "
                          "N detector patterns from pinned host memory through submit/wait, copied "
-                         "and then gathered, three batches of 32 in flight")
+                         "and then gathered, three batches of 32 in flight; the fused kernel reading N "
+                         "pinned host detector patterns in place (cp.async staging)")
     ap.add_argument("--no-plain", action="store_true", help="skip the plain-form comparison")
     ap.add_argument("--sample-seconds", type=float, default=0.0,
                     help="reference arm: seconds of host work per step (default: ~20 s in all)")
@@ -524,6 +525,26 @@ def run_profile_target(args):
     __graft_entry__.build_library()
     from emida_gb300 import DeviceBuffer, GpuOffset, _lib, pinned_array, synth
     n = args.profile_case
+    if args.profile_target == "inplace":
+        ref, uniq, begins = workload()
+        host = pinned_array((n, 1024, 1024))
+        host[:] = np.resize(uniq, (n, 1024, 1024))
+        g = GpuOffset((1024, 1024), begins, (64, 64), (127, 127), 32, "fft", 5, 1, "float",
+                      np.uint16, "fused")
+        g.allocate_memory(ref)
+        o = DeviceBuffer(n * len(begins) * 16)
+        for _ in range(3):
+            g.run_device(host.ctypes.data, n, o)
+        _lib.call("emida_gb_synchronize")
+        t0 = time.perf_counter()
+        for _ in range(3):
+            g.run_device(host.ctypes.data, n, o)
+        _lib.call("emida_gb_synchronize")
+        ms = (time.perf_counter() - t0) * 1000 / 3
+        print(json.dumps({"profile_target": "inplace", "patterns": n, "ms": ms,
+                          "pairs_per_s": n * len(begins) / (ms / 1000)}))
+        g.close()
+        return
     if args.profile_target == "ingest":
         ref, uniq, begins = workload()
         host = pinned_array((n, 1024, 1024))
