@@ -613,6 +613,7 @@ int emida_gb_create(const emida_gb_params *p, emida_gb_handle **out)
 
 int emida_gb_set_reference(emida_gb_handle *h, const void *ref)
 {
+    trace_range tr("emida_gb_set_reference");
     if (!h || !ref) return fail(EMIDA_GB_INVALID_ARGUMENT, "null argument");
     std::lock_guard<std::mutex> lk(h->mu);
     const size_t pat_bytes = (size_t)h->src.x * h->src.y * h->in_elem;
@@ -637,6 +638,7 @@ int emida_gb_set_reference(emida_gb_handle *h, const void *ref)
 
 int emida_gb_transfer_async(emida_gb_handle *h, const void *batch, uint32_t *buffer_index)
 {
+    trace_range tr("emida_gb_transfer_async");
     if (!h || !batch) return fail(EMIDA_GB_INVALID_ARGUMENT, "null argument");
     const uint32_t i = h->in_next.fetch_add(1) % (uint32_t)h->d_in.size();
     CKS(copy_patterns(h, h->d_in[i], batch, h->B, h->in_stream));
@@ -648,6 +650,7 @@ int emida_gb_transfer_async(emida_gb_handle *h, const void *batch, uint32_t *buf
 int emida_gb_offsets_core(emida_gb_handle *h, uint32_t buffer_index, void *maxes_out,
                           void *neigh_out)
 {
+    trace_range tr("emida_gb_offsets_core");
     if (!h) return fail(EMIDA_GB_INVALID_ARGUMENT, "null handle");
     if (buffer_index >= h->d_in.size()) return fail(EMIDA_GB_INVALID_ARGUMENT, "bad buffer index");
     if (!h->ref_set) return fail(EMIDA_GB_INVALID_ARGUMENT, "reference pattern not set");
@@ -668,6 +671,7 @@ int emida_gb_offsets_core(emida_gb_handle *h, uint32_t buffer_index, void *maxes
 int emida_gb_finalize(emida_gb_handle *h, const void *maxes, const void *neigh, double *offsets,
                       double *coefs)
 {
+    trace_range tr("emida_gb_finalize");
     if (!h || !maxes || !neigh || !offsets) return fail(EMIDA_GB_INVALID_ARGUMENT, "null argument");
     CK(cudaStreamSynchronize(h->out_stream));
     CKS(check_device_error(h));
@@ -703,6 +707,7 @@ int emida_gb_finalize(emida_gb_handle *h, const void *maxes, const void *neigh, 
 int emida_gb_get_offset(emida_gb_handle *h, const void *batch, double *offsets, double *coefs,
                         uint32_t *peaks)
 {
+    trace_range tr("emida_gb_get_offset");
     if (!h || !batch || !offsets) return fail(EMIDA_GB_INVALID_ARGUMENT, "null argument");
     if (!h->ref_set) return fail(EMIDA_GB_INVALID_ARGUMENT, "reference pattern not set");
     std::lock_guard<std::mutex> lk(h->mu);
@@ -753,6 +758,7 @@ static int ring_init(emida_gb_handle *h)
 
 int emida_gb_submit(emida_gb_handle *h, const void *batch, uint32_t patterns, uint64_t *ticket)
 {
+    trace_range tr("emida_gb_submit");
     if (!h || !batch || !ticket) return fail(EMIDA_GB_INVALID_ARGUMENT, "null argument");
     if (patterns == 0 || patterns > h->B)
         return fail(EMIDA_GB_INVALID_ARGUMENT, "patterns must be in [1, batch_size]");
@@ -825,6 +831,7 @@ int emida_gb_submit(emida_gb_handle *h, const void *batch, uint32_t patterns, ui
 int emida_gb_wait(emida_gb_handle *h, uint64_t ticket, double *offsets, double *coefs,
                   uint32_t *peaks)
 {
+    trace_range tr("emida_gb_wait");
     if (!h || !offsets) return fail(EMIDA_GB_INVALID_ARGUMENT, "null argument");
     emida_gb_handle::slot *r = nullptr;
     {
@@ -852,6 +859,7 @@ int emida_gb_run_device(emida_gb_handle *h, const void *dev_patterns, uint32_t p
                         double *dev_offsets, double *dev_coefs, void *dev_maxes, void *dev_neigh,
                         void *stream)
 {
+    trace_range tr("emida_gb_run_device");
     if (!h || !dev_patterns || !dev_offsets) return fail(EMIDA_GB_INVALID_ARGUMENT, "null argument");
     if (!h->ref_set) return fail(EMIDA_GB_INVALID_ARGUMENT, "reference pattern not set");
     bool on_device = true;

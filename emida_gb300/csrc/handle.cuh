@@ -3,6 +3,7 @@
 #pragma once
 
 #include <cuda.h>
+#include <nvtx3/nvToolsExt.h>
 
 #include <atomic>
 #include <cstdint>
@@ -20,6 +21,16 @@ struct emida_gb_handle;
 
 namespace emida_gb {
 namespace host {
+
+// An NVTX range over a scope, for timeline tools (nsys, ncu's range replay):
+// the entry points of the C ABI and the request loop's stages are named after
+// themselves.  Without a tool attached the calls do nothing.
+struct trace_range {
+    explicit trace_range(const char *name) { nvtxRangePushA(name); }
+    ~trace_range() { nvtxRangePop(); }
+    trace_range(const trace_range &) = delete;
+    trace_range &operator=(const trace_range &) = delete;
+};
 
 // Records the message for emida_gb_last_error() and returns `code`.
 int fail(int code, const char *fmt, ...);

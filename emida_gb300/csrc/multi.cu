@@ -448,6 +448,7 @@ int emida_gb_multi_run(emida_gb_multi *m, const void *dev_patterns, uint32_t pat
                        const uint32_t *layout_of, double *dev_offsets, double *dev_coefs,
                        void *dev_maxes, int use_graph)
 {
+    trace_range tr("emida_gb_multi_run");
     if (!m || !dev_patterns || !layout_of || !dev_offsets)
         return fail(EMIDA_GB_INVALID_ARGUMENT, "null argument");
     std::lock_guard<std::mutex> lk(m->mu);
@@ -496,6 +497,7 @@ int emida_gb_multi_run_slots(emida_gb_multi *m, const void *dev_patterns, uint32
                              uint32_t patterns, const uint32_t *slots, const uint32_t *layout_of,
                              double *dev_offsets, double *dev_coefs, void *dev_maxes)
 {
+    trace_range tr("emida_gb_multi_run_slots");
     if (!m || !dev_patterns || !slots || !layout_of || !dev_offsets)
         return fail(EMIDA_GB_INVALID_ARGUMENT, "null argument");
     std::lock_guard<std::mutex> lk(m->mu);
@@ -511,6 +513,7 @@ int emida_gb_multi_run_table(emida_gb_multi *m, const void *const *patterns, uin
                              const uint32_t *layout_of, double *dev_offsets, double *dev_coefs,
                              void *dev_maxes)
 {
+    trace_range tr("emida_gb_multi_run_table");
     if (!m || !patterns || !layout_of || !dev_offsets)
         return fail(EMIDA_GB_INVALID_ARGUMENT, "null argument");
     for (uint32_t p = 0; p < n; ++p) {

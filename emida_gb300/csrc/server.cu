@@ -247,6 +247,7 @@ int launch_step(emida_gb_server *sv, pool &p, step &st, bool other_busy)
         budget -= take;
     }
     if (st.parts.empty()) return EMIDA_GB_OK;
+    trace_range tr("server step");
     // sized once for the largest step this pool can build (a regrow frees
     // device memory, which waits for the whole device)
     CKS(ensure_step_buffers(st, std::max<size_t>(st.rois, (size_t)sv->step_patterns * p.max_rois)));
@@ -269,6 +270,7 @@ int launch_step(emida_gb_server *sv, pool &p, step &st, bool other_busy)
 // Hands a finished step's results to its rows; frees their arena slots.
 void retire_step(emida_gb_server *sv, pool &p, step &st)
 {
+    trace_range tr("server retire");
     for (const auto &part : st.parts) {
         request *r = part.r;
         const size_t n = (size_t)part.count * r->rois;
