@@ -128,6 +128,59 @@ template <int DIR, typename C> struct rdft<1, DIR, C> {
     static __device__ __forceinline__ void run(C *) {}
     static __device__ __forceinline__ void run_half(C *) {}
 };
+// Lengths 3 * M with M = 2, 4, 8 (6, 12, 24): the Good-Thomas prime-factor
+// algorithm, which needs no twiddles between its 3-point and M-point passes.
+// Input n = (M n1 + 3 n2) mod L goes to row n1 (3-point DFTs along n1), and
+// output k = (A k1 + B k2) mod L comes from k1 of the 3-point pass and k2 of
+// the M-point pass, A = M (M^-1 mod 3), B = 3 (3^-1 mod M): then
+// W_L^(n k) = W_3^(n1 k1) W_M^(n2 k2).
+template <int M, int DIR, typename C> struct pfa3 {
+    static constexpr int L = 3 * M;
+    static constexpr int inv_mod(int a, int m)
+    {
+        for (int x = 1; x < m; ++x)
+            if ((a * x) % m == 1) return x;
+        return 1;
+    }
+    static constexpr int A = M * inv_mod(M % 3, 3);
+    static constexpr int B = 3 * inv_mod(3 % M, M);
+    static __device__ __forceinline__ void run(C *a);
+};
+template <int L, int DIR, typename C> struct rdft;
+template <int M, int DIR, typename C> __device__ __forceinline__ void pfa3<M, DIR, C>::run(C *a)
+{
+    C y[3][M];
+#pragma unroll
+    for (int n2 = 0; n2 < M; ++n2) {
+        C t[3];
+#pragma unroll
+        for (int n1 = 0; n1 < 3; ++n1) t[n1] = a[(M * n1 + 3 * n2) % L];
+        rdft<3, DIR, C>::run(t);
+#pragma unroll
+        for (int k1 = 0; k1 < 3; ++k1) y[k1][n2] = t[k1];
+    }
+#pragma unroll
+    for (int k1 = 0; k1 < 3; ++k1) {
+        rdft<M, DIR, C>::run(y[k1]);
+#pragma unroll
+        for (int k2 = 0; k2 < M; ++k2) a[(A * k1 + B * k2) % L] = y[k1][k2];
+    }
+}
+#define EMIDA_GB_PFA3(LEN, M)                                                              \
+    template <int DIR, typename C> struct rdft<LEN, DIR, C> {                              \
+        static __device__ __forceinline__ void run(C *a) { pfa3<M, DIR, C>::run(a); }      \
+        static __device__ __forceinline__ void run_half(C *a)                              \
+        {                                                                                  \
+            using T = decltype(C::x);                                                      \
+            _Pragma("unroll") for (int n = LEN / 2; n < LEN; ++n) a[n] = cmake<C>((T)0, (T)0); \
+            pfa3<M, DIR, C>::run(a);                                                       \
+        }                                                                                  \
+    };
+EMIDA_GB_PFA3(6, 2)
+EMIDA_GB_PFA3(12, 4)
+EMIDA_GB_PFA3(24, 8)
+#undef EMIDA_GB_PFA3
+
 // Length 3: X0 = a0 + s, X1,2 = a0 - s/2 +- DIR i (sqrt(3)/2) d, s = a1 + a2, d = a1 - a2.
 template <int DIR, typename C> struct rdft<3, DIR, C> {
     static __device__ __forceinline__ void run(C *a)
