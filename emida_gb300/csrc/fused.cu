@@ -128,6 +128,47 @@ __device__ __forceinline__ void better(T &bv, uint32_t &bi, T v, uint32_t i)
 
 }  // namespace
 
+// The conj product of column c of the spectrum (held in v, E values per lane
+// of the 8- or 4-lane group) with its reference column, in place.  `first`:
+// warp 0 in its first column round, whose column 0 packs the DC and Nyquist
+// columns.
+template <int N, int G, typename T>
+__device__ __forceinline__ void conj_product(cplx<T> *v, cplx<T> *S, const cplx<T> *R, int c, int t,
+                                             bool first)
+{
+    using C = cplx<T>;
+    constexpr int E = N / G, SL = N / 2;
+    const C *Rc = R + (size_t)c * N;
+    if (first) {
+        // This warp holds column 0, whose slot packs the DC and Nyquist
+        // columns: unpack X[ky] with its mirror X[N-ky], multiply each
+        // half by its own reference column, repack.  The exchange goes
+        // through the warp's columns with full-warp syncs.
+#pragma unroll
+        for (int j = 0; j < E; ++j) *sp<N>(S, t + G * j, c) = v[j];
+        __syncwarp();
+#pragma unroll
+        for (int j = 0; j < E; ++j) {
+            const int ky = t + G * j;
+            if (c == 0) {
+                C x = v[j];
+                C xm = *sp<N>(S, ky == 0 ? 0 : N - ky, 0);
+                C p0 = cmake<C>((x.x + xm.x) * (T)0.5, (x.y - xm.y) * (T)0.5);
+                C p64 = cmake<C>((x.y + xm.y) * (T)0.5, (xm.x - x.x) * (T)0.5);
+                C q0 = cmulc(p0, __ldg(R + ky));
+                C q64 = cmulc(p64, __ldg(R + (size_t)SL * N + ky));
+                v[j] = cmake<C>(q0.x - q64.y, q0.y + q64.x);
+            } else {
+                v[j] = cmulc(v[j], __ldg(Rc + ky));
+            }
+        }
+        __syncwarp();
+    } else {
+#pragma unroll
+        for (int j = 0; j < E; ++j) v[j] = cmulc(v[j], __ldg(Rc + t + G * j));
+    }
+}
+
 // Resident CTAs per SM the register budget is sized for (shared memory allows
 // as many): FP32 128-point and 192-point transforms are register-heavy.
 __host__ __device__ constexpr int fused_min_blocks(int N, int tsize)
@@ -398,37 +439,29 @@ __global__ void __launch_bounds__(N * G / 4, fused_min_blocks(N, sizeof(T)))
 #pragma unroll
             for (int m = 0; m < E / 2; ++m) v[m] = *sp<N>(S, t + G * m, c);
             col_line<N, C> line{S, c};
-            group_fft<N, -1, true, T, G>(v, t, line, twf);
-            const C *Rc = R + (size_t)c * N;
-            if (warp == 0 && rnd == 0) {
-                // This warp holds column 0, whose slot packs the DC and Nyquist
-                // columns: unpack X[ky] with its mirror X[N-ky], multiply each
-                // half by its own reference column, repack.  The exchange goes
-                // through the warp's columns with full-warp syncs.
+            if constexpr (E % 3 != 0) {
+                group_fft<N, -1, true, T, G>(v, t, line, twf);
+                conj_product<N, G, T>(v, S, R, c, t, warp == 0 && rnd == 0);
+                group_fft<N, +1, false, T, G>(v, t, line, twi);
+            } else {
+                // Prime-factor lengths gain nothing from the zero half of the
+                // input, so both transforms run one copy of the code: the
+                // inverse as conj(forward(conj(.))), exact in floating point.
+                // Half the column code keeps the loop in the instruction cache.
 #pragma unroll
-                for (int j = 0; j < E; ++j) *sp<N>(S, t + G * j, c) = v[j];
-                __syncwarp();
+                for (int m = E / 2; m < E; ++m) v[m] = cmake<C>((T)0, (T)0);
+#pragma unroll 1
+                for (int pass = 0; pass < 2; ++pass) {
+                    group_fft<N, -1, false, T, G>(v, t, line, twf);
+                    if (pass == 0) {
+                        conj_product<N, G, T>(v, S, R, c, t, warp == 0 && rnd == 0);
 #pragma unroll
-                for (int j = 0; j < E; ++j) {
-                    const int ky = t + G * j;
-                    if (c == 0) {
-                        C x = v[j];
-                        C xm = *sp<N>(S, ky == 0 ? 0 : N - ky, 0);
-                        C p0 = cmake<C>((x.x + xm.x) * (T)0.5, (x.y - xm.y) * (T)0.5);
-                        C p64 = cmake<C>((x.y + xm.y) * (T)0.5, (xm.x - x.x) * (T)0.5);
-                        C q0 = cmulc(p0, __ldg(R + ky));
-                        C q64 = cmulc(p64, __ldg(R + (size_t)SL * N + ky));
-                        v[j] = cmake<C>(q0.x - q64.y, q0.y + q64.x);
-                    } else {
-                        v[j] = cmulc(v[j], __ldg(Rc + ky));
+                        for (int j = 0; j < E; ++j) v[j].y = -v[j].y;
                     }
                 }
-                __syncwarp();
-            } else {
 #pragma unroll
-                for (int j = 0; j < E; ++j) v[j] = cmulc(v[j], __ldg(Rc + t + G * j));
+                for (int j = 0; j < E; ++j) v[j].y = -v[j].y;
             }
-            group_fft<N, +1, false, T, G>(v, t, line, twi);
 #pragma unroll
             for (int j = 0; j < E; ++j) *sp<N>(S, t + G * j, c) = v[j];
         }
