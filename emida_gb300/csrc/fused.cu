@@ -31,10 +31,17 @@ namespace {
 // slot offsets, and its neighbour group's column (c + 1) the odd ones.  Two
 // groups' row accesses (rows 8w + 2g' + e) land in different 8-slot halves.
 // So every half-warp access covers 16 distinct 8-byte slots.
+//
+// The 96-point kernel's FFT groups are 4 lanes wide, so a half-warp holds four
+// groups: its column accesses cover 4 rows of 4 adjacent columns, its row
+// accesses the same slots of rows 2g and 2g + 1 of four groups g.  There
+// f = 4 ((row ^ row >> 1) mod 4) gives each of those 4 rows its own 4-slot
+// block.  Both forms change slot bits 1-3 only, so a slot stays in its row.
 template <int N, typename C>
 __device__ __forceinline__ C *sp(C *S, int row, int slot)
 {
-    const int f = ((row & 1) << 1) | (row & 4) | ((row & 2) << 2);
+    const int f = N == 96 ? ((row ^ (row >> 1)) & 3) << 2
+                          : ((row & 1) << 1) | (row & 4) | ((row & 2) << 2);
     return S + row * (N / 2) + (slot ^ f);
 }
 
