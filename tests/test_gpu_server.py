@@ -102,3 +102,24 @@ def test_row_larger_than_arena_is_refused(world):
     with pytest.raises(EmidaError, match="exceeds"):
         s.submit(lid, big)
     s.close()
+
+
+def test_long_copied_row_equals_its_patterns_alone(world):
+    # a copied row longer than the copy window (8 chunks of 16 patterns): its
+    # copies are queued over many rounds of the loop while steps of it run
+    from emida_gb300 import Server, synth
+    sizes, layouts, _ = world
+    lid = next(i for i, l in enumerate(layouts) if l[0] == 256)
+    w, begins, side, fs = layouts[lid]
+    pics, _ = synth.deformed_patterns(256, 32, 30, 3e-3, first=200)
+    long_row = np.ascontiguousarray(np.tile(pics, (10, 1, 1)))  # 300 pageable patterns: copied
+    s = Server("float", hbm_bytes=512 * 256 * 256 * 2, step_patterns=64)
+    ids = [s.add_layout((l[0], l[0]), l[1], l[2], l[3], sizes[l[0]]) for l in layouts]
+    alone_offs, alone_coefs, _ = s.wait(s.submit(ids[lid], pics))
+    offs, coefs, _ = s.wait(s.submit(ids[lid], long_row))
+    n = len(begins)
+    assert offs.shape == (300 * n, 2)
+    for k in range(10):
+        sl = slice(30 * n * k, 30 * n * (k + 1))
+        assert np.array_equal(offs[sl], alone_offs) and np.array_equal(coefs[sl], alone_coefs)
+    s.close()
