@@ -771,7 +771,6 @@ int emida_gb_submit(emida_gb_handle *h, const void *batch, uint32_t patterns, ui
     if (r.busy)
         return fail(EMIDA_GB_INVALID_ARGUMENT, "all %zu slots in flight: wait for ticket %llu first",
                     h->ring.size(), (unsigned long long)r.ticket);
-    const size_t bytes = (size_t)h->src.x * h->src.y * h->in_elem * patterns;
     cudaPointerAttributes pa{};
     CK(cudaPointerGetAttributes(&pa, batch));
     // device batches are used in place; pinned host batches are copied or read
