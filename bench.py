@@ -56,7 +56,7 @@ TRAFFIC_PER_LAUNCH = 6.66e6
 def parse():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
-    ap.add_argument("--steps", type=int, default=20)
+    ap.add_argument("--steps", type=int, default=100)
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--precision", default="float", choices=["float", "double"])
@@ -102,7 +102,11 @@ def workload(seed=2024):
 
 
 class ClockSampler:
-    """nvidia-smi clocks and throttle reasons during the timed region."""
+    """nvidia-smi clocks and throttle reasons during the timed region (the body
+    of the `with`): samples every 20 ms, read with their arrival times by a
+    thread; the region starts only once the first sample has arrived, and only
+    samples that arrive inside it (or the first one after it, for a region
+    shorter than the sampling interval) are summarised."""
 
     FIELDS = ("clocks.sm,clocks.max.sm,clocks_event_reasons.hw_slowdown,"
               "clocks_event_reasons.hw_thermal_slowdown,clocks_event_reasons.sw_thermal_slowdown,"
@@ -111,33 +115,50 @@ class ClockSampler:
     def __init__(self, index=0):
         self.index = index
         self.proc = None
+        self.stamped = []
+        self.lines = []
+
+    def _read(self):
+        for line in self.proc.stdout:
+            if line.strip():
+                self.stamped.append((time.perf_counter(), line.strip()))
 
     def __enter__(self):
         try:
             self.proc = subprocess.Popen(
                 ["nvidia-smi", "-i", str(self.index), f"--query-gpu={self.FIELDS}",
-                 "--format=csv,noheader,nounits", "-lms", "200"],
+                 "--format=csv,noheader,nounits", "-lms", "20"],
                 stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
         except OSError:
             self.proc = None
+        if self.proc:
+            self.reader = threading.Thread(target=self._read, daemon=True)
+            self.reader.start()
+            deadline = time.perf_counter() + 5.0
+            while not self.stamped and time.perf_counter() < deadline and self.proc.poll() is None:
+                time.sleep(0.005)
+        self.t0 = time.perf_counter()
         return self
 
     def __exit__(self, *exc):
-        self.lines = []
+        t1 = time.perf_counter()
         if self.proc:
-            time.sleep(0.3)
+            time.sleep(0.05)
             self.proc.terminate()
             try:
-                out, _ = self.proc.communicate(timeout=5)
+                self.proc.wait(timeout=5)
             except subprocess.TimeoutExpired:
                 self.proc.kill()
-                out, _ = self.proc.communicate()
-            self.lines = [l for l in out.splitlines() if l.strip()]
+                self.proc.wait()
+            self.reader.join(timeout=5)
+            inside = [l for t, l in self.stamped if self.t0 <= t <= t1]
+            after = [l for t, l in self.stamped if t > t1]
+            self.lines = inside or after[:1]
 
     def summary(self):
         sm, mx, reasons = [], None, set()
         names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
-        for l in getattr(self, "lines", []):
+        for l in self.lines:
             parts = [p.strip() for p in l.split(",")]
             if len(parts) < 6:
                 continue
