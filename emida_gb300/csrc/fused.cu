@@ -333,6 +333,12 @@ __global__ void __launch_bounds__(N * G / 4, fused_min_blocks(N, sizeof(T)))
     if (tma && tid == 0 && blockIdx.x < a.n_pairs) issue_tile(blockIdx.x);
     if (cpa && blockIdx.x < a.n_pairs) issue_chunks(blockIdx.x);
 
+    // uint16 tiles staged ahead (TMA or cp.async): warps 1..WARPS-1 sum the next
+    // pair's tile while warp 0 finishes the current pair, so the next pair
+    // starts from their partial sums without a summing pass and its barrier
+    const bool sum_ahead = U16 && (tma || cpa);
+    uint32_t *red_u = reinterpret_cast<uint32_t *>(red_s);  // next tile's partial sums
+    bool summed = false;  // this pair's tile was summed ahead (uniform over the CTA)
     uint32_t iter = 0;
     for (uint32_t pair = blockIdx.x; pair < a.n_pairs; pair += gridDim.x, ++iter) {
         const uint4 it = item(pair);
@@ -358,16 +364,21 @@ __global__ void __launch_bounds__(N * G / 4, fused_min_blocks(N, sizeof(T)))
                     for (int x = lane; x < side; x += 32) t16[r * TW + xo + x] = src[(size_t)r * a.src_w + x];
                 __syncthreads();
             }
-            uint32_t acc = 0;  // exact, so any summation order gives the same total
-            for (int r = tid >> 2; r < side; r += THREADS >> 2)
-                for (int x = tid & 3; x < side; x += 4) acc += t16[r * TW + xo + x];
+            uint32_t total = 0;  // exact, so any summation order gives the same total
+            if (summed) {
 #pragma unroll
-            for (int o = 16; o; o >>= 1) acc += __shfl_xor_sync(0xffffffffu, acc, o);
-            if (lane == 0) red_i[warp] = acc;
-            __syncthreads();
-            uint32_t total = 0;
+                for (int w = 1; w < WARPS; ++w) total += red_u[w];
+            } else {
+                uint32_t acc = 0;
+                for (int r = tid >> 2; r < side; r += THREADS >> 2)
+                    for (int x = tid & 3; x < side; x += 4) acc += t16[r * TW + xo + x];
 #pragma unroll
-            for (int w = 0; w < WARPS; ++w) total += red_i[w];
+                for (int o = 16; o; o >>= 1) acc += __shfl_xor_sync(0xffffffffu, acc, o);
+                if (lane == 0) red_i[warp] = acc;
+                __syncthreads();
+#pragma unroll
+                for (int w = 0; w < WARPS; ++w) total += red_i[w];
+            }
             mean = (T)total / (T)(side * side);
         } else {
             const double *src = reinterpret_cast<const double *>(pattern_base(pic)) +
@@ -569,6 +580,21 @@ __global__ void __launch_bounds__(N * G / 4, fused_min_blocks(N, sizeof(T)))
             const bool last = pair + gridDim.x >= a.n_pairs;
             if (slot == 31 || last) fit_batch<T>(a, fbuf, fmeta, fval, (int)slot + 1, lane, N - 1);
         }
+        const bool ahead = sum_ahead && pair + gridDim.x < a.n_pairs;
+        if (ahead && warp != 0) {
+            // the next tile was requested after this pair's row pass: wait for it
+            // and sum it over the other warps' threads
+            if (!mbar_wait(bar, (iter + 1) & 1)) atomicOr(a.err, DEV_ERR_TMA_TIMEOUT);
+            const int nxo = (int)(a.begins[item(pair + gridDim.x).y].x & 7u);
+            const int u = tid - 32;
+            uint32_t acc = 0;
+            for (int r = u >> 2; r < side; r += (THREADS - 32) >> 2)
+                for (int x = u & 3; x < side; x += 4) acc += t16[r * TW + nxo + x];
+#pragma unroll
+            for (int o = 16; o; o >>= 1) acc += __shfl_xor_sync(0xffffffffu, acc, o);
+            if (lane == 0) red_u[warp] = acc;
+        }
+        summed = ahead;
         __syncthreads();
     }
 }
