@@ -120,8 +120,9 @@ int emida_gb_wait(emida_gb_handle *h, uint64_t ticket, double *offsets, double *
 
 /* Device-resident form for pipelines and benchmarks: `patterns` whole
  * patterns (any count, not limited to batch_size) already in device memory,
- * or in pinned host memory that the kernels read in place (only the ROI
- * pixels cross the host link), results to device memory, all on `stream`
+ * or in pinned host memory that the kernels read in place (only the 16-byte
+ * chunks that hold ROI pixels cross the host link), results to device memory,
+ * all on `stream`
  * (NULL: the handle's compute stream), no synchronisation.  Pageable host
  * memory is refused (EMIDA_GB_INVALID_ARGUMENT).  coefs, maxes, neigh may be
  * NULL. */
