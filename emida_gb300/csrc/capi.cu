@@ -16,6 +16,7 @@
 #include "deformation.cuh"
 #include "fft.cuh"
 #include "handle.cuh"
+#include "ptx.cuh"
 
 using namespace emida_gb;
 using namespace emida_gb::host;
@@ -1032,6 +1033,38 @@ int emida_gb_synchronize(void)
 {
     CK(cudaDeviceSynchronize());
     return EMIDA_GB_OK;
+}
+
+}  // extern "C"
+
+namespace {
+
+// One warp waits on phase 0 of an mbarrier that expects one arrival and gets
+// none: the bounded wait gives up after `budget` cycles and records it.
+__global__ void k_selftest_wait(uint32_t *err, long long budget)
+{
+    __shared__ __align__(8) uint64_t bar;
+    if (threadIdx.x == 0) emida_gb::ptx::mbar_init(&bar, 1);
+    __syncthreads();
+    const bool done = emida_gb::ptx::mbar_wait_for(&bar, 0, budget);
+    if (!done && threadIdx.x == 0) atomicOr(err, DEV_ERR_WAIT_TIMEOUT);
+    __syncthreads();
+}
+
+}  // namespace
+
+extern "C" {
+
+int emida_gb_selftest_bounded_wait(emida_gb_handle *h, int64_t budget_cycles)
+{
+    if (!h) return fail(EMIDA_GB_INVALID_ARGUMENT, "null handle");
+    if (budget_cycles < 1 || budget_cycles > 4000000000LL)
+        return fail(EMIDA_GB_INVALID_ARGUMENT, "budget must be in [1, 4e9] cycles");
+    std::lock_guard<std::mutex> lk(h->mu);
+    k_selftest_wait<<<1, 32, 0, h->comp>>>(h->d_err, (long long)budget_cycles);
+    CK(cudaGetLastError());
+    CK(cudaStreamSynchronize(h->comp));
+    return check_device_error(h);
 }
 
 // ---- per-stage launchers --------------------------------------------------------

@@ -25,10 +25,9 @@ __device__ __forceinline__ void mbar_arrive(uint64_t *bar)
 }
 
 // Waits until the phase with parity `parity` of `bar` has completed, for at
-// most about two seconds; returns false when that budget ran out.
-__device__ __forceinline__ bool mbar_wait(uint64_t *bar, uint32_t parity)
+// most `budget` SM clock cycles; returns false when that budget ran out.
+__device__ __forceinline__ bool mbar_wait_for(uint64_t *bar, uint32_t parity, long long budget)
 {
-    const long long budget = 4000000000LL;
     const long long start = clock64();
     while (true) {
         uint32_t done;
@@ -41,6 +40,12 @@ __device__ __forceinline__ bool mbar_wait(uint64_t *bar, uint32_t parity)
         if (done) return true;
         if (clock64() - start > budget) return false;
     }
+}
+
+// The same with a budget of about two seconds.
+__device__ __forceinline__ bool mbar_wait(uint64_t *bar, uint32_t parity)
+{
+    return mbar_wait_for(bar, parity, 4000000000LL);
 }
 
 // Makes this thread's generic-proxy shared-memory writes visible to the async

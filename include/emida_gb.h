@@ -283,6 +283,13 @@ int emida_gb_memcpy_d2d(void *dev_dst, const void *dev_src, size_t bytes);
 int emida_gb_malloc_host(void **host_ptr, size_t bytes);
 int emida_gb_free_host(void *host_ptr);
 int emida_gb_synchronize(void);
+/* Self-test of the bounded waits every device spin loop uses: one warp waits
+ * on an mbarrier phase that nothing completes, for about `budget_cycles` SM
+ * clock cycles (at most 4e9, ~2 s).  The wait runs out, sets the handle's
+ * device error word, and the call returns what a real timeout returns:
+ * EMIDA_GB_DEVICE_CHECK, "pipeline wait ran out".  The context and the
+ * handle stay usable; the error word is cleared.  No reference counterpart. */
+int emida_gb_selftest_bounded_wait(emida_gb_handle *h, int64_t budget_cycles);
 /* CUDA-event timing on a stream: elapsed ms of `repeats` runs of the handle's
  * device form over the same inputs, measured on the launching stream. */
 int emida_gb_time_device(emida_gb_handle *h, const void *dev_patterns, uint32_t patterns,
