@@ -65,14 +65,14 @@ def parse():
     ap.add_argument("--profile-case", type=int, default=0,
                     help="run only N patterns through the chosen form a few times (for ncu)")
     ap.add_argument("--profile-target", default="fused",
-                    choices=["fused", "cluster", "homography", "ingest", "inplace", "fused96",
-                             "fused192"],
+                    choices=["fused", "cluster", "homography", "ingest", "inplace", "fused64",
+                             "fused96", "fused192"],
                     help="profile case: the detector's fused kernel; the 256-point cluster kernel "
                          "(1024^2, 6 x 6 ROIs of 128^2); the deformation fit (N patterns x 100 ROIs); "
                          "N detector patterns from pinned host memory through submit/wait, copied "
                          "and then gathered, three batches of 32 in flight; the fused kernel reading N "
-                         "pinned host detector patterns in place (cp.async staging); the 96- and "
-                         "192-point fused kernels (1024^2, 10 x 10 ROIs of 48^2 or 96^2)")
+                         "pinned host detector patterns in place (cp.async staging); the 64-, 96- "
+                         "and 192-point fused kernels (1024^2, 10 x 10 ROIs of 32^2, 48^2 or 96^2)")
     ap.add_argument("--no-plain", action="store_true", help="skip the plain-form comparison")
     ap.add_argument("--sample-seconds", type=float, default=0.0,
                     help="reference arm: seconds of host work per step (default: ~20 s in all)")
@@ -590,8 +590,8 @@ def run_profile_target(args):
         print(json.dumps(out))
         g.close()
         return
-    if args.profile_target in ("fused96", "fused192"):
-        side = 48 if args.profile_target == "fused96" else 96
+    if args.profile_target in ("fused64", "fused96", "fused192"):
+        side = {"fused64": 32, "fused96": 48, "fused192": 96}[args.profile_target]
         ref = synth.reference_pattern(1024, 5)
         uniq, _ = synth.deformed_patterns(1024, 5, 8, sigma_eps=5e-3)
         _, begins = synth.roi_grid(1024, 10, side // 2, margin=side // 2 + 8)

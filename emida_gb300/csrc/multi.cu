@@ -568,7 +568,7 @@ int emida_gb_multi_autotune(emida_gb_multi *m, const void *dev_patterns, uint32_
         if (!k.fused || pl.items[c].empty()) continue;
         float best = 1e30f;
         int best_grid = 0;
-        for (int per_sm = 1; per_sm <= 4; ++per_sm) {
+        for (int per_sm = 1; per_sm <= 6; ++per_sm) {
             const int grid = per_sm * sms;
             CKS(launch_plan(m, pl, ws, dev_patterns, patterns, dev_offsets, nullptr, nullptr, (int)c, grid));
             CK(cudaEventRecord(a, m->stream));
