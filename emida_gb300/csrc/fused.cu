@@ -466,8 +466,10 @@ __global__ void __launch_bounds__(N * G / 4, fused_min_blocks(N, sizeof(T)))
             } else {
                 // Prime-factor lengths gain nothing from the zero half of the
                 // input, so both transforms run one copy of the code: the
-                // inverse as conj(forward(conj(.))), exact in floating point.
-                // Half the column code keeps the loop in the instruction cache.
+                // inverse as conj(forward(conj(.))).  The negations are exact,
+                // so only the pairing of multiply-adds can differ from a direct
+                // inverse.  Half the column code keeps the loop in the
+                // instruction cache.
 #pragma unroll
                 for (int m = E / 2; m < E; ++m) v[m] = cmake<C>((T)0, (T)0);
 #pragma unroll 1
