@@ -68,7 +68,7 @@ def build(verbose=False, extra=()):
 def build_cli():
     """The `emida` command line (emida_gb300/cli), linked against the library."""
     src = os.path.join(HERE, "cli", "main.cpp")
-    deps = [src, os.path.join(HERE, "cli", "tiff.hpp"), LIB,
+    deps = [src, os.path.join(HERE, "cli", "tiff.hpp"), os.path.join(HERE, "cli", "text.hpp"), LIB,
             os.path.join(REPO, "include", "emida_gb", "gpu_offset.hpp")]
     if not _stale(CLI, deps):
         return CLI

@@ -29,6 +29,7 @@
 #include <vector>
 
 #include "../../include/emida_gb/gpu_offset.hpp"
+#include "text.hpp"
 #include "tiff.hpp"
 
 using namespace emida;
@@ -438,12 +439,14 @@ int process(const params &a)
     });
     // finalize stage (src/process_files.hpp:219-264)
     std::thread fin([&]() {
+        std::string text;  // one batch's lines, written at once
         for (esize_t b = 0; b < n_batches; ++b) {
             stopwatch fsw;
             auto f = done.pop();
             fsw.tick("Finalize wait");
             if (f->files == 0) continue;  // a batch that failed to load is skipped
             auto r = offs.finalize(f->maxes.data(), f->neigh.data());
+            text.reserve((size_t)f->files * S * (a.write_coefs ? 120 : 40));
             for (esize_t j = f->first; j < f->first + f->files; ++j) {
                 if (bin) {
                     // the same content, unrounded: pattern header, then one record per ROI
@@ -463,23 +466,40 @@ int process(const params &a)
                     }
                     continue;
                 }
-                printf("%f %f %llu %s\n", work[j].x, work[j].y, (unsigned long long)S,
-                       work[j].fname.c_str());
+                // "%f %f %llu %s\n", then per ROI "%lu %lu %f %f" (+ 6 x " %f" with -q)
+                using emida_cli::put_f;
+                using emida_cli::put_u;
+                put_f(text, work[j].x);
+                text += ' ';
+                put_f(text, work[j].y);
+                text += ' ';
+                put_u(text, (unsigned long long)S);
+                text += ' ';
+                text += work[j].fname;
+                text += '\n';
                 const esize_t it = j - f->first;
                 for (esize_t i = it * S; i < (it + 1) * S; ++i) {
                     const esize_t bi = i % S;
                     double ox = r.offsets[i].x, oy = r.offsets[i].y;
                     if (std::isnan(ox)) ox = std::numeric_limits<double>::quiet_NaN();
                     if (std::isnan(oy)) oy = std::numeric_limits<double>::quiet_NaN();
+                    put_u(text, (unsigned long)a.mids[bi].x);
+                    text += ' ';
+                    put_u(text, (unsigned long)a.mids[bi].y);
+                    text += ' ';
+                    put_f(text, ox);
+                    text += ' ';
+                    put_f(text, oy);
                     if (a.write_coefs)
-                        printf("%lu %lu %f %f %f %f %f %f %f %f\n", (unsigned long)a.mids[bi].x,
-                               (unsigned long)a.mids[bi].y, ox, oy, r.coefs[i][0], r.coefs[i][1],
-                               r.coefs[i][2], r.coefs[i][3], r.coefs[i][4], r.coefs[i][5]);
-                    else
-                        printf("%lu %lu %f %f\n", (unsigned long)a.mids[bi].x,
-                               (unsigned long)a.mids[bi].y, ox, oy);
+                        for (int k = 0; k < 6; ++k) {
+                            text += ' ';
+                            put_f(text, r.coefs[i][k]);
+                        }
+                    text += '\n';
                 }
             }
+            if (!text.empty()) fwrite(text.data(), 1, text.size(), stdout);
+            text.clear();
             fsw.tick("Finalize");
         }
     });
