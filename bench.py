@@ -79,10 +79,11 @@ def parse():
     ap.add_argument("--in-flight", type=int, default=3,
                     help="e2e: batches in flight through submit/wait (device input buffers)")
     ap.add_argument("--config", default="detector",
-                    choices=["detector", "batching", "serving", "precision"],
+                    choices=["detector", "batching", "serving", "precision", "cli"],
                     help="detector: 256 x 1024^2, 100 ROIs r=32 (default); batching: patterns on "
                          "uneven layouts; serving: Poisson stream of scan rows; precision: 2048 "
-                         "patterns, brute on the tensor cores beside the FP32 FFT")
+                         "patterns, brute on the tensor cores beside the FP32 FFT; cli: the emida "
+                         "command line from TIFF files to text")
     ap.add_argument("--rate", type=float, default=50.0, help="serving: rows per second")
     ap.add_argument("--duration", type=float, default=8.0, help="serving: seconds of arrivals")
     ap.add_argument("--layout", default="mixed", choices=["mixed", "detector"],
@@ -434,6 +435,65 @@ def run_serving(args):
     srv.close()
 
 
+def run_cli_config(args):
+    """The reference's command line end to end (src/main.cpp, src/process_files.hpp):
+    1024^2 16-bit TIFFs on tmpfs (16 distinct patterns listed in turn), 100 ROIs
+    of 64^2, FFT, float, fit 5, batch 32, 8 loader threads, text to /dev/null.
+    Each run is a whole process; the pattern rate comes from a long and a short
+    run, whose difference cancels the fixed start-up (CUDA context, reference
+    spectra)."""
+    import shutil
+    import tempfile
+    import __graft_entry__
+    __graft_entry__.build_library()  # the library and the command line
+    from emida_gb300 import synth
+    cli = os.path.join(ROOT, "emida_gb300", "bin", "emida")
+    tmp = tempfile.mkdtemp(dir="/dev/shm" if os.path.isdir("/dev/shm") else None)
+    try:
+        synth.write_tiff(os.path.join(tmp, "ref.tif"), synth.reference_pattern(1024, 7))
+        uniq, _ = synth.deformed_patterns(1024, 7, 16, sigma_eps=5e-3)
+        names = [os.path.join(tmp, f"def_{i}.tif") for i in range(16)]
+        for n, p in zip(names, uniq):
+            synth.write_tiff(n, p)
+        mids, _ = synth.roi_grid(1024, 10, 32, margin=40)
+        synth.write_roi_file(os.path.join(tmp, "roi.txt"), 32, mids)
+        long_n, short_n = 8192, 512
+        for n in (long_n, short_n):
+            synth.write_deformed_list(os.path.join(tmp, f"def_{n}.txt"),
+                                      [(float(i), 0.0, names[i % 16]) for i in range(n)])
+
+        def run(n, extra):
+            cmd = [cli, "-i", os.path.join(tmp, "ref.tif"), "-d", os.path.join(tmp, f"def_{n}.txt"),
+                   "-b", os.path.join(tmp, "roi.txt"), "--precision", "float", "-f", "5",
+                   "--crosspolicy", "fft", "--batchsize", "32", "--loadworkers", "8"] + extra
+            t0 = time.perf_counter()
+            r = subprocess.run(cmd, stdout=subprocess.DEVNULL, stderr=subprocess.PIPE, text=True)
+            if r.returncode != 0:
+                raise RuntimeError(r.stderr[-500:])
+            return time.perf_counter() - t0
+
+        out = {}
+        for key, extra in (("offsets", []), ("offsets_and_coefs", ["-q"])):
+            run(short_n, extra)  # page cache and driver warm
+            ts = statistics.median(run(short_n, extra) for _ in range(3))
+            tl = statistics.median(run(long_n, extra) for _ in range(3))
+            rate = (long_n - short_n) / (tl - ts)
+            out[key] = {"patterns_per_s": rate, "pairs_per_s": rate * len(mids),
+                        f"wall_s_{long_n}": tl, f"wall_s_{short_n}": ts,
+                        "startup_s": max(0.0, ts - short_n / rate)}
+    finally:
+        shutil.rmtree(tmp, ignore_errors=True)
+    print(json.dumps({
+        "metric": "patterns/s through the emida command line, TIFF files in, text out",
+        "value": out["offsets"]["patterns_per_s"], "unit": "patterns/s", "n_gpus": 1,
+        "higher_is_better": True, "dtype": "f32", "data": "synthetic",
+        "config": {"workload": "1024^2 uint16 TIFFs (16 distinct, listed in turn) on tmpfs, 100 ROIs "
+                               "of 64^2, --crosspolicy fft --precision float -f 5 --batchsize 32 "
+                               "--loadworkers 8, text to /dev/null",
+                   "patterns": [short_n, long_n]},
+        "runs": out}), flush=True)
+
+
 def run_precision(args):
     """2048 patterns of 1024^2, 100 ROIs r=32 (10 x 10 grid), fit size 7: the
     brute policy's 127 x 127-lag correlation as a BF16 hi/lo contraction on the
@@ -650,6 +710,8 @@ def main():
         return run_serving(args)
     if args.config == "precision":
         return run_precision(args)
+    if args.config == "cli":
+        return run_cli_config(args)
     if args.profile_case and args.profile_target != "fused":
         return run_profile_target(args)
 

@@ -94,3 +94,40 @@ def write_roi_file(path, radius, mids):
         f.write(f"{radius}\n")
         for x, y in mids:
             f.write(f"{int(x)} {int(y)}\n")
+
+
+def write_tiff(path, img, rows_per_strip=16):
+    """A little-endian, uncompressed, single-channel 16-bit TIFF in strips: the
+    kind the reference loads (src/load_tiff.hpp:14-53)."""
+    import struct
+    img = np.ascontiguousarray(img, dtype="<u2")
+    h, w = img.shape
+    data = img.tobytes()
+    strips = [data[r * w * 2:min(h, r + rows_per_strip) * w * 2] for r in range(0, h, rows_per_strip)]
+    n, entries = len(strips), 10
+    offs_at = 8 + 2 + 12 * entries + 4
+    counts_at = offs_at + 4 * n
+    pos, offsets = counts_at + 4 * n, []
+    for s in strips:
+        offsets.append(pos)
+        pos += len(s)
+
+    def ent(tag, typ, count, value):
+        if typ == 3 and count == 1:
+            return struct.pack("<HHIHH", tag, typ, count, value, 0)
+        return struct.pack("<HHII", tag, typ, count, value)
+
+    out = b"II" + struct.pack("<HI", 42, 8) + struct.pack("<H", entries)
+    out += ent(256, 4, 1, w) + ent(257, 4, 1, h) + ent(258, 3, 1, 16) + ent(259, 3, 1, 1)
+    out += ent(262, 3, 1, 1) + ent(273, 4, n, offs_at) + ent(274, 3, 1, 1) + ent(277, 3, 1, 1)
+    out += ent(278, 4, 1, rows_per_strip) + ent(279, 4, n, counts_at) + struct.pack("<I", 0)
+    out += struct.pack(f"<{n}I", *offsets) + struct.pack(f"<{n}I", *[len(s) for s in strips])
+    with open(path, "wb") as f:
+        f.write(out + b"".join(strips))
+
+
+def write_deformed_list(path, entries):
+    """The reference's --deformed list: 'x y path' lines (src/process_files.hpp:56-75)."""
+    with open(path, "w") as f:
+        for x, y, name in entries:
+            f.write(f"{x} {y} {name}\n")
