@@ -37,11 +37,17 @@ namespace {
 // accesses the same slots of rows 2g and 2g + 1 of four groups g.  There
 // f = 4 ((row ^ row >> 1) mod 4) gives each of those 4 rows its own 4-slot
 // block.  Both forms change slot bits 1-3 only, so a slot stays in its row.
+//
+// FP64 slots are 16 bytes, so an access is served per quarter-warp, one 8-lane
+// group, over 8 bank groups: f = row mod 8 gives a group's column access (8
+// rows of one column) 8 distinct slots mod 8, and leaves its row accesses
+// (consecutive slots) distinct.
 template <int N, typename C>
 __device__ __forceinline__ C *sp(C *S, int row, int slot)
 {
     const int f = N == 96 ? ((row ^ (row >> 1)) & 3) << 2
-                          : ((row & 1) << 1) | (row & 4) | ((row & 2) << 2);
+                  : sizeof(C) == 16 ? (row & 7)
+                                    : ((row & 1) << 1) | (row & 4) | ((row & 2) << 2);
     return S + row * (N / 2) + (slot ^ f);
 }
 
