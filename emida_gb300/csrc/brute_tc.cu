@@ -413,4 +413,9 @@ cudaError_t launch_brute_tc(const brute_tc_args &a, int grid, cudaStream_t st)
 
 size_t brute_tc_smem_bytes() { return L::bytes; }
 
+cudaError_t preload_brute_tc()
+{
+    return cudaFuncSetAttribute(brute_tc_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, L::bytes);
+}
+
 }  // namespace emida_gb

@@ -32,5 +32,7 @@ constexpr uint32_t BRUTE_TC_CROSS = 2 * BRUTE_TC_SIDE - 1;
 cudaError_t launch_brute_tc(const brute_tc_args &a, int grid, cudaStream_t st);
 // Dynamic shared memory of one CTA.
 size_t brute_tc_smem_bytes();
+// Loads the kernel without launching it (see preload_fused).
+cudaError_t preload_brute_tc();
 
 }  // namespace emida_gb

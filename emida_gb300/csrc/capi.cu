@@ -632,6 +632,9 @@ int emida_gb_set_reference(emida_gb_handle *h, const void *ref)
             CK(run_spec_to_colmajor(h->d_ref_spec, h->d_ref_spec_cm, h->S, h->w2, h->h2, h->dbl,
                                     h->comp));
     }
+    // the path's kernel is loaded now rather than at the first batch
+    if (h->mode == EMIDA_GB_MODE_FUSED) CK(preload_fused(h->w2, h->dbl, h->in_f64));
+    if (h->mode == EMIDA_GB_MODE_TENSOR) CK(preload_brute_tc());
     CK(cudaStreamSynchronize(h->comp));
     h->ref_set = true;
     return EMIDA_GB_OK;

@@ -58,6 +58,10 @@ __host__ __device__ inline int lstsq_offset(int s)
 bool fused_supported(uint32_t fft_n, bool dbl, bool in_f64 = false);
 // The smallest fused transform that holds a zero-padded ROI of this side (0: none).
 uint32_t fused_size_for(uint32_t side, bool dbl, bool in_f64 = false);
+// Loads the fused kernel of this length and types without launching it.  CUDA
+// loads a kernel's module at its first use; done when a layout is registered,
+// that cost (tens of milliseconds) stays out of the first request's latency.
+cudaError_t preload_fused(uint32_t fft_n, bool dbl, bool in_f64);
 // Dynamic shared memory of one CTA of the fused kernel for this length.
 size_t fused_smem_bytes(uint32_t fft_n, bool dbl);
 // Rows of the TMA box a CTA stages per ROI (the 256-point kernel's CTAs each
