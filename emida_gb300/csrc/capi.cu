@@ -415,6 +415,10 @@ int validate(const emida_gb_params *p)
     if (p->n_rois == 0 || !p->begins) return fail(EMIDA_GB_INVALID_ARGUMENT, "no ROIs");
     if (p->slice_w < 2 || p->slice_h < 2) return fail(EMIDA_GB_INVALID_ARGUMENT, "ROI smaller than 2x2");
     if (p->batch_size == 0) return fail(EMIDA_GB_INVALID_ARGUMENT, "batchsize must be greater than 0");
+    // pair counts and pair indices are 32-bit on the device
+    if ((uint64_t)p->n_rois * p->batch_size > 0x7fffffffu)
+        return fail(EMIDA_GB_INVALID_ARGUMENT, "ROIs x batchsize (%llu) exceeds 2^31 - 1",
+                    (unsigned long long)p->n_rois * p->batch_size);
     if (p->policy != EMIDA_GB_BRUTE && p->policy != EMIDA_GB_FFT)
         return fail(EMIDA_GB_INVALID_ARGUMENT, "invalid cross policy %d", p->policy);
     if (p->precision != EMIDA_GB_DOUBLE && p->precision != EMIDA_GB_FLOAT)

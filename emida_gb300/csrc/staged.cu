@@ -86,12 +86,13 @@ template <> __device__ __forceinline__ double add_rn(double a, double b) { retur
 template <typename T>
 __global__ void __launch_bounds__(BLOCK)
     k_cross_corr(const T *__restrict__ pics, const T *__restrict__ ref, T *__restrict__ res,
-                 size2 size, size2 res_size, uint32_t ref_slices)
+                 size2 size, size2 res_size, uint32_t ref_slices, uint32_t pair0)
 {
     extern __shared__ __align__(16) unsigned char smem_raw[];
     T *sp = reinterpret_cast<T *>(smem_raw);
     T *sr = sp + size.x * size.y;
-    const uint32_t py = blockIdx.x, pair = blockIdx.y;
+    // pairs run in launches of at most 65,535 (grid.y); pair0 is the launch's first
+    const uint32_t py = blockIdx.x, pair = pair0 + blockIdx.y;
     const uint32_t area = size.x * size.y;
     const T *p = pics + (size_t)pair * area;
     const T *r = ref + (size_t)(pair % ref_slices) * area;
@@ -398,6 +399,9 @@ __global__ void __launch_bounds__(256) k_gather_rois(const uint16_t *__restrict_
 
 inline uint32_t grid_for(uint64_t n) { return (uint32_t)((n + BLOCK - 1) / BLOCK); }
 
+// the largest grid.y a launch takes
+constexpr uint32_t CROSS_CORR_MAX_Y = 65535;
+
 }  // namespace
 
 uint32_t gather_width(uint32_t side) { return (side + 14) & ~7u; }
@@ -473,22 +477,27 @@ cudaError_t run_cross_corr(const void *pics, const void *ref, void *res, bool db
 {
     const uint32_t n = ref_slices * batch;
     if (n == 0) return cudaSuccess;
-    dim3 grid(res_size.y, n);
     const size_t smem = (size_t)2 * size.x * size.y * (dbl ? 8 : 4);
     if (dbl) {
-        auto k = k_cross_corr<double>;
-        if (smem > 48 * 1024) cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
-        k<<<grid, BLOCK, smem, st>>>(reinterpret_cast<const double *>(pics),
-                                     reinterpret_cast<const double *>(ref),
-                                     reinterpret_cast<double *>(res), size, res_size, ref_slices);
-    } else {
-        auto k = k_cross_corr<float>;
-        if (smem > 48 * 1024) cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
-        k<<<grid, BLOCK, smem, st>>>(reinterpret_cast<const float *>(pics),
-                                     reinterpret_cast<const float *>(ref),
-                                     reinterpret_cast<float *>(res), size, res_size, ref_slices);
+        if (smem > 48 * 1024)
+            cudaFuncSetAttribute(k_cross_corr<double>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+    } else if (smem > 48 * 1024) {
+        cudaFuncSetAttribute(k_cross_corr<float>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
     }
-    return cudaGetLastError();
+    for (uint32_t pair0 = 0; pair0 < n; pair0 += CROSS_CORR_MAX_Y) {
+        const dim3 grid(res_size.y, n - pair0 < CROSS_CORR_MAX_Y ? n - pair0 : CROSS_CORR_MAX_Y);
+        if (dbl)
+            k_cross_corr<double><<<grid, BLOCK, smem, st>>>(
+                reinterpret_cast<const double *>(pics), reinterpret_cast<const double *>(ref),
+                reinterpret_cast<double *>(res), size, res_size, ref_slices, pair0);
+        else
+            k_cross_corr<float><<<grid, BLOCK, smem, st>>>(
+                reinterpret_cast<const float *>(pics), reinterpret_cast<const float *>(ref),
+                reinterpret_cast<float *>(res), size, res_size, ref_slices, pair0);
+        const cudaError_t e = cudaGetLastError();
+        if (e != cudaSuccess) return e;
+    }
+    return cudaSuccess;
 }
 
 cudaError_t run_fft_r2c(const void *real_in, void *spec, uint32_t maps, const fft_tables &t,

@@ -62,6 +62,7 @@ def test_fitsize_rejected(lib):
 @pytest.mark.parametrize("kw,msg", [
     (dict(s=4), "Wrong fitting size"),
     (dict(batch_size=0), "batchsize"),
+    (dict(batch_size=2 ** 31), "exceeds 2\\^31"),
     (dict(begins=[(200, 0)]), "out of bounds"),
     (dict(cross_size=(200, 3)), "cross size"),
     (dict(policy="sideways"), "crosspolicy"),

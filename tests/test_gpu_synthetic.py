@@ -226,3 +226,23 @@ def test_repeatable(data512):
     a = run(ref, pics, begins, 64, "fft", 5, "float", "fused")
     b = run(ref, pics, begins, 64, "fft", 5, "float", "fused")
     assert all(np.array_equal(x, y) for x, y in zip(a, b))
+
+
+def test_brute_more_pairs_than_one_launch_holds():
+    # 256 ROIs x 260 patterns = 66,560 pairs: the brute correlation runs in
+    # launches of at most 65,535 pairs, and the pairs past the first launch
+    # keep the oracle's bits
+    from emida_gb300 import synth
+    ref = synth.reference_pattern(128, seed=13)
+    base, _ = synth.deformed_patterns(128, 13, 4, sigma_eps=2e-3)
+    pics = np.ascontiguousarray(base[np.arange(260) % 4])
+    begins = [(x, y) for y in range(0, 121, 8) for x in range(0, 121, 8)]
+    offs, coefs, peaks = run(ref, pics, begins, 8, "brute", 3, "double", "plain", (15, 15))
+    n = len(begins)
+    o_offs, o_coefs, o_peaks = oracle(ref, pics[-4:], begins, 8, "brute", 3, (15, 15))
+    assert np.array_equal(peaks[-4 * n:], o_peaks)
+    assert np.array_equal(offs[-4 * n:], o_offs)
+    assert np.array_equal(coefs[-4 * n:], o_coefs)
+    # and every repeat of a pattern gives its first result
+    first = offs[:4 * n].reshape(4, n, 2)
+    assert np.array_equal(offs.reshape(260, n, 2), first[np.arange(260) % 4])
