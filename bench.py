@@ -18,7 +18,8 @@ copied), the path, and the offsets, coefficients and maxima back to the host.
 The timed steps run as one stream of batches, as a scan is processed;
 one_step_ms is a single step with the pipeline filled and drained inside it.
 e2e_ingest: the same with the other ingest modes (kernels reading each batch's
-ROI pixels in place, alternating batches, gathered ROI rows).
+ROI pixels in place, alternating batches, gathered ROI rows, row bands copied
+by SM loads).
 
 --impl reference times the reference algorithm on the host cores instead (the
 CPU FP64 oracle port of the same path; the reference's own CPU code is built
@@ -246,6 +247,12 @@ def run_reference(args, rank, world):
                 "d2h_bytes_per_step": 0},
     }
     print(json.dumps(line), flush=True)
+
+
+INGEST_HOW = {
+    "copy": "one pitched copy-engine copy per row band",
+    "sm_copy": "each row band by SM loads on 16 CTAs beside the previous batch's path",
+}
 
 
 def roi_rows(begins, side):
@@ -641,7 +648,7 @@ def run_profile_target(args):
                       np.uint16, "fused")
         g.allocate_memory(ref)
         out = {"profile_target": "ingest", "patterns": n}
-        for mode in ("copy", "gather"):
+        for mode in ("copy", "gather", "sm_copy"):
             g.ingest = mode
             t0 = time.perf_counter()
             pending = []
@@ -857,6 +864,9 @@ def main():
         barrier()
         return max_over_ranks((time.perf_counter() - t0) * 1000 / steps, dist, device="cuda")
 
+    # the library's default ingest for this form: the row bands copied by SM
+    # loads on a few CTAs beside the path
+    default_ingest = g.ingest
     e2e_run(1)
     assert np.array_equal(host_offs, offs), "e2e offsets differ from the device-resident run"
     e2e_ms = e2e_time(e2e_steps)
@@ -864,10 +874,12 @@ def main():
     # one step alone, the pipeline filled and drained inside it
     e2e_one_ms = statistics.median(e2e_time(1) for _ in range(3))
     # the other ingest modes: kernels reading the ROI pixels in place (no
-    # copy), every other batch each way, and a gather kernel packing the ROI
-    # rows beside the path
+    # copy), every other batch each way, a gather kernel packing the ROI rows
+    # beside the path, and the row bands copied by SM loads
     ingest = {}
-    for mode in ("in_place", "split", "gather"):
+    for mode in ("copy", "in_place", "split", "gather", "sm_copy"):
+        if mode == default_ingest:
+            continue
         g.ingest = mode
         if g.ingest != mode:
             continue
@@ -877,7 +889,7 @@ def main():
         one_ms = statistics.median(e2e_time(1) for _ in range(3))
         ingest[mode] = {"value": whole_job_rate(pairs_per_step, m_ms / 1000.0, world), "ms_per_step": m_ms,
                         "one_step_ms": one_ms}
-    g.ingest = "copy"
+    g.ingest = default_ingest
     _lib.call("emida_gb_free_host", hbuf)
 
     cpu = None
@@ -919,8 +931,9 @@ def main():
                     "ms_per_step": e2e_ms,
                     "steps": e2e_steps,
                     "one_step_ms": e2e_one_ms,
+                    "ingest": default_ingest,
                     "input": f"pinned host batches; the {roi_rows(begins, 64)} of 1024 rows that hold "
-                             "ROI pixels are copied (one pitched copy per row band)",
+                             "ROI pixels are copied, " + INGEST_HOW.get(default_ingest, default_ingest),
                     "pipeline": f"the steps run as one stream of {nb}-batch passes through submit/wait, "
                                 f"{in_flight} batches of 32 in flight across step boundaries; "
                                 "one_step_ms: a single step with the pipeline filled and drained in it"},

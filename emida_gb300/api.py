@@ -276,7 +276,7 @@ class GpuOffset:
     def stream(self):
         return _lib.lib().emida_gb_stream(self._h)
 
-    INGEST = ("copy", "in_place", "split", "gather")
+    INGEST = ("copy", "in_place", "split", "gather", "sm_copy")
 
     @property
     def ingest(self):
@@ -284,7 +284,9 @@ class GpuOffset:
         "in_place" (kernels read the ROI pixels over the host link, no copy),
         "split" (alternate batches, copy engine and host reads in parallel) or
         "gather" (a gather kernel on a few SMs packs only the ROI rows into
-        device memory beside the previous batch's path)."""
+        device memory beside the previous batch's path) or "sm_copy" (the
+        row bands that "copy" moves, copied by SM loads on a few CTAs instead
+        of the copy engine)."""
         return self.INGEST[_lib.lib().emida_gb_ingest(self._h)]
 
     @ingest.setter
@@ -292,7 +294,8 @@ class GpuOffset:
         """In-place modes are honoured only when the ROIs cover at most half
         of each pattern (a fused or tensor form); "gather" only for a fused or
         tensor form with uint16 input, a width divisible by 8 and a compact
-        ROI layout no larger than a pattern; otherwise "copy" stays."""
+        ROI layout no larger than a pattern; "sm_copy" when a pattern row is
+        a whole number of 16-byte chunks; otherwise "copy" stays."""
         _lib.call("emida_gb_set_ingest", self._h, self.INGEST.index(mode))
 
     def launches_per_run(self):

@@ -527,6 +527,13 @@ int emida_gb_create(const emida_gb_params *p, emida_gb_handle **out)
     h->gather_allowed = h->mode != EMIDA_GB_MODE_PLAIN && !h->in_f64 && p->src_w % 8 == 0 &&
                         (uint64_t)p->n_rois * p->slice_h * gather_width(p->slice_w) <=
                             (uint64_t)p->src_w * p->src_h;
+    // a pattern of at most 2^31 16-byte chunks (chunk indices within a run
+    // stay 32-bit), whose rows are whole chunks
+    h->sm_copy_allowed = ((uint64_t)p->src_w * h->in_elem) % 16 == 0 &&
+                         (uint64_t)p->src_w * p->src_h * h->in_elem / 16 <= 0x7fffffffu;
+    // the fused and tensor forms leave CTA slots for the SM copy beside them
+    h->ingest = h->sm_copy_allowed && h->mode != EMIDA_GB_MODE_PLAIN ? EMIDA_GB_INGEST_SM_COPY
+                                                                     : EMIDA_GB_INGEST_COPY;
     if (h->mode == EMIDA_GB_MODE_FUSED) {
         // the resident reference spectra are computed at the fused length
         h->w2 = h->h2 = fn;
@@ -569,6 +576,17 @@ int emida_gb_create(const emida_gb_params *p, emida_gb_handle **out)
         TRY([&]() -> int {
             CK(cudaMemcpy(h->d_begins_compact, compact.data(), sizeof(uint2) * h->S,
                           cudaMemcpyHostToDevice));
+            return EMIDA_GB_OK;
+        }());
+    }
+    if (h->sm_copy_allowed) {
+        const uint32_t row16 = (uint32_t)(h->src.x * h->in_elem / 16);
+        std::vector<uint2> runs;
+        for (const auto &b : h->bands) runs.push_back(make_uint2(b.first * row16, b.second * row16));
+        h->n_band_runs = (uint32_t)runs.size();
+        TRY(h->alloc((void **)&h->d_band_runs, sizeof(uint2) * runs.size()));
+        TRY([&]() -> int {
+            CK(cudaMemcpy(h->d_band_runs, runs.data(), sizeof(uint2) * runs.size(), cudaMemcpyHostToDevice));
             return EMIDA_GB_OK;
         }());
     }
@@ -743,6 +761,7 @@ int emida_gb_get_offset(emida_gb_handle *h, const void *batch, double *offsets, 
 // (about 145 GB/s of ROI pixels against 211 GB/s for contiguous reads) when
 // they run alone; beside the path's CTAs they run slower.
 constexpr int GATHER_CTAS = 16;
+constexpr int COPY_CTAS = 16;
 
 static int ring_init(emida_gb_handle *h)
 {
@@ -789,6 +808,8 @@ int emida_gb_submit(emida_gb_handle *h, const void *batch, uint32_t patterns, ui
                                 (h->ingest == EMIDA_GB_INGEST_SPLIT && (t & 1)));
     const bool gather = pa.type == cudaMemoryTypeHost && h->ingest == EMIDA_GB_INGEST_GATHER &&
                         (uintptr_t)batch % 16 == 0;
+    const bool sm_copy = pa.type == cudaMemoryTypeHost && h->ingest == EMIDA_GB_INGEST_SM_COPY &&
+                         (uintptr_t)batch % 16 == 0;
     const void *src = batch;
     batch_view compact{size2{gather_width(h->slice.x), h->S * h->slice.y}, h->d_begins_compact};
     const batch_view *view = nullptr;
@@ -809,6 +830,21 @@ int emida_gb_submit(emida_gb_handle *h, const void *batch, uint32_t patterns, ui
         src = h->d_in[si];
         view = &compact;
         grid = -GATHER_CTAS;
+    } else if (sm_copy) {
+        // the row bands cross the host link by SM loads on COPY_CTAS CTAs of
+        // the path's footprint, beside the previous batch's path, which
+        // launches that many CTAs short of a full wave
+        const size_t smem = h->mode == EMIDA_GB_MODE_FUSED   ? fused_smem_bytes(h->w2, h->dbl)
+                            : h->mode == EMIDA_GB_MODE_TENSOR ? brute_tc_smem_bytes()
+                                                              : 0;
+        const uint64_t pat16 = (uint64_t)h->src.x * h->src.y * h->in_elem / 16;
+        CK(cudaStreamWaitEvent(h->in_stream, r.comp, 0));
+        CK(run_copy_bands(batch, h->d_in[si], h->d_band_runs, h->n_band_runs, pat16, patterns, COPY_CTAS,
+                          smem, h->in_stream));
+        CK(cudaEventRecord(r.h2d, h->in_stream));
+        CK(cudaStreamWaitEvent(h->comp, r.h2d, 0));
+        src = h->d_in[si];
+        grid = h->mode == EMIDA_GB_MODE_PLAIN ? 0 : -COPY_CTAS;
     } else if (!(pa.type == cudaMemoryTypeDevice || pa.type == cudaMemoryTypeManaged || in_place_host)) {
         // the input buffer is free once the slot's previous computation ran
         CK(cudaStreamWaitEvent(h->in_stream, r.comp, 0));
@@ -901,12 +937,13 @@ int emida_gb_ingest(const emida_gb_handle *h) { return h ? h->ingest : -1; }
 int emida_gb_set_ingest(emida_gb_handle *h, int mode)
 {
     if (!h) return fail(EMIDA_GB_INVALID_ARGUMENT, "null handle");
-    if (mode < EMIDA_GB_INGEST_COPY || mode > EMIDA_GB_INGEST_GATHER)
+    if (mode < EMIDA_GB_INGEST_COPY || mode > EMIDA_GB_INGEST_SM_COPY)
         return fail(EMIDA_GB_INVALID_ARGUMENT, "invalid ingest mode %d", mode);
     std::lock_guard<std::mutex> lk(h->mu);
-    const bool ok = mode == EMIDA_GB_INGEST_GATHER ? h->gather_allowed
-                    : mode == EMIDA_GB_INGEST_COPY ? true
-                                                   : h->in_place_allowed;
+    const bool ok = mode == EMIDA_GB_INGEST_GATHER    ? h->gather_allowed
+                    : mode == EMIDA_GB_INGEST_SM_COPY ? h->sm_copy_allowed
+                    : mode == EMIDA_GB_INGEST_COPY    ? true
+                                                      : h->in_place_allowed;
     h->ingest = ok ? mode : EMIDA_GB_INGEST_COPY;
     return EMIDA_GB_OK;
 }

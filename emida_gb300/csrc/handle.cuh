@@ -140,12 +140,18 @@ struct emida_gb_handle {
     bool in_place_allowed = false;
     // rows [first, first + second) of a pattern that hold ROI pixels, merged
     std::vector<std::pair<uint32_t, uint32_t>> bands;
-    int ingest = EMIDA_GB_INGEST_COPY;
+    int ingest = EMIDA_GB_INGEST_COPY;  // SM_COPY for the fused and tensor forms where allowed
     // The gather ingest: allowed for the fused and tensor forms with uint16
     // input, src_w % 8 == 0 and a compact layout no larger than the patterns;
     // d_begins_compact holds each ROI's place in the compact layout.
     bool gather_allowed = false;
     uint2 *d_begins_compact = nullptr;
+    // The SM-copy ingest: the row bands as (first 16-byte chunk, chunks) runs
+    // within a pattern; allowed when a pattern row is a whole number of
+    // 16-byte chunks.
+    bool sm_copy_allowed = false;
+    uint2 *d_band_runs = nullptr;
+    uint32_t n_band_runs = 0;
     std::mutex mu;
     std::vector<void *> allocs;
     // submit/wait ring: one slot per input buffer

@@ -397,6 +397,34 @@ __global__ void __launch_bounds__(256) k_gather_rois(const uint16_t *__restrict_
     }
 }
 
+// One CTA per (pattern, band) run at a time: the run's 16-byte chunks in
+// strides of the block, four loads in flight per thread before their stores,
+// so that a CTA keeps 32 KB of host reads in flight over the link.
+constexpr int COPY_THREADS = 512;
+
+__global__ void __launch_bounds__(COPY_THREADS)
+    k_copy_bands(const int4 *__restrict__ src, int4 *__restrict__ dst, const uint2 *__restrict__ runs,
+                 uint32_t n_runs, uint64_t pat16, uint32_t units)
+{
+    for (uint32_t u = blockIdx.x; u < units; u += gridDim.x) {
+        const uint32_t p = u / n_runs;
+        const uint2 r = runs[u - p * n_runs];  // (first chunk, chunks) within a pattern
+        const uint64_t base = (uint64_t)p * pat16 + r.x;
+        const int4 *s = src + base;
+        int4 *d = dst + base;
+        const uint32_t n = r.y, stride = COPY_THREADS;
+        uint32_t i = threadIdx.x;
+        for (; i + 3 * stride < n; i += 4 * stride) {
+            const int4 a = s[i], b = s[i + stride], c = s[i + 2 * stride], e = s[i + 3 * stride];
+            d[i] = a;
+            d[i + stride] = b;
+            d[i + 2 * stride] = c;
+            d[i + 3 * stride] = e;
+        }
+        for (; i < n; i += stride) d[i] = s[i];
+    }
+}
+
 inline uint32_t grid_for(uint64_t n) { return (uint32_t)((n + BLOCK - 1) / BLOCK); }
 
 // the largest grid.y a launch takes
@@ -431,6 +459,22 @@ cudaError_t run_gather_rois(const uint16_t *pics, size2 src, const uint2 *begins
         if (e != cudaSuccess) return e;
     }
     return cudaSuccess;
+}
+
+cudaError_t run_copy_bands(const void *src, void *dst, const uint2 *runs, uint32_t n_runs,
+                           uint64_t pat16, uint32_t patterns, int ctas, size_t smem,
+                           cudaStream_t st)
+{
+    if ((uintptr_t)src % 16 || (uintptr_t)dst % 16) return cudaErrorInvalidValue;
+    const uint64_t units = (uint64_t)patterns * n_runs;
+    if (units == 0) return cudaSuccess;
+    if (units > 0xffffffffu) return cudaErrorInvalidValue;
+    cudaError_t e = cudaFuncSetAttribute(k_copy_bands, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+    if (e != cudaSuccess) return e;
+    const uint32_t grid = (uint32_t)std::min<uint64_t>(units, (uint64_t)std::max(ctas, 1));
+    k_copy_bands<<<grid, COPY_THREADS, smem, st>>>(static_cast<const int4 *>(src), static_cast<int4 *>(dst),
+                                                   runs, n_runs, pat16, (uint32_t)units);
+    return cudaGetLastError();
 }
 
 cudaError_t run_sums(const void *pics, int in_type, size2 src, const uint2 *begins,

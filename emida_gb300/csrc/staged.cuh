@@ -81,6 +81,16 @@ cudaError_t run_gather_rois(const uint16_t *pics, size2 src, const uint2 *begins
                             size2 slice, uint32_t patterns, uint16_t *out, int ctas, size_t smem,
                             cudaStream_t st);
 
+// Copy of the ROI row bands of `patterns` patterns from src (pinned host
+// memory, read over NVLink-C2C) to dst in the same layout, by SM loads on at
+// most `ctas` CTAs rather than by the copy engine.  runs[n_runs] holds each
+// band as (first 16-byte chunk, chunk count) within a pattern of pat16
+// chunks; src and dst 16-byte aligned.  Each CTA reserves `smem` bytes of
+// (unused) dynamic shared memory, as run_gather_rois does.
+cudaError_t run_copy_bands(const void *src, void *dst, const uint2 *runs, uint32_t n_runs,
+                           uint64_t pat16, uint32_t patterns, int ctas, size_t smem,
+                           cudaStream_t st);
+
 // Reference spectra from cuFFT layout [S][h2][w2/2+1] to the fused kernel's
 // column-major layout [S][w2/2+1][h2].
 cudaError_t run_spec_to_colmajor(const void *spec, void *out, uint32_t maps, uint32_t w2,

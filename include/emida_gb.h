@@ -111,7 +111,8 @@ int emida_gb_get_offset(emida_gb_handle *h, const void *batch, double *offsets, 
  * until its ticket is waited for.  The process_files pipeline of the reference
  * (src/process_files.hpp:98-233) does the same with threads and two streams.
  * A batch in device memory is used in place.  A batch in pinned host memory
- * arrives as emida_gb_set_ingest chose (default EMIDA_GB_INGEST_COPY). */
+ * arrives as emida_gb_set_ingest chose (default EMIDA_GB_INGEST_SM_COPY for
+ * the fused and tensor forms where it is allowed, else EMIDA_GB_INGEST_COPY). */
 int emida_gb_submit(emida_gb_handle *h, const void *batch, uint32_t patterns, uint64_t *ticket);
 /* Waits for a ticket and copies its offsets [patterns*n_rois][2], coefficients
  * [..][6] and argmax indices [..] to the host (coefs, peaks may be NULL). */
@@ -144,17 +145,24 @@ int emida_gb_resolved_mode(const emida_gb_handle *h);
  *             and the lowest latency per batch; with several batches in flight
  *             the copy engine keeps up better, as the gather's host reads slow
  *             down beside the path's CTAs).
+ *   SM_COPY   the ROI row bands, as COPY moves them, copied by SM loads on a
+ *             few CTAs beside the previous batch's path rather than by the
+ *             copy engine (a pitched copy engine transfer of the bands runs
+ *             below the link's rate; SM loads of whole runs reach it).
  * IN_PLACE and SPLIT are taken only by a fused or tensor form whose ROIs cover
  * at most half of each pattern; GATHER by a fused or tensor form with uint16
  * input, src_w a multiple of 8 and a compact layout (n_rois ROIs of side x
  * ((side + 14) & ~7) pixels) no larger than a pattern, and only for 16-byte
- * aligned batches (others are copied).  Otherwise the mode stays COPY.
+ * aligned batches (others are copied); SM_COPY when a pattern row is a whole
+ * number of 16-byte chunks, and only for 16-byte aligned batches (others are
+ * copied).  Otherwise the mode stays COPY.
  * emida_gb_ingest reports the mode in force. */
 enum {
     EMIDA_GB_INGEST_COPY = 0,
     EMIDA_GB_INGEST_IN_PLACE = 1,
     EMIDA_GB_INGEST_SPLIT = 2,
-    EMIDA_GB_INGEST_GATHER = 3
+    EMIDA_GB_INGEST_GATHER = 3,
+    EMIDA_GB_INGEST_SM_COPY = 4
 };
 int emida_gb_set_ingest(emida_gb_handle *h, int mode);
 int emida_gb_ingest(const emida_gb_handle *h);

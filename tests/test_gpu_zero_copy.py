@@ -56,11 +56,11 @@ def test_submit_reads_pinned_batches_in_place(data):
     ref, pics, begins = data
     g = GpuOffset((512, 512), begins, (64, 64), (127, 127), 3, "fft", 5, 3, "float", np.uint16, "fused")
     g.allocate_memory(ref)
-    assert g.ingest == "copy"  # the default
+    assert g.ingest == "sm_copy"  # the default of the fused form (1024-byte rows)
     host = pinned_array(pics.shape)
     host[:] = pics
     expect = [g.get_offset(pics[k:k + 3]) for k in (0, 3)]
-    for mode in ("in_place", "split", "copy"):
+    for mode in ("in_place", "split", "copy", "sm_copy"):
         g.ingest = mode
         assert g.ingest == mode  # 16 ROIs of 64^2 cover a quarter of a 512^2 pattern
         tickets = [g.submit(host[k:k + 3]) for k in (0, 3, 0)]
@@ -184,7 +184,11 @@ def test_gather_ingest_needs_its_geometry():
     # a width that is not a multiple of 8
     g = GpuOffset((260, 256), [(0, 0), (100, 90)], (64, 64), (127, 127), 1, "fft", 5, 1, "float",
                   np.uint16, "fused")
+    assert g.ingest == "copy"  # the default where the SM copy is not allowed
     g.ingest = "gather"
+    assert g.ingest == "copy"
+    # nor are its 520-byte rows whole 16-byte chunks for the SM copy
+    g.ingest = "sm_copy"
     assert g.ingest == "copy"
     g.close()
     # a compact layout larger than the pattern (overlapping ROIs)
@@ -196,6 +200,46 @@ def test_gather_ingest_needs_its_geometry():
     # the staged form and FP64 input read whole patterns
     for mode, in_type in (("plain", np.uint16), ("fused", np.float64)):
         g = GpuOffset((256, 256), [(0, 0)], (64, 64), (127, 127), 1, "fft", 5, 1, "float", in_type, mode)
+        # the staged form leaves no CTA slots for the SM copy: the copy engine is its default
+        assert g.ingest == ("copy" if mode == "plain" else "sm_copy")
         g.ingest = "gather"
         assert g.ingest == "copy"
         g.close()
+
+
+@pytest.mark.parametrize("side,precision,mode,in_type,n_rois", [
+    (32, "float", "fused", np.uint16, 12), (48, "float", "fused", np.uint16, 3),
+    (64, "float", "tensor", np.uint16, 12), (32, "float", "plain", np.uint16, 12),
+    (32, "double", "fused", np.float64, 12), (32, "float", "fused", np.uint16, 60)])
+def test_submit_sm_copy_ingest_equals_copy(side, precision, mode, in_type, n_rois):
+    # the row bands of a pinned batch copied by SM loads instead of the copy
+    # engine: the bits of the copied batch, for sparse bands, a single band and
+    # bands that cover the whole pattern (60 ROIs)
+    from emida_gb300 import GpuOffset, pinned_array, synth
+    w, h, batch = 520, 384, 3
+    ref = synth.reference_pattern((w, h), seed=side + 1)
+    pics, _ = synth.deformed_patterns((w, h), side + 1, 2 * batch, sigma_eps=3e-3)
+    pics = pics.astype(in_type)
+    begins = _ragged_begins(w, h, side, n_rois, seed=side + n_rois)
+    policy = "brute" if mode == "tensor" else "fft"
+    g = GpuOffset((w, h), begins, (side, side), (2 * side - 1, 2 * side - 1), batch, policy, 5, 3,
+                  precision, in_type, mode)
+    g.allocate_memory(ref.astype(in_type))
+    host = pinned_array(pics.shape, in_type)
+    host[:] = pics
+    expect = [g.get_offset(pics[k:k + batch]) for k in (0, batch)]
+    g.ingest = "sm_copy"
+    assert g.ingest == "sm_copy"
+    tickets = [g.submit(host[k:k + batch]) for k in (0, batch, 0)]
+    for t, (e_offs, e_coefs) in zip(tickets, expect + expect[:1]):
+        offs, coefs = g.wait(t)
+        assert np.array_equal(offs, e_offs) and np.array_equal(coefs, e_coefs)
+    # a partial batch, and a batch that is not 16-byte aligned (copied instead)
+    offs, _ = g.wait(g.submit(host[:2]))
+    assert np.array_equal(offs, expect[0][0][:2 * len(begins)])
+    flat = pinned_array((batch * w * h + 8,), in_type)
+    odd = flat[1:1 + batch * w * h].reshape(batch, h, w)
+    odd[:] = pics[:batch]
+    offs, coefs = g.wait(g.submit(odd))
+    assert np.array_equal(offs, expect[0][0]) and np.array_equal(coefs, expect[0][1])
+    g.close()
