@@ -549,7 +549,12 @@ int emida_gb_create(const emida_gb_params *p, emida_gb_handle **out)
     if ((st = (expr)) != EMIDA_GB_OK) return bail(st);
     TRY([&]() -> int { CK(cudaGetDevice(&h->device)); return EMIDA_GB_OK; }());
     TRY([&]() -> int {
-        CK(cudaStreamCreateWithFlags(&h->in_stream, cudaStreamNonBlocking));
+        // the input stream's copy CTAs are dispatched ahead of a path's
+        // pending CTAs when two batches' paths overlap
+        int least = 0;
+        int greatest = 0;
+        CK(cudaDeviceGetStreamPriorityRange(&least, &greatest));
+        CK(cudaStreamCreateWithPriority(&h->in_stream, cudaStreamNonBlocking, greatest));
         CK(cudaStreamCreateWithFlags(&h->out_stream, cudaStreamNonBlocking));
         CK(cudaStreamCreateWithFlags(&h->comp, cudaStreamNonBlocking));
         CK(cudaEventCreateWithFlags(&h->comp_done, cudaEventDisableTiming));
@@ -779,6 +784,9 @@ static int ring_init(emida_gb_handle *h)
         CK(cudaEventCreateWithFlags(&r.comp, cudaEventDisableTiming));
         CK(cudaEventCreateWithFlags(&r.done, cudaEventDisableTiming));
     }
+    // the staged form's scratch buffers are shared between batches: one stream
+    if (h->mode != EMIDA_GB_MODE_PLAIN && !h->comp_alt)
+        CK(cudaStreamCreateWithFlags(&h->comp_alt, cudaStreamNonBlocking));
     h->ring = std::move(ring);
     return EMIDA_GB_OK;
 }
@@ -798,6 +806,7 @@ int emida_gb_submit(emida_gb_handle *h, const void *batch, uint32_t patterns, ui
     if (r.busy)
         return fail(EMIDA_GB_INVALID_ARGUMENT, "all %zu slots in flight: wait for ticket %llu first",
                     h->ring.size(), (unsigned long long)r.ticket);
+    cudaStream_t cs = h->comp_alt && (t & 1) ? h->comp_alt : h->comp;
     cudaPointerAttributes pa{};
     CK(cudaPointerGetAttributes(&pa, batch));
     // device batches are used in place; pinned host batches are copied or read
@@ -826,7 +835,7 @@ int emida_gb_submit(emida_gb_handle *h, const void *batch, uint32_t patterns, ui
                            patterns, static_cast<uint16_t *>(h->d_in[si]), GATHER_CTAS, smem,
                            h->in_stream));
         CK(cudaEventRecord(r.h2d, h->in_stream));
-        CK(cudaStreamWaitEvent(h->comp, r.h2d, 0));
+        CK(cudaStreamWaitEvent(cs, r.h2d, 0));
         src = h->d_in[si];
         view = &compact;
         grid = -GATHER_CTAS;
@@ -842,7 +851,7 @@ int emida_gb_submit(emida_gb_handle *h, const void *batch, uint32_t patterns, ui
         CK(run_copy_bands(batch, h->d_in[si], h->d_band_runs, h->n_band_runs, pat16, patterns, COPY_CTAS,
                           smem, h->in_stream));
         CK(cudaEventRecord(r.h2d, h->in_stream));
-        CK(cudaStreamWaitEvent(h->comp, r.h2d, 0));
+        CK(cudaStreamWaitEvent(cs, r.h2d, 0));
         src = h->d_in[si];
         grid = h->mode == EMIDA_GB_MODE_PLAIN ? 0 : -COPY_CTAS;
     } else if (!(pa.type == cudaMemoryTypeDevice || pa.type == cudaMemoryTypeManaged || in_place_host)) {
@@ -850,11 +859,14 @@ int emida_gb_submit(emida_gb_handle *h, const void *batch, uint32_t patterns, ui
         CK(cudaStreamWaitEvent(h->in_stream, r.comp, 0));
         CKS(copy_patterns(h, h->d_in[si], batch, patterns, h->in_stream));
         CK(cudaEventRecord(r.h2d, h->in_stream));
-        CK(cudaStreamWaitEvent(h->comp, r.h2d, 0));
+        CK(cudaStreamWaitEvent(cs, r.h2d, 0));
         src = h->d_in[si];
     }
-    CKS(run_any(h, src, patterns, r.d_maxes, h->d_neigh, r.d_offsets, r.d_coefs, h->comp, view, grid));
-    CK(cudaEventRecord(r.comp, h->comp));
+    // the neighbourhoods are scratch for the staged form only; the fused and
+    // tensor forms of two batches may run at once and keep them in shared memory
+    CKS(run_any(h, src, patterns, r.d_maxes, h->mode == EMIDA_GB_MODE_PLAIN ? h->d_neigh : nullptr,
+                r.d_offsets, r.d_coefs, cs, view, grid));
+    CK(cudaEventRecord(r.comp, cs));
     CK(cudaStreamWaitEvent(h->out_stream, r.comp, 0));
     const size_t n = (size_t)patterns * h->S;
     CK(cudaMemcpyAsync(r.h_offsets, r.d_offsets, 2 * sizeof(double) * n, cudaMemcpyDeviceToHost, h->out_stream));
@@ -959,6 +971,7 @@ void emida_gb_destroy(emida_gb_handle *h)
 {
     if (!h) return;
     if (h->comp) cudaStreamSynchronize(h->comp);
+    if (h->comp_alt) cudaStreamSynchronize(h->comp_alt);
     if (h->in_stream) cudaStreamSynchronize(h->in_stream);
     if (h->out_stream) cudaStreamSynchronize(h->out_stream);
     for (auto &r : h->ring) {
@@ -974,6 +987,7 @@ void emida_gb_destroy(emida_gb_handle *h)
         if (e) cudaEventDestroy(e);
     if (h->comp_done) cudaEventDestroy(h->comp_done);
     if (h->comp) cudaStreamDestroy(h->comp);
+    if (h->comp_alt) cudaStreamDestroy(h->comp_alt);
     if (h->in_stream) cudaStreamDestroy(h->in_stream);
     if (h->out_stream) cudaStreamDestroy(h->out_stream);
     delete h;

@@ -168,6 +168,10 @@ struct emida_gb_handle {
     };
     std::vector<slot> ring;
     uint64_t next_ticket = 1;
+    // Fused and tensor forms: batches of odd tickets run on this second compute
+    // stream, so that a batch's path starts on the CTA slots the previous
+    // batch's last CTAs leave free instead of after its tail.
+    cudaStream_t comp_alt = nullptr;
 
     int alloc(void **ptr, size_t bytes, bool zero = false)
     {
