@@ -439,7 +439,7 @@ def run_serving(args):
                    "rate_rows_per_s": args.rate, "duration_s": args.duration,
                    "hbm_arena_bytes_per_size": 24 << 30, "step_patterns": args.step_patterns,
                    "rows": "copied into the device arena" if args.copy_rows else
-                           "pinned rows read in place where ROIs cover <= half the pattern"},
+                           "pinned rows read in place by the kernels (no copy-engine transfer)"},
         "parity": {"max_abs_err_px": max(errs),
                    "rms_err_px": float(np.sqrt(np.concatenate(sq).mean())),
                    "vs": "FP64 oracle, one row per size"},

@@ -450,7 +450,10 @@ class Server:
         self._h = h
         self.rois = []
         self._rows = {}
-        _lib.call("emida_gb_server_set_zero_copy", h, int(bool(zero_copy)))
+        # True: every pinned row read in place; "sparse": rows of layouts whose
+        # ROIs cover at most half of the pattern; False: every row copied
+        level = 1 if zero_copy == "sparse" else 2 if zero_copy else 0
+        _lib.call("emida_gb_server_set_zero_copy", h, level)
 
     def add_layout(self, src_size, begins, side, fitsize, ref):
         begins = np.ascontiguousarray(np.asarray(begins, dtype=np.uint32).reshape(-1, 2))

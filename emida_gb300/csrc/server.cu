@@ -108,7 +108,9 @@ struct emida_gb_server {
     bool stop = false;
     int error = EMIDA_GB_OK;
     std::string error_msg;
-    bool zero_copy = true;  // pinned rows on sparse layouts are read in place
+    // which pinned rows the kernels read in place: 0 none, 1 rows of sparse
+    // layouts, 2 every pinned row (no copy-engine transfer on the row path)
+    int zero_copy = 2;
 };
 
 namespace {
@@ -409,7 +411,7 @@ int emida_gb_server_submit(emida_gb_server *sv, uint32_t layout_id, const uint16
     const auto &L = sv->layouts[layout_id];
     pool &p = *sv->pools[L.pool];
     bool in_place = false;
-    if (L.sparse && sv->zero_copy) {
+    if (sv->zero_copy == 2 || (sv->zero_copy == 1 && L.sparse)) {
         cudaPointerAttributes pa{};
         CK(cudaPointerGetAttributes(&pa, patterns));
         in_place = pa.type == cudaMemoryTypeHost;
@@ -441,8 +443,9 @@ int emida_gb_server_submit(emida_gb_server *sv, uint32_t layout_id, const uint16
 int emida_gb_server_set_zero_copy(emida_gb_server *sv, int enable)
 {
     if (!sv) return fail(EMIDA_GB_INVALID_ARGUMENT, "null argument");
+    if (enable < 0 || enable > 2) return fail(EMIDA_GB_INVALID_ARGUMENT, "zero-copy level %d not in 0..2", enable);
     std::lock_guard<std::mutex> lk(sv->mu);
-    sv->zero_copy = enable != 0;
+    sv->zero_copy = enable;
     return EMIDA_GB_OK;
 }
 

@@ -235,10 +235,9 @@ void emida_gb_multi_destroy(emida_gb_multi *m);
  * and computed in steps of up to step_patterns patterns drawn from every
  * admitted row in turn, so rows that arrive while others run share the next
  * steps.  The host patterns must stay valid until the request is waited for;
- * pinned memory lets the copies overlap.  A pinned row on a layout whose ROIs
- * cover at most half of the pattern is not copied at all: the kernels read its
- * ROI pixels in place (switch off with emida_gb_server_set_zero_copy).  Results
- * are per row, pattern-major. */
+ * pinned memory lets the copies overlap.  A pinned row is not copied at all:
+ * the kernels read its ROI pixels in place (emida_gb_server_set_zero_copy sets
+ * which rows).  Results are per row, pattern-major. */
 typedef struct emida_gb_server emida_gb_server;
 int emida_gb_server_create(int32_t precision, uint64_t hbm_bytes, uint32_t step_patterns,
                            emida_gb_server **out);
@@ -247,7 +246,11 @@ int emida_gb_server_add_layout(emida_gb_server *s, uint32_t src_w, uint32_t src_
                                int32_t fitsize, const uint16_t *ref, uint32_t *layout_id);
 int emida_gb_server_submit(emida_gb_server *s, uint32_t layout_id, const uint16_t *patterns,
                            uint32_t n, uint64_t *request_id);
-/* enable = 0: every row is copied into the arena (rows submitted later). */
+/* Which pinned rows submitted later are read in place rather than copied into
+ * the arena: 2 every pinned row (default), 1 rows of layouts whose ROIs cover
+ * at most half of the pattern, 0 none.  Reading in place keeps the row path
+ * off the copy engine, whose transfers stalled for tens of milliseconds at
+ * times on a shared host. */
 int emida_gb_server_set_zero_copy(emida_gb_server *s, int enable);
 /* Blocks until the row is done; offsets [n*rois][2], coefs [n*rois][6] may be
  * NULL; latency_ms = submission to completion. */

@@ -113,9 +113,10 @@ def test_multi_run_table_mixes_device_and_host_patterns(data):
 def test_server_rows_in_place_equal_copied_rows(data):
     from emida_gb300 import Server, pinned_array, synth
     ref, pics, begins = data
-    _, wide = synth.roi_grid(512, 7, 32, margin=32)  # covers most of the pattern: copied
+    # `wide` covers most of the pattern: copied under "sparse", read in place by default
+    _, wide = synth.roi_grid(512, 7, 32, margin=32)
     results = {}
-    for zero_copy in (False, True):
+    for zero_copy in (False, "sparse", True):
         s = Server("float", hbm_bytes=8 * 512 * 512 * 2, step_patterns=4, zero_copy=zero_copy)
         sparse = s.add_layout((512, 512), begins, 64, 5, ref)
         dense = s.add_layout((512, 512), wide, 64, 3, ref)
@@ -127,8 +128,9 @@ def test_server_rows_in_place_equal_copied_rows(data):
         rids = [s.submit(lid, h) for lid, h in rows]
         results[zero_copy] = [s.wait(r)[:2] for r in rids]
         s.close()
-    for (a_offs, a_coefs), (b_offs, b_coefs) in zip(results[False], results[True]):
-        assert np.array_equal(a_offs, b_offs) and np.array_equal(a_coefs, b_coefs)
+    for level in ("sparse", True):
+        for (a_offs, a_coefs), (b_offs, b_coefs) in zip(results[False], results[level]):
+            assert np.array_equal(a_offs, b_offs) and np.array_equal(a_coefs, b_coefs)
 
 
 def _ragged_begins(w, h, side, n, seed):
