@@ -245,7 +245,7 @@ int emida_gb::host::run_plain_chunk(emida_gb_handle *h, const void *pics, uint32
 }
 
 int emida_gb::host::run_fused(emida_gb_handle *h, const void *pics, uint32_t pats, void *maxes, void *neigh,
-              double *offsets, double *coefs, cudaStream_t st, const batch_view *view, int grid)
+              double *offsets, double *coefs, cudaStream_t st, const batch_view *view, int grid, uint32_t *err)
 {
     const size2 src = view ? view->src : h->src;
     fused_args a{};
@@ -266,7 +266,7 @@ int emida_gb::host::run_fused(emida_gb_handle *h, const void *pics, uint32_t pat
     a.coefs = coefs;
     a.maxes = maxes;
     a.neigh = neigh;
-    a.err = h->d_err;
+    a.err = err ? err : h->d_err;
     CUtensorMap map;
     std::memset(&map, 0, sizeof map);
     a.stage = STAGE_PLAIN;
@@ -293,7 +293,7 @@ int emida_gb::host::run_fused(emida_gb_handle *h, const void *pics, uint32_t pat
 }
 
 int emida_gb::host::run_tensor(emida_gb_handle *h, const void *pics, uint32_t pats, void *maxes, void *neigh,
-               double *offsets, double *coefs, cudaStream_t st, const batch_view *view, int grid)
+               double *offsets, double *coefs, cudaStream_t st, const batch_view *view, int grid, uint32_t *err)
 {
     brute_tc_args a{};
     a.pics = static_cast<const uint16_t *>(pics);
@@ -310,18 +310,18 @@ int emida_gb::host::run_tensor(emida_gb_handle *h, const void *pics, uint32_t pa
     a.coefs = coefs;
     a.maxes = maxes;
     a.neigh = static_cast<float *>(neigh);
-    a.err = h->d_err;
+    a.err = err ? err : h->d_err;
     CK(launch_brute_tc(a, grid, st));
     return EMIDA_GB_OK;
 }
 
 int emida_gb::host::run_any(emida_gb_handle *h, const void *pics, uint32_t pats, void *maxes, void *neigh,
-            double *offsets, double *coefs, cudaStream_t st, const batch_view *view, int grid)
+            double *offsets, double *coefs, cudaStream_t st, const batch_view *view, int grid, uint32_t *err)
 {
     if (h->mode == EMIDA_GB_MODE_FUSED)
-        return run_fused(h, pics, pats, maxes, neigh, offsets, coefs, st, view, grid);
+        return run_fused(h, pics, pats, maxes, neigh, offsets, coefs, st, view, grid, err);
     if (h->mode == EMIDA_GB_MODE_TENSOR)
-        return run_tensor(h, pics, pats, maxes, neigh, offsets, coefs, st, view, grid);
+        return run_tensor(h, pics, pats, maxes, neigh, offsets, coefs, st, view, grid, err);
     if (view) return fail(EMIDA_GB_UNSUPPORTED, "the staged form reads whole patterns only");
     const size_t pat_bytes = (size_t)h->src.x * h->src.y * h->in_elem;
     const size_t s2 = (size_t)h->p.fitsize * h->p.fitsize;
@@ -393,12 +393,13 @@ void row_bands(emida_gb_handle *h)
 
 }  // namespace
 
-int emida_gb::host::check_device_error(emida_gb_handle *h)
+int emida_gb::host::check_device_error(emida_gb_handle *h, uint32_t *word)
 {
+    uint32_t *w = word ? word : h->d_err;
     uint32_t err = 0;
-    CK(cudaMemcpy(&err, h->d_err, sizeof err, cudaMemcpyDeviceToHost));
+    CK(cudaMemcpy(&err, w, sizeof err, cudaMemcpyDeviceToHost));
     if (err) {
-        CK(cudaMemset(h->d_err, 0, sizeof err));
+        CK(cudaMemset(w, 0, sizeof err));
         return fail(EMIDA_GB_DEVICE_CHECK, "device check failed (flags 0x%x%s%s)", err,
                     (err & DEV_ERR_TMA_TIMEOUT) ? ": TMA wait ran out" : "",
                     (err & DEV_ERR_WAIT_TIMEOUT) ? ": pipeline wait ran out" : "");
@@ -779,6 +780,7 @@ static int ring_init(emida_gb_handle *h)
         CK(cudaMallocHost((void **)&r.h_offsets, 2 * sizeof(double) * h->N));
         CK(cudaMallocHost((void **)&r.h_coefs, 6 * sizeof(double) * h->N));
         CK(cudaMallocHost(&r.h_maxes, h->di_elem * h->N));
+        CKS(h->alloc((void **)&r.d_err, sizeof(uint32_t), true));
         CK(cudaMallocHost((void **)&r.h_err, sizeof(uint32_t)));
         CK(cudaEventCreateWithFlags(&r.h2d, cudaEventDisableTiming));
         CK(cudaEventCreateWithFlags(&r.comp, cudaEventDisableTiming));
@@ -865,7 +867,7 @@ int emida_gb_submit(emida_gb_handle *h, const void *batch, uint32_t patterns, ui
     // the neighbourhoods are scratch for the staged form only; the fused and
     // tensor forms of two batches may run at once and keep them in shared memory
     CKS(run_any(h, src, patterns, r.d_maxes, h->mode == EMIDA_GB_MODE_PLAIN ? h->d_neigh : nullptr,
-                r.d_offsets, r.d_coefs, cs, view, grid));
+                r.d_offsets, r.d_coefs, cs, view, grid, r.d_err));
     CK(cudaEventRecord(r.comp, cs));
     CK(cudaStreamWaitEvent(h->out_stream, r.comp, 0));
     const size_t n = (size_t)patterns * h->S;
@@ -873,7 +875,7 @@ int emida_gb_submit(emida_gb_handle *h, const void *batch, uint32_t patterns, ui
     CK(cudaMemcpyAsync(r.h_coefs, r.d_coefs, 6 * sizeof(double) * n, cudaMemcpyDeviceToHost, h->out_stream));
     CK(cudaMemcpyAsync(r.h_maxes, r.d_maxes, h->di_elem * n, cudaMemcpyDeviceToHost, h->out_stream));
     // the error word travels with the results: wait() reads it without a synchronous copy
-    CK(cudaMemcpyAsync(r.h_err, h->d_err, sizeof(uint32_t), cudaMemcpyDeviceToHost, h->out_stream));
+    CK(cudaMemcpyAsync(r.h_err, r.d_err, sizeof(uint32_t), cudaMemcpyDeviceToHost, h->out_stream));
     CK(cudaEventRecord(r.done, h->out_stream));
     r.busy = true;
     r.ticket = t;
@@ -897,7 +899,7 @@ int emida_gb_wait(emida_gb_handle *h, uint64_t ticket, double *offsets, double *
             return fail(EMIDA_GB_INVALID_ARGUMENT, "unknown ticket %llu", (unsigned long long)ticket);
     }
     CK(cudaEventSynchronize(r->done));
-    if (*r->h_err) CKS(check_device_error(h));  // reports the flags and clears the word
+    if (*r->h_err) CKS(check_device_error(h, r->d_err));  // reports the flags and clears the slot's word
     const size_t n = (size_t)r->patterns * h->S;
     std::memcpy(offsets, r->h_offsets, 2 * sizeof(double) * n);
     if (coefs) std::memcpy(coefs, r->h_coefs, 6 * sizeof(double) * n);

@@ -61,18 +61,20 @@ struct batch_view {
     size2 src;
     const uint2 *begins;
 };
-// `grid` as launch_fused and launch_brute_tc take it (<= 0: one wave less -grid CTAs).
+// `grid` as launch_fused and launch_brute_tc take it (<= 0: one wave less -grid CTAs);
+// `err` the device error word the kernel sets (nullptr: the handle's).
 int run_fused(emida_gb_handle *h, const void *pics, uint32_t pats, void *maxes, void *neigh,
               double *offsets, double *coefs, cudaStream_t st, const batch_view *view = nullptr,
-              int grid = 0);
+              int grid = 0, uint32_t *err = nullptr);
 int run_tensor(emida_gb_handle *h, const void *pics, uint32_t pats, void *maxes, void *neigh,
                double *offsets, double *coefs, cudaStream_t st, const batch_view *view = nullptr,
-               int grid = 0);
+               int grid = 0, uint32_t *err = nullptr);
 // Either form, any number of patterns (a view only for the fused and tensor forms).
 int run_any(emida_gb_handle *h, const void *pics, uint32_t pats, void *maxes, void *neigh,
             double *offsets, double *coefs, cudaStream_t st, const batch_view *view = nullptr,
-            int grid = 0);
-int check_device_error(emida_gb_handle *h);
+            int grid = 0, uint32_t *err = nullptr);
+// Reads a device error word (nullptr: the handle's), clears it and reports its flags.
+int check_device_error(emida_gb_handle *h, uint32_t *word = nullptr);
 // Host -> device copy of `patterns` whole patterns as the kernels need them:
 // only the row bands that hold ROI pixels (one pitched copy per band over all
 // patterns), or everything when the bands cover most of a pattern.
@@ -160,7 +162,8 @@ struct emida_gb_handle {
         void *d_maxes = nullptr;
         double *h_offsets = nullptr, *h_coefs = nullptr;
         void *h_maxes = nullptr;
-        uint32_t *h_err = nullptr;  // the device error word as it stood after this slot's path
+        uint32_t *d_err = nullptr;  // the error word this slot's path sets
+        uint32_t *h_err = nullptr;  // its host copy, taken after the path
         cudaEvent_t h2d = nullptr, comp = nullptr, done = nullptr;
         uint64_t ticket = 0;
         uint32_t patterns = 0;
