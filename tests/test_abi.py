@@ -37,6 +37,25 @@ def test_binding_covers_header(lib):
     assert set(header_symbols()) == set(_lib.SIGNATURES)
 
 
+def header_enums():
+    text = open(os.path.join(ROOT, "include", "emida_gb.h")).read()
+    return {k: int(v) for k, v in re.findall(r"\b(EMIDA_GB_[A-Z0-9_]+)\s*=\s*(-?\d+)", text)}
+
+
+def test_python_constants_match_header_enums():
+    # the Python mirror's constants and mode names index the header's enums
+    from emida_gb300 import GpuOffset, _lib
+    enums = header_enums()
+    for name in ("OK", "BRUTE", "FFT", "DOUBLE", "FLOAT", "IN_U16", "IN_F64", "MODE_AUTO",
+                 "MODE_PLAIN", "MODE_FUSED", "MODE_TENSOR"):
+        assert getattr(_lib, name) == enums["EMIDA_GB_" + name], name
+    ingest = {k[len("EMIDA_GB_INGEST_"):].lower(): v for k, v in enums.items()
+              if k.startswith("EMIDA_GB_INGEST_")}
+    assert len(ingest) == len(GpuOffset.INGEST)
+    for i, name in enumerate(GpuOffset.INGEST):
+        assert ingest[name] == i, name
+
+
 @pytest.mark.parametrize("s", [3, 5, 7, 9])
 def test_library_lstsq_tables_are_the_references(lib, s):
     from emida_gb300 import lstsq_matrix
