@@ -115,7 +115,7 @@ struct emida_gb_server {
 
 namespace {
 
-int admit(emida_gb_server *sv, pool &p)
+int admit(emida_gb_server *, pool &p)
 {
     while (!p.pending.empty()) {
         request *r = p.pending.front();
