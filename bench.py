@@ -874,10 +874,10 @@ def main():
     # one step alone, the pipeline filled and drained inside it
     e2e_one_ms = statistics.median(e2e_time(1) for _ in range(3))
     # the other ingest modes: kernels reading the ROI pixels in place (no
-    # copy), every other batch each way, a gather kernel packing the ROI rows
+    # copy), a gather kernel packing the ROI rows
     # beside the path, and the row bands copied by SM loads
     ingest = {}
-    for mode in ("copy", "in_place", "split", "gather", "sm_copy"):
+    for mode in ("copy", "in_place", "gather", "sm_copy"):
         if mode == default_ingest:
             continue
         g.ingest = mode

@@ -103,6 +103,7 @@ SIGNATURES = {
     "emida_gb_free_host": [_VP],
     "emida_gb_synchronize": [],
     "emida_gb_selftest_bounded_wait": [_VP, ctypes.c_int64],
+    "emida_gb_selftest_arm_submit": [_VP, ctypes.c_int64],
     "emida_gb_time_device": [_VP, _VP, _U32, _VP, _I32, ctypes.POINTER(ctypes.c_float)],
     "emida_gb_run_sum": [_VP, _I32, _U32, _U32, _VP, _U32, _U32, _U32, _U32, _VP],
     "emida_gb_run_prepare": [_VP, _I32, _I32, _VP, _VP, _VP, _VP, _U32, _U32, _U32, _U32,

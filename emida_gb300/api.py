@@ -276,13 +276,13 @@ class GpuOffset:
     def stream(self):
         return _lib.lib().emida_gb_stream(self._h)
 
-    INGEST = ("copy", "in_place", "split", "gather", "sm_copy")
+    # index = EMIDA_GB_INGEST_* value; 2 is not a mode
+    INGEST = ("copy", "in_place", None, "gather", "sm_copy")
 
     @property
     def ingest(self):
         """How submit() brings pinned host batches to the kernels: "copy",
         "in_place" (kernels read the ROI pixels over the host link, no copy),
-        "split" (alternate batches, copy engine and host reads in parallel) or
         "gather" (a gather kernel on a few SMs packs only the ROI rows into
         device memory beside the previous batch's path) or "sm_copy" (the
         row bands that "copy" moves, copied by SM loads on a few CTAs instead
@@ -296,6 +296,8 @@ class GpuOffset:
         tensor form with uint16 input, a width divisible by 8 and a compact
         ROI layout no larger than a pattern; "sm_copy" when a pattern row is
         a whole number of 16-byte chunks; otherwise "copy" stays."""
+        if mode not in self.INGEST or mode is None:
+            raise ValueError(f"unknown ingest mode {mode!r}")
         _lib.call("emida_gb_set_ingest", self._h, self.INGEST.index(mode))
 
     def launches_per_run(self):

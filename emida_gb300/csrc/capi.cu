@@ -393,18 +393,26 @@ void row_bands(emida_gb_handle *h)
 
 }  // namespace
 
+int emida_gb::host::device_flags_status(uint32_t err)
+{
+    if (!err) return EMIDA_GB_OK;
+    return fail(EMIDA_GB_DEVICE_CHECK, "device check failed (flags 0x%x%s%s)", err,
+                (err & DEV_ERR_TMA_TIMEOUT) ? ": TMA wait ran out" : "",
+                (err & DEV_ERR_WAIT_TIMEOUT) ? ": pipeline wait ran out" : "");
+}
+
 int emida_gb::host::check_device_error(emida_gb_handle *h, uint32_t *word)
 {
     uint32_t *w = word ? word : h->d_err;
     uint32_t err = 0;
     CK(cudaMemcpy(&err, w, sizeof err, cudaMemcpyDeviceToHost));
     if (err) {
-        CK(cudaMemset(w, 0, sizeof err));
-        return fail(EMIDA_GB_DEVICE_CHECK, "device check failed (flags 0x%x%s%s)", err,
-                    (err & DEV_ERR_TMA_TIMEOUT) ? ": TMA wait ran out" : "",
-                    (err & DEV_ERR_WAIT_TIMEOUT) ? ": pipeline wait ran out" : "");
+        // the handle's streams do not wait for the legacy stream: the clear
+        // completes here, before any later launch can set the word again
+        CK(cudaMemsetAsync(w, 0, sizeof err, cudaStreamLegacy));
+        CK(cudaStreamSynchronize(cudaStreamLegacy));
     }
-    return EMIDA_GB_OK;
+    return device_flags_status(err);
 }
 
 namespace {
@@ -450,6 +458,22 @@ int validate(const emida_gb_params *p)
                     "the tensor-core form takes the brute policy, float precision, uint16 input, "
                     "64x64 ROIs and a 127x127 lag window");
     return EMIDA_GB_OK;
+}
+
+}  // namespace
+
+namespace {
+
+// One warp waits on phase 0 of an mbarrier that expects one arrival and gets
+// none: the bounded wait gives up after `budget` cycles and records it.
+__global__ void k_selftest_wait(uint32_t *err, long long budget)
+{
+    __shared__ __align__(8) uint64_t bar;
+    if (threadIdx.x == 0) emida_gb::ptx::mbar_init(&bar, 1);
+    __syncthreads();
+    const bool done = emida_gb::ptx::mbar_wait_for(&bar, 0, budget);
+    if (!done && threadIdx.x == 0) atomicOr(err, DEV_ERR_WAIT_TIMEOUT);
+    __syncthreads();
 }
 
 }  // namespace
@@ -812,11 +836,8 @@ int emida_gb_submit(emida_gb_handle *h, const void *batch, uint32_t patterns, ui
     cudaPointerAttributes pa{};
     CK(cudaPointerGetAttributes(&pa, batch));
     // device batches are used in place; pinned host batches are copied or read
-    // in place as the ingest mode says (SPLIT: every other batch each way, so
-    // the copy engine and the kernels' host reads share the load)
-    const bool in_place_host = pa.type == cudaMemoryTypeHost &&
-                               (h->ingest == EMIDA_GB_INGEST_IN_PLACE ||
-                                (h->ingest == EMIDA_GB_INGEST_SPLIT && (t & 1)));
+    // in place as the ingest mode says
+    const bool in_place_host = pa.type == cudaMemoryTypeHost && h->ingest == EMIDA_GB_INGEST_IN_PLACE;
     const bool gather = pa.type == cudaMemoryTypeHost && h->ingest == EMIDA_GB_INGEST_GATHER &&
                         (uintptr_t)batch % 16 == 0;
     const bool sm_copy = pa.type == cudaMemoryTypeHost && h->ingest == EMIDA_GB_INGEST_SM_COPY &&
@@ -864,6 +885,13 @@ int emida_gb_submit(emida_gb_handle *h, const void *batch, uint32_t patterns, ui
         CK(cudaStreamWaitEvent(cs, r.h2d, 0));
         src = h->d_in[si];
     }
+    if (h->selftest_budget > 0) {
+        // armed by emida_gb_selftest_arm_submit: this batch's error word is set
+        // by a bounded wait that runs out, as a real timeout of its path would
+        k_selftest_wait<<<1, 32, 0, cs>>>(r.d_err, (long long)h->selftest_budget);
+        CK(cudaGetLastError());
+        h->selftest_budget = 0;
+    }
     // the neighbourhoods are scratch for the staged form only; the fused and
     // tensor forms of two batches may run at once and keep them in shared memory
     CKS(run_any(h, src, patterns, r.d_maxes, h->mode == EMIDA_GB_MODE_PLAIN ? h->d_neigh : nullptr,
@@ -899,7 +927,22 @@ int emida_gb_wait(emida_gb_handle *h, uint64_t ticket, double *offsets, double *
             return fail(EMIDA_GB_INVALID_ARGUMENT, "unknown ticket %llu", (unsigned long long)ticket);
     }
     CK(cudaEventSynchronize(r->done));
-    if (*r->h_err) CKS(check_device_error(h, r->d_err));  // reports the flags and clears the slot's word
+    if (const uint32_t flags = *r->h_err) {
+        // The batch failed its device check.  Its ticket is consumed and its
+        // slot released, with the slot's word cleared (and the clear complete)
+        // before the slot can be submitted again.
+        *r->h_err = 0;
+        cudaError_t e = cudaMemsetAsync(r->d_err, 0, sizeof(uint32_t), h->out_stream);
+        if (e == cudaSuccess) e = cudaStreamSynchronize(h->out_stream);
+        {
+            std::lock_guard<std::mutex> lk(h->mu);
+            r->busy = false;
+        }
+        if (e != cudaSuccess)
+            return fail(EMIDA_GB_CUDA_ERROR, "clearing the error word of ticket %llu: %s",
+                        (unsigned long long)ticket, cudaGetErrorString(e));
+        return device_flags_status(flags);
+    }
     const size_t n = (size_t)r->patterns * h->S;
     std::memcpy(offsets, r->h_offsets, 2 * sizeof(double) * n);
     if (coefs) std::memcpy(coefs, r->h_coefs, 6 * sizeof(double) * n);
@@ -951,7 +994,7 @@ int emida_gb_ingest(const emida_gb_handle *h) { return h ? h->ingest : -1; }
 int emida_gb_set_ingest(emida_gb_handle *h, int mode)
 {
     if (!h) return fail(EMIDA_GB_INVALID_ARGUMENT, "null handle");
-    if (mode < EMIDA_GB_INGEST_COPY || mode > EMIDA_GB_INGEST_SM_COPY)
+    if (mode < EMIDA_GB_INGEST_COPY || mode > EMIDA_GB_INGEST_SM_COPY || mode == 2)
         return fail(EMIDA_GB_INVALID_ARGUMENT, "invalid ingest mode %d", mode);
     std::lock_guard<std::mutex> lk(h->mu);
     const bool ok = mode == EMIDA_GB_INGEST_GATHER    ? h->gather_allowed
@@ -1097,22 +1140,6 @@ int emida_gb_synchronize(void)
 
 }  // extern "C"
 
-namespace {
-
-// One warp waits on phase 0 of an mbarrier that expects one arrival and gets
-// none: the bounded wait gives up after `budget` cycles and records it.
-__global__ void k_selftest_wait(uint32_t *err, long long budget)
-{
-    __shared__ __align__(8) uint64_t bar;
-    if (threadIdx.x == 0) emida_gb::ptx::mbar_init(&bar, 1);
-    __syncthreads();
-    const bool done = emida_gb::ptx::mbar_wait_for(&bar, 0, budget);
-    if (!done && threadIdx.x == 0) atomicOr(err, DEV_ERR_WAIT_TIMEOUT);
-    __syncthreads();
-}
-
-}  // namespace
-
 extern "C" {
 
 int emida_gb_selftest_bounded_wait(emida_gb_handle *h, int64_t budget_cycles)
@@ -1125,6 +1152,16 @@ int emida_gb_selftest_bounded_wait(emida_gb_handle *h, int64_t budget_cycles)
     CK(cudaGetLastError());
     CK(cudaStreamSynchronize(h->comp));
     return check_device_error(h);
+}
+
+int emida_gb_selftest_arm_submit(emida_gb_handle *h, int64_t budget_cycles)
+{
+    if (!h) return fail(EMIDA_GB_INVALID_ARGUMENT, "null handle");
+    if (budget_cycles < 1 || budget_cycles > 4000000000LL)
+        return fail(EMIDA_GB_INVALID_ARGUMENT, "budget must be in [1, 4e9] cycles");
+    std::lock_guard<std::mutex> lk(h->mu);
+    h->selftest_budget = budget_cycles;
+    return EMIDA_GB_OK;
 }
 
 // ---- per-stage launchers --------------------------------------------------------
@@ -1207,7 +1244,9 @@ int emida_gb_run_fft_c2r(void *spec, void *real_out, uint32_t maps, uint32_t w2,
 // emida_gb_run_fft_r2c builds its two twiddle tables in cudaMalloc'd memory and
 // frees them on return.  The variant below keeps them in one fixed device array
 // instead: the row table at byte 0, the column table at byte NOALLOC_COL_OFFSET,
-// each up to NOALLOC_MAX_SIDE complex doubles, 32 KiB in all.
+// each up to NOALLOC_MAX_SIDE complex doubles, 32 KiB in all.  It runs on a
+// non-blocking stream of its own, so it neither waits for nor holds up the work
+// of any other stream on the device.
 namespace {
 
 constexpr uint32_t NOALLOC_MAX_SIDE = 1024;
@@ -1216,12 +1255,18 @@ constexpr int NOALLOC_MAX_DEVICES = 64;
 
 static __device__ __align__(256) unsigned char g_noalloc_twiddles[2 * NOALLOC_COL_OFFSET];
 
+// Per device: the array's device address and the entry point's stream.
+struct noalloc_device {
+    void *scratch = nullptr;
+    cudaStream_t stream = nullptr;
+};
 std::mutex g_noalloc_mutex;
-void *g_noalloc_ptr[NOALLOC_MAX_DEVICES];  // device address of the array, per device
+noalloc_device g_noalloc[NOALLOC_MAX_DEVICES];
 
-// Address of g_noalloc_twiddles on the current device, looked up on the first
-// call made with that device current and cached afterwards.
-int noalloc_scratch(void **out)
+// The current device's set-up, done by the first call made with that device
+// current and cached afterwards: the address of g_noalloc_twiddles (a host-side
+// name that no kernel may be given) and a non-blocking stream.
+int noalloc_setup(noalloc_device *out)
 {
     int dev = 0;
     CK(cudaGetDevice(&dev));
@@ -1229,15 +1274,22 @@ int noalloc_scratch(void **out)
         return fail(EMIDA_GB_UNSUPPORTED, "fft r2c (no-alloc): device %d beyond the %d supported",
                     dev, NOALLOC_MAX_DEVICES);
     std::lock_guard<std::mutex> lock(g_noalloc_mutex);
-    if (!g_noalloc_ptr[dev]) {
+    noalloc_device &d = g_noalloc[dev];
+    if (!d.scratch) {
         void *p = nullptr;
         cudaError_t e = cudaGetSymbolAddress(&p, g_noalloc_twiddles);
         if (e != cudaSuccess || !p)
             return fail(EMIDA_GB_CUDA_ERROR, "fft r2c (no-alloc): scratch address on device %d: %s",
                         dev, cudaGetErrorString(e));
-        g_noalloc_ptr[dev] = p;
+        cudaStream_t st = nullptr;
+        e = cudaStreamCreateWithFlags(&st, cudaStreamNonBlocking);
+        if (e != cudaSuccess)
+            return fail(EMIDA_GB_CUDA_ERROR, "fft r2c (no-alloc): stream on device %d: %s", dev,
+                        cudaGetErrorString(e));
+        d.stream = st;
+        d.scratch = p;
     }
-    *out = g_noalloc_ptr[dev];
+    *out = d;
     return EMIDA_GB_OK;
 }
 
@@ -1256,17 +1308,20 @@ template <typename C> void twiddles_into(C *w, uint32_t n)
 
 template <typename C>
 int fft_r2c_noalloc(const void *real_in, void *spec, uint32_t maps, uint32_t w2, uint32_t h2,
-                    unsigned char *scratch)
+                    const noalloc_device &d)
 {
     // Host staging on the stack: two tables of at most NOALLOC_MAX_SIDE entries.
+    // The copies from pageable memory have read them before they return.
     C row[NOALLOC_MAX_SIDE], col[NOALLOC_MAX_SIDE];
     twiddles_into(row, w2);
     twiddles_into(col, h2);
-    CK(cudaMemcpy(scratch, row, w2 * sizeof(C), cudaMemcpyHostToDevice));
-    CK(cudaMemcpy(scratch + NOALLOC_COL_OFFSET, col, h2 * sizeof(C), cudaMemcpyHostToDevice));
+    auto *scratch = static_cast<unsigned char *>(d.scratch);
+    CK(cudaMemcpyAsync(scratch, row, w2 * sizeof(C), cudaMemcpyHostToDevice, d.stream));
+    CK(cudaMemcpyAsync(scratch + NOALLOC_COL_OFFSET, col, h2 * sizeof(C), cudaMemcpyHostToDevice,
+                       d.stream));
     const fft_tables t{scratch, scratch + NOALLOC_COL_OFFSET, w2, h2};
-    CK(run_fft_r2c(real_in, spec, maps, t, sizeof(C) == sizeof(double2), 0));
-    CK(cudaDeviceSynchronize());
+    CK(run_fft_r2c(real_in, spec, maps, t, sizeof(C) == sizeof(double2), d.stream));
+    CK(cudaStreamSynchronize(d.stream));
     return EMIDA_GB_OK;
 }
 
@@ -1286,11 +1341,10 @@ int emida_gb_run_fft_r2c_noalloc(const void *real_in, void *spec, uint32_t maps,
                     w2, h2, NOALLOC_MAX_SIDE, NOALLOC_MAX_SIDE);
     if (maps == 0) return EMIDA_GB_OK;
     if (!real_in || !spec) return fail(EMIDA_GB_INVALID_ARGUMENT, "fft r2c (no-alloc): null buffer");
-    void *scratch = nullptr;
-    CKS(noalloc_scratch(&scratch));
-    auto *s = static_cast<unsigned char *>(scratch);
-    return precision == EMIDA_GB_DOUBLE ? fft_r2c_noalloc<double2>(real_in, spec, maps, w2, h2, s)
-                                        : fft_r2c_noalloc<float2>(real_in, spec, maps, w2, h2, s);
+    noalloc_device d;
+    CKS(noalloc_setup(&d));
+    return precision == EMIDA_GB_DOUBLE ? fft_r2c_noalloc<double2>(real_in, spec, maps, w2, h2, d)
+                                        : fft_r2c_noalloc<float2>(real_in, spec, maps, w2, h2, d);
 }
 
 int emida_gb_run_hadamard(void *pics, const void *ref, uint32_t one_area, uint32_t ref_slices,

@@ -75,6 +75,8 @@ int run_any(emida_gb_handle *h, const void *pics, uint32_t pats, void *maxes, vo
             int grid = 0, uint32_t *err = nullptr);
 // Reads a device error word (nullptr: the handle's), clears it and reports its flags.
 int check_device_error(emida_gb_handle *h, uint32_t *word = nullptr);
+// EMIDA_GB_OK for no flags, else EMIDA_GB_DEVICE_CHECK with the flags named.
+int device_flags_status(uint32_t flags);
 // Host -> device copy of `patterns` whole patterns as the kernels need them:
 // only the row bands that hold ROI pixels (one pitched copy per band over all
 // patterns), or everything when the bands cover most of a pattern.
@@ -175,6 +177,9 @@ struct emida_gb_handle {
     // stream, so that a batch's path starts on the CTA slots the previous
     // batch's last CTAs leave free instead of after its tail.
     cudaStream_t comp_alt = nullptr;
+    // emida_gb_selftest_arm_submit: the next submit's slot word is set by a
+    // bounded wait of this many cycles that runs out (0: not armed)
+    int64_t selftest_budget = 0;
 
     int alloc(void **ptr, size_t bytes, bool zero = false)
     {

@@ -137,8 +137,6 @@ int emida_gb_resolved_mode(const emida_gb_handle *h);
  *   COPY      a copy on the input stream, overlapping the previous batch's path;
  *   IN_PLACE  no copy: the kernels read the batch's ROI pixels in place over the
  *             host link (lowest latency per batch);
- *   SPLIT     every other batch each way, so the copy engine and the kernels'
- *             host reads work in parallel;
  *   GATHER    a gather kernel on a few SMs reads only the 16-byte chunks that
  *             hold ROI pixels over the host link into a compact device layout,
  *             beside the previous batch's path (the fewest bytes over the link
@@ -149,7 +147,9 @@ int emida_gb_resolved_mode(const emida_gb_handle *h);
  *             few CTAs beside the previous batch's path rather than by the
  *             copy engine (a pitched copy engine transfer of the bands runs
  *             below the link's rate; SM loads of whole runs reach it).
- * IN_PLACE and SPLIT are taken only by a fused or tensor form whose ROIs cover
+ * Value 2 is not a mode (it named an alternating mode that was withdrawn, as it
+ * was slower than every other); emida_gb_set_ingest refuses it.
+ * IN_PLACE is taken only by a fused or tensor form whose ROIs cover
  * at most half of each pattern; GATHER by a fused or tensor form with uint16
  * input, src_w a multiple of 8 and a compact layout (n_rois ROIs of side x
  * ((side + 14) & ~7) pixels) no larger than a pattern, and only for 16-byte
@@ -160,7 +160,6 @@ int emida_gb_resolved_mode(const emida_gb_handle *h);
 enum {
     EMIDA_GB_INGEST_COPY = 0,
     EMIDA_GB_INGEST_IN_PLACE = 1,
-    EMIDA_GB_INGEST_SPLIT = 2,
     EMIDA_GB_INGEST_GATHER = 3,
     EMIDA_GB_INGEST_SM_COPY = 4
 };
@@ -301,6 +300,13 @@ int emida_gb_synchronize(void);
  * EMIDA_GB_DEVICE_CHECK, "pipeline wait ran out".  The context and the
  * handle stay usable; the error word is cleared.  No reference counterpart. */
 int emida_gb_selftest_bounded_wait(emida_gb_handle *h, int64_t budget_cycles);
+/* Self-test of a failed batch in the submit/wait ring: the next emida_gb_submit
+ * on this handle sets its slot's device error word by the same bounded wait
+ * (about budget_cycles cycles, at most 4e9) before the batch's path runs.  Its
+ * emida_gb_wait then returns EMIDA_GB_DEVICE_CHECK ("pipeline wait ran out"),
+ * consumes the ticket and frees the slot, and later batches run as usual.
+ * One-shot; no fault, trap or hang.  No reference counterpart. */
+int emida_gb_selftest_arm_submit(emida_gb_handle *h, int64_t budget_cycles);
 /* CUDA-event timing on a stream: elapsed ms of `repeats` runs of the handle's
  * device form over the same inputs, measured on the launching stream. */
 int emida_gb_time_device(emida_gb_handle *h, const void *dev_patterns, uint32_t patterns,
@@ -324,16 +330,22 @@ int emida_gb_run_cross_corr(const void *pics, const void *ref, void *res, int pr
 int emida_gb_run_fft_r2c(const void *real_in, void *spec, uint32_t maps, uint32_t w2,
                          uint32_t h2, int precision);
 /* Allocation-free form of emida_gb_run_fft_r2c (no counterpart in the reference):
- * same arguments, same results.  It is for callers that must not allocate device
- * memory during a run, e.g. a pipeline whose other streams must not be stalled by
- * the device-wide synchronisation cudaFree implies, or one whose memory pool has
- * claimed the free HBM up front.  Its twiddle tables live in one fixed 32 KiB
- * device array shared by every call, so w2 and h2 must each be 1..1024 (larger
- * sizes return EMIDA_GB_INVALID_ARGUMENT), and calls that overlap in time on the
- * same device (other host threads) race on that array.  The first call on each
- * device looks the array's address up with that device current; make that first
- * call before any stream capture begins.  Each call writes both tables before
- * its kernels read them, so nothing in the array has to start at zero. */
+ * same arguments, same results, bit for bit.  It is for callers that must not
+ * allocate device memory during a run: cudaFree synchronises the whole device,
+ * which would stall a pipeline's other streams, and a caller whose memory pool
+ * has claimed the free HBM up front has nothing left to allocate from.  Its
+ * twiddle tables live in one fixed 32 KiB device array shared by every call,
+ * so w2 and h2 must each be 1..1024 (larger sizes return
+ * EMIDA_GB_INVALID_ARGUMENT), and calls that overlap in time on the same
+ * device (from other host threads) race on that array.  The call runs on a
+ * non-blocking stream of the library's own and waits for that stream only:
+ * it orders nothing against the caller's streams, so real_in must be complete
+ * before the call and spec is complete when it returns.  The first call on
+ * each device, with that device current, looks the array's address up and
+ * creates the stream; make that first call before any stream capture begins
+ * (a condition on the first call only, not a statement about later calls).
+ * Each call writes both tables before its kernels read them, so nothing in
+ * the array has to start at zero. */
 int emida_gb_run_fft_r2c_noalloc(const void *real_in, void *spec, uint32_t maps, uint32_t w2,
                                  uint32_t h2, int precision);
 /* unnormalised C2R of [maps][h2][w2/2+1] (overwritten) into [maps][h2][w2] real. */

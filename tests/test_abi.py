@@ -51,9 +51,11 @@ def test_python_constants_match_header_enums():
         assert getattr(_lib, name) == enums["EMIDA_GB_" + name], name
     ingest = {k[len("EMIDA_GB_INGEST_"):].lower(): v for k, v in enums.items()
               if k.startswith("EMIDA_GB_INGEST_")}
-    assert len(ingest) == len(GpuOffset.INGEST)
+    names = [n for n in GpuOffset.INGEST if n is not None]
+    assert len(ingest) == len(names)
     for i, name in enumerate(GpuOffset.INGEST):
-        assert ingest[name] == i, name
+        if name is not None:
+            assert ingest[name] == i, name
 
 
 @pytest.mark.parametrize("s", [3, 5, 7, 9])

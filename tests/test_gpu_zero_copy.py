@@ -60,7 +60,7 @@ def test_submit_reads_pinned_batches_in_place(data):
     host = pinned_array(pics.shape)
     host[:] = pics
     expect = [g.get_offset(pics[k:k + 3]) for k in (0, 3)]
-    for mode in ("in_place", "split", "copy", "sm_copy"):
+    for mode in ("in_place", "copy", "sm_copy"):
         g.ingest = mode
         assert g.ingest == mode  # 16 ROIs of 64^2 cover a quarter of a 512^2 pattern
         tickets = [g.submit(host[k:k + 3]) for k in (0, 3, 0)]
@@ -71,7 +71,7 @@ def test_submit_reads_pinned_batches_in_place(data):
     # ROIs that cover most of the pattern are copied, not read in place
     _, dense = __import__("emida_gb300").synth.roi_grid(512, 7, 32, margin=32)
     g = GpuOffset((512, 512), dense, (64, 64), (127, 127), 1, "fft", 5, 1, "float", np.uint16, "fused")
-    g.ingest = "split"
+    g.ingest = "in_place"
     assert g.ingest == "copy"
     g.close()
 

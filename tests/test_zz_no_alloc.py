@@ -1,8 +1,10 @@
 """emida_gb_run_fft_r2c_noalloc: the forward FFT with its twiddle tables in a
-fixed device array instead of allocated memory.  Its spectra must match
-emida_gb_run_fft_r2c's on the same input, call after call, since every call
-rewrites the shared tables.  The file name sorts last so the entry point is also
-exercised after every other test in the same process."""
+fixed device array instead of allocated memory, for callers that must not
+allocate device memory mid-run.  Both forms compute the same twiddles on the
+host and run the same kernels, so the spectra must be the same bits, call after
+call (every call rewrites the shared tables), and agree with numpy's rfft2.
+The file name sorts last so the entry point is also exercised after every other
+test in the same process."""
 import numpy as np
 import pytest
 
@@ -32,18 +34,26 @@ def _spectra(name, x, precision):
     return spec.download(cdt, (maps, h2, half))
 
 
+# consecutive calls with different sizes and precisions: each must see its own
+# tables.  (1, 1024, 1024) DOUBLE fills the column table to the array's last
+# byte; (2, 1024, 96) has a full-length row table beside a short column table.
+CASES = [((3, 128, 128), DOUBLE), ((2, 80, 96), FLOAT), ((4, 48, 64), DOUBLE),
+         ((1, 1024, 1024), FLOAT), ((1, 1024, 1024), DOUBLE), ((2, 1024, 96), DOUBLE),
+         ((2, 96, 1024), FLOAT)]
+
+
 @pytest.mark.gpu
-def test_noalloc_matches_allocating_entry_point():
+def test_noalloc_matches_allocating_entry_point_and_numpy():
     rng = np.random.default_rng(2024)
-    # consecutive calls with different sizes and precisions: each must see its own tables
-    cases = [((3, 128, 128), DOUBLE), ((2, 80, 96), FLOAT), ((4, 48, 64), DOUBLE),
-             ((1, 1024, 1024), FLOAT)]
-    for shape, precision in cases:
-        x = rng.normal(size=shape).astype(np.float64 if precision == DOUBLE else np.float32)
+    for (maps, h2, w2), precision in CASES:
+        x = rng.normal(size=(maps, h2, w2)).astype(np.float64 if precision == DOUBLE else np.float32)
         exp = _spectra("emida_gb_run_fft_r2c", x, precision)
         got = _spectra("emida_gb_run_fft_r2c_noalloc", x, precision)
-        rel = 1e-10 if precision == DOUBLE else 1e-5
-        assert np.abs(got - exp).max() <= rel * np.abs(exp).max(), (shape, precision)
+        assert np.array_equal(got, exp), ((maps, h2, w2), precision)
+        ref = np.fft.rfft2(x.astype(np.float64))
+        rel = 1e-12 if precision == DOUBLE else 2e-5
+        err = np.abs(got - ref).max() / np.abs(ref).max()
+        assert err <= rel, ((maps, h2, w2), precision, err)
 
 
 @pytest.mark.gpu
@@ -53,8 +63,7 @@ def test_noalloc_twice_in_a_row_same_input():
     exp = _spectra("emida_gb_run_fft_r2c", x, DOUBLE)
     first = _spectra("emida_gb_run_fft_r2c_noalloc", x, DOUBLE)
     second = _spectra("emida_gb_run_fft_r2c_noalloc", x, DOUBLE)
-    for got in (first, second):
-        assert np.abs(got - exp).max() <= 1e-10 * np.abs(exp).max()
+    assert np.array_equal(first, exp) and np.array_equal(second, exp)
 
 
 def test_noalloc_rejects_sizes_beyond_the_scratch():
