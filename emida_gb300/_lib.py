@@ -82,6 +82,9 @@ SIGNATURES = {
     "emida_gb_ingest": [_VP],
     "emida_gb_set_ingest": [_VP, _I32],
     "emida_gb_stream": [_VP],
+    "emida_gb_streams": [_VP, ctypes.POINTER(_VP), ctypes.POINTER(_VP)],
+    "emida_gb_stage_buffers": [_VP, ctypes.POINTER(_VP), ctypes.POINTER(_VP), ctypes.POINTER(_VP)],
+    "emida_gb_cross_corr_fft": [_VP],
     "emida_gb_launches_per_run": [_VP],
     "emida_gb_destroy": [_VP],
     "emida_gb_last_error": [],

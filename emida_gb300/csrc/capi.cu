@@ -478,6 +478,64 @@ __global__ void k_selftest_wait(uint32_t *err, long long budget)
 
 }  // namespace
 
+namespace {
+
+// The staged form's buffers behind the test hooks (src/gpu_offset.hpp:303-325):
+// the staged handle's own, or for the fused and tensor forms, which keep no
+// such buffers, a set at the staged sizes made on first use.  With the FFT
+// policy and a reference registered, the set's reference spectra are computed
+// from the registered pattern.
+int stage_hooks(emida_gb_handle *h)
+{
+    auto &k = h->hk;
+    if (k.ready) return EMIDA_GB_OK;
+    if (h->mode == EMIDA_GB_MODE_PLAIN) {
+        k.pic = h->d_prep;
+        k.temp = h->fft ? h->d_ref_spec : h->d_ref_prep;
+        k.spec = h->d_spec;
+        k.map = h->d_map;
+        k.tw_row = h->d_tw_row;
+        k.tw_col = h->d_tw_col;
+        k.ready = true;
+        return EMIDA_GB_OK;
+    }
+    if (!h->fft) {
+        // the tensor form: FP32 prepared patterns and brute maps; its FP32
+        // reference ROIs are the ones set_reference prepares
+        CKS(h->alloc(&k.pic, (size_t)h->slice.x * h->slice.y * h->N * h->t_elem, true));
+        CKS(h->alloc(&k.map, (size_t)h->cross.x * h->cross.y * h->N * h->t_elem, true));
+        k.temp = h->d_ref_prep;
+        k.ready = true;
+        return EMIDA_GB_OK;
+    }
+    const uint32_t w2 = 2 * h->slice.x, h2 = 2 * h->slice.y, half = w2 / 2 + 1;
+    CKS(h->alloc(&k.pic, (size_t)w2 * h2 * h->N * h->t_elem, true));
+    CKS(h->alloc(&k.ref_prep, (size_t)w2 * h2 * h->S * h->t_elem, true));
+    CKS(h->alloc(&k.temp, (size_t)h2 * half * h->S * h->c_elem, true));
+    CKS(h->alloc(&k.spec, (size_t)h2 * half * h->N * h->c_elem));
+    CKS(h->alloc(&k.map, (size_t)w2 * h2 * h->N * h->t_elem, true));
+    CKS(upload_twiddles(h, &k.tw_row, w2));
+    CKS(upload_twiddles(h, &k.tw_col, h2));
+    k.ready = true;
+    if (h->ref_set) CKS(stage_hooks_reference(h));
+    return EMIDA_GB_OK;
+}
+
+}  // namespace
+
+int emida_gb::host::stage_hooks_reference(emida_gb_handle *h)
+{
+    auto &k = h->hk;
+    if (!k.ready || !k.ref_prep) return EMIDA_GB_OK;
+    const uint32_t w2 = 2 * h->slice.x, h2 = 2 * h->slice.y;
+    const int in_type = h->in_f64 ? IN_F64 : IN_U16;
+    CK(run_prepare(h->d_ref_in, in_type, h->dbl, k.ref_prep, h->d_hann, h->d_sums_ref, h->d_begins,
+                   h->src, h->slice, size2{w2, h2}, h->S, 1, h->comp));
+    CK(run_fft_r2c(k.ref_prep, k.temp, h->S, fft_tables{k.tw_row, k.tw_col, w2, h2}, h->dbl, h->comp));
+    CK(cudaStreamSynchronize(h->comp));
+    return EMIDA_GB_OK;
+}
+
 extern "C" {
 
 const char *emida_gb_last_error(void) { return g_last_error.c_str(); }
@@ -583,8 +641,11 @@ int emida_gb_create(const emida_gb_params *p, emida_gb_handle **out)
         CK(cudaStreamCreateWithFlags(&h->out_stream, cudaStreamNonBlocking));
         CK(cudaStreamCreateWithFlags(&h->comp, cudaStreamNonBlocking));
         CK(cudaEventCreateWithFlags(&h->comp_done, cudaEventDisableTiming));
+        CK(cudaEventCreateWithFlags(&h->out_done, cudaEventDisableTiming));
         h->in_done.resize(h->p.in_buffers);
         for (auto &e : h->in_done) CK(cudaEventCreateWithFlags(&e, cudaEventDisableTiming));
+        h->in_used.resize(h->p.in_buffers);
+        for (auto &e : h->in_used) CK(cudaEventCreateWithFlags(&e, cudaEventDisableTiming));
         return EMIDA_GB_OK;
     }());
     const size_t pat_bytes = (size_t)h->src.x * h->src.y * h->in_elem;
@@ -689,7 +750,7 @@ int emida_gb_set_reference(emida_gb_handle *h, const void *ref)
     if (h->mode == EMIDA_GB_MODE_TENSOR) CK(preload_brute_tc());
     CK(cudaStreamSynchronize(h->comp));
     h->ref_set = true;
-    return EMIDA_GB_OK;
+    return stage_hooks_reference(h);
 }
 
 int emida_gb_transfer_async(emida_gb_handle *h, const void *batch, uint32_t *buffer_index)
@@ -697,6 +758,10 @@ int emida_gb_transfer_async(emida_gb_handle *h, const void *batch, uint32_t *buf
     trace_range tr("emida_gb_transfer_async");
     if (!h || !batch) return fail(EMIDA_GB_INVALID_ARGUMENT, "null argument");
     const uint32_t i = h->in_next.fetch_add(1) % (uint32_t)h->d_in.size();
+    // offsets_core returns before its kernels have read the buffer (the
+    // reference's waits for the device): the copy waits for the last
+    // offsets_core that read this buffer
+    CK(cudaStreamWaitEvent(h->in_stream, h->in_used[i], 0));
     CKS(copy_patterns(h, h->d_in[i], batch, h->B, h->in_stream));
     CK(cudaEventRecord(h->in_done[i], h->in_stream));
     if (buffer_index) *buffer_index = i;
@@ -712,7 +777,12 @@ int emida_gb_offsets_core(emida_gb_handle *h, uint32_t buffer_index, void *maxes
     if (!h->ref_set) return fail(EMIDA_GB_INVALID_ARGUMENT, "reference pattern not set");
     std::lock_guard<std::mutex> lk(h->mu);
     CK(cudaStreamWaitEvent(h->comp, h->in_done[buffer_index], 0));
+    // the previous call's copies of the maxima and neighbourhoods read the
+    // buffers this call overwrites (the reference's kernels on the legacy
+    // stream wait for its blocking output stream in the same way)
+    CK(cudaStreamWaitEvent(h->comp, h->out_done, 0));
     CKS(run_any(h, h->d_in[buffer_index], h->B, h->d_maxes, h->d_neigh, nullptr, nullptr, h->comp));
+    CK(cudaEventRecord(h->in_used[buffer_index], h->comp));
     CK(cudaEventRecord(h->comp_done, h->comp));
     CK(cudaStreamWaitEvent(h->out_stream, h->comp_done, 0));
     const size_t s2 = (size_t)h->p.fitsize * h->p.fitsize;
@@ -721,6 +791,7 @@ int emida_gb_offsets_core(emida_gb_handle *h, uint32_t buffer_index, void *maxes
     if (neigh_out)
         CK(cudaMemcpyAsync(neigh_out, h->d_neigh, s2 * h->t_elem * h->N, cudaMemcpyDeviceToHost,
                            h->out_stream));
+    CK(cudaEventRecord(h->out_done, h->out_stream));
     return EMIDA_GB_OK;
 }
 
@@ -767,6 +838,7 @@ int emida_gb_get_offset(emida_gb_handle *h, const void *batch, double *offsets, 
     if (!h || !batch || !offsets) return fail(EMIDA_GB_INVALID_ARGUMENT, "null argument");
     if (!h->ref_set) return fail(EMIDA_GB_INVALID_ARGUMENT, "reference pattern not set");
     std::lock_guard<std::mutex> lk(h->mu);
+    CK(cudaStreamWaitEvent(h->comp, h->out_done, 0));  // offsets_core's copies read d_maxes, d_neigh
     CKS(copy_patterns(h, h->d_in[0], batch, h->B, h->comp));
     CKS(run_any(h, h->d_in[0], h->B, h->d_maxes, h->d_neigh, h->d_offsets, h->d_coefs, h->comp));
     CK(cudaMemcpyAsync(offsets, h->d_offsets, 2 * sizeof(double) * h->N, cudaMemcpyDeviceToHost, h->comp));
@@ -1005,6 +1077,40 @@ int emida_gb_set_ingest(emida_gb_handle *h, int mode)
     return EMIDA_GB_OK;
 }
 void *emida_gb_stream(emida_gb_handle *h) { return h ? (void *)h->comp : nullptr; }
+
+int emida_gb_streams(emida_gb_handle *h, void **in_stream, void **out_stream)
+{
+    if (!h) return fail(EMIDA_GB_INVALID_ARGUMENT, "null handle");
+    if (in_stream) *in_stream = (void *)h->in_stream;
+    if (out_stream) *out_stream = (void *)h->out_stream;
+    return EMIDA_GB_OK;
+}
+
+int emida_gb_stage_buffers(emida_gb_handle *h, void **pic, void **temp, void **maps)
+{
+    if (!h) return fail(EMIDA_GB_INVALID_ARGUMENT, "null handle");
+    std::lock_guard<std::mutex> lk(h->mu);
+    CKS(stage_hooks(h));
+    if (pic) *pic = h->hk.pic;
+    if (temp) *temp = h->hk.temp;
+    if (maps) *maps = h->hk.map;
+    return EMIDA_GB_OK;
+}
+
+int emida_gb_cross_corr_fft(emida_gb_handle *h)
+{
+    trace_range tr("emida_gb_cross_corr_fft");
+    if (!h) return fail(EMIDA_GB_INVALID_ARGUMENT, "null handle");
+    if (!h->fft) return fail(EMIDA_GB_UNSUPPORTED, "cross_corr_fft needs the FFT policy");
+    std::lock_guard<std::mutex> lk(h->mu);
+    CKS(stage_hooks(h));
+    const fft_tables t{h->hk.tw_row, h->hk.tw_col, 2 * h->slice.x, 2 * h->slice.y};
+    CK(run_fft_r2c(h->hk.pic, h->hk.spec, h->N, t, h->dbl, h->comp));
+    CK(run_hadamard(h->hk.spec, h->hk.temp, t.h2 * (t.w2 / 2 + 1), h->S, h->B, h->dbl, h->comp));
+    CK(run_fft_c2r(h->hk.spec, h->hk.map, h->N, t, h->dbl, h->comp));
+    CK(cudaStreamSynchronize(h->comp));
+    return EMIDA_GB_OK;
+}
 int emida_gb_launches_per_run(const emida_gb_handle *h)
 {
     if (!h) return -1;
@@ -1030,7 +1136,10 @@ void emida_gb_destroy(emida_gb_handle *h)
     for (void *p : h->allocs) cudaFree(p);
     for (auto e : h->in_done)
         if (e) cudaEventDestroy(e);
+    for (auto e : h->in_used)
+        if (e) cudaEventDestroy(e);
     if (h->comp_done) cudaEventDestroy(h->comp_done);
+    if (h->out_done) cudaEventDestroy(h->out_done);
     if (h->comp) cudaStreamDestroy(h->comp);
     if (h->comp_alt) cudaStreamDestroy(h->comp_alt);
     if (h->in_stream) cudaStreamDestroy(h->in_stream);

@@ -77,6 +77,9 @@ int run_any(emida_gb_handle *h, const void *pics, uint32_t pats, void *maxes, vo
 int check_device_error(emida_gb_handle *h, uint32_t *word = nullptr);
 // EMIDA_GB_OK for no flags, else EMIDA_GB_DEVICE_CHECK with the flags named.
 int device_flags_status(uint32_t flags);
+// Recomputes the test hooks' reference spectra (fused and tensor forms) from
+// the registered reference pattern; nothing when no hook buffers exist.
+int stage_hooks_reference(emida_gb_handle *h);
 // Host -> device copy of `patterns` whole patterns as the kernels need them:
 // only the row bands that hold ROI pixels (one pitched copy per band over all
 // patterns), or everything when the bands cover most of a pattern.
@@ -122,7 +125,9 @@ struct emida_gb_handle {
     size_t in_elem = 2, t_elem = 4, c_elem = 8, di_elem = 8;
     cudaStream_t in_stream = nullptr, out_stream = nullptr, comp = nullptr;
     std::vector<cudaEvent_t> in_done;
+    std::vector<cudaEvent_t> in_used;  // per input buffer: offsets_core's kernels that read it
     cudaEvent_t comp_done = nullptr;
+    cudaEvent_t out_done = nullptr;  // offsets_core's result copies on the output stream
     std::vector<void *> d_in;
     std::atomic<uint32_t> in_next{0};
     void *d_ref_in = nullptr;
@@ -177,6 +182,14 @@ struct emida_gb_handle {
     // stream, so that a batch's path starts on the CTA slots the previous
     // batch's last CTAs leave free instead of after its tail.
     cudaStream_t comp_alt = nullptr;
+    // The staged form's buffers behind emida_gb_stage_buffers and
+    // emida_gb_cross_corr_fft (the reference's test hooks): the staged form's
+    // own, or a set at the staged sizes made on first use by the other forms.
+    struct stage_hook_buffers {
+        bool ready = false;
+        void *pic = nullptr, *temp = nullptr, *spec = nullptr, *map = nullptr, *ref_prep = nullptr;
+        void *tw_row = nullptr, *tw_col = nullptr;
+    } hk;
     // emida_gb_selftest_arm_submit: the next submit's slot word is set by a
     // bounded wait of this many cycles that runs out (0: not armed)
     int64_t selftest_budget = 0;

@@ -81,13 +81,17 @@ int emida_gb_set_reference(emida_gb_handle *h, const void *ref);
 
 /* transfer_pic_to_device_async (src/gpu_offset.hpp:213-218): asynchronous copy
  * of one batch from (pinned) host memory into the next input buffer on the
- * input stream; thread-safe; returns the buffer index. */
+ * input stream; thread-safe; returns the buffer index.  The copy waits on the
+ * device for the last emida_gb_offsets_core that read that buffer, as
+ * offsets_core returns before its kernels have run. */
 int emida_gb_transfer_async(emida_gb_handle *h, const void *batch, uint32_t *buffer_index);
 
 /* get_offset_core (src/gpu_offset.hpp:234-278): runs the path on input buffer
  * `buffer_index` (after the input stream) and copies the per-ROI maxima
  * (data_index<T> {T value; uint32 index}) and s*s neighbourhoods (T) to the
- * host buffers, asynchronously on the output stream.  Either may be NULL. */
+ * host buffers, asynchronously on the output stream.  Either may be NULL.
+ * Its kernels wait for the previous call's result copies, which read the
+ * device buffers this call overwrites. */
 int emida_gb_offsets_core(emida_gb_handle *h, uint32_t buffer_index, void *maxes_out,
                           void *neigh_out);
 
@@ -167,6 +171,33 @@ int emida_gb_set_ingest(emida_gb_handle *h, int mode);
 int emida_gb_ingest(const emida_gb_handle *h);
 /* The handle's compute stream (a cudaStream_t). */
 void *emida_gb_stream(emida_gb_handle *h);
+/* The public in_stream and out_stream members of gpu_offset
+ * (src/gpu_offset.hpp:96-97): the streams of transfer_async's copies and of
+ * offsets_core's result copies, as cudaStream_t values that the caller's own
+ * CUDA runtime accepts (src/process_files.hpp:196 synchronises in_stream).
+ * Either pointer may be NULL. */
+int emida_gb_streams(emida_gb_handle *h, void **in_stream, void **out_stream);
+/* The test hooks get_cu_pic() and get_cu_temp() of gpu_offset
+ * (src/gpu_offset.hpp:318-325), plus the correlation maps they produce:
+ * device buffers of the staged form, T = the handle's precision.
+ *   FFT policy:   pic  [batch*n_rois][2*slice_h][2*slice_w] T, the prepared,
+ *                      zero-padded ROIs (the R2C input);
+ *                 temp [n_rois][2*slice_h][slice_w+1] complex T, the reference
+ *                      spectra (computed by set_reference);
+ *                 maps [batch*n_rois][2*slice_h][2*slice_w] T, the C2R output.
+ *   brute policy: pic  [batch*n_rois][slice_h][slice_w] T, temp [n_rois][slice_h]
+ *                 [slice_w] T (the prepared reference ROIs), maps
+ *                 [batch*n_rois][cross_h][cross_w] T.
+ * The staged form (EMIDA_GB_MODE_PLAIN) returns the buffers its
+ * offsets_core uses; the fused and tensor forms keep no such buffers, so the
+ * first call makes a set at these sizes for the hooks alone.  Any pointer may
+ * be NULL. */
+int emida_gb_stage_buffers(emida_gb_handle *h, void **pic, void **temp, void **maps);
+/* The test hook cross_corr_fft() (src/gpu_offset.hpp:303-316): R2C of the
+ * pic buffer, the product with the conjugate reference spectra of temp, and
+ * the unnormalised C2R into maps, on the compute stream; returns when done.
+ * FFT policy only. */
+int emida_gb_cross_corr_fft(emida_gb_handle *h);
 /* Number of kernel launches one emida_gb_run_device call makes. */
 int emida_gb_launches_per_run(const emida_gb_handle *h);
 void emida_gb_destroy(emida_gb_handle *h);

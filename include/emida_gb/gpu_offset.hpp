@@ -7,6 +7,12 @@
 // member signatures, types (src/common.hpp:24-145, src/subpixel_max.hpp:69-74)
 // and failure behaviour (std::runtime_error).  The device buffers are freed by
 // the destructor (the reference never frees them).
+//
+// The public in_stream and out_stream members are the library's own streams,
+// set by allocate_memory; the caller's CUDA runtime accepts them
+// (cudaStreamSynchronize(offs.in_stream) as src/process_files.hpp:196 does).
+// This header needs no CUDA header: cudaStream_t is declared as the CUDA
+// headers declare it, so either may be included first.
 #pragma once
 
 #include <array>
@@ -17,6 +23,9 @@
 #include <vector>
 
 #include "../emida_gb.h"
+
+struct CUstream_st;
+typedef struct CUstream_st *cudaStream_t;
 
 namespace emida {
 
@@ -69,6 +78,10 @@ class gpu_offset {
     int mode_ = EMIDA_GB_MODE_AUTO;
 
 public:
+    // src/gpu_offset.hpp:96-97
+    cudaStream_t in_stream = nullptr;
+    cudaStream_t out_stream = nullptr;
+
     gpu_offset() {}
     gpu_offset(size2_t src_size, const std::vector<size2_t> *begins, size2_t slice_size,
                size2_t cross_size, esize_t batch_size, cross_policy policy = CROSS_POLICY_BRUTE,
@@ -106,6 +119,8 @@ public:
         total_slices_ = o.total_slices_;
         s_ = o.s_;
         mode_ = o.mode_;
+        std::swap(in_stream, o.in_stream);
+        std::swap(out_stream, o.out_stream);
         return *this;
     }
     ~gpu_offset() { emida_gb_destroy(h_); }
@@ -116,6 +131,10 @@ public:
         if (!h_) {
             p_.begins = begins_.data();
             check_status(emida_gb_create(&p_, &h_));
+            void *in = nullptr, *out = nullptr;
+            check_status(emida_gb_streams(h_, &in, &out));
+            in_stream = static_cast<cudaStream_t>(in);
+            out_stream = static_cast<cudaStream_t>(out);
         }
         if (temp) check_status(emida_gb_set_reference(h_, temp));
     }
@@ -152,6 +171,27 @@ public:
         check_status(emida_gb_finalize(h_, maxes_i, neighbors, o.data(), c.data()));
         unpack(o, c, r);
         return r;
+    }
+
+    // src/gpu_offset.hpp:303-316: R2C of get_cu_pic(), the conjugate product
+    // with get_cu_temp()'s reference spectra, and the C2R into the correlation
+    // maps (returns when they are done)
+    void cross_corr_fft() const { check_status(emida_gb_cross_corr_fft(h_)); }
+
+    // src/gpu_offset.hpp:318-321: device buffer of the prepared patterns
+    T *get_cu_pic()
+    {
+        void *p = nullptr;
+        check_status(emida_gb_stage_buffers(h_, &p, nullptr, nullptr));
+        return static_cast<T *>(p);
+    }
+    // src/gpu_offset.hpp:322-325: device buffer of the reference spectra (FFT
+    // policy) or of the prepared reference ROIs (brute policy)
+    T *get_cu_temp()
+    {
+        void *p = nullptr;
+        check_status(emida_gb_stage_buffers(h_, nullptr, &p, nullptr));
+        return static_cast<T *>(p);
     }
 
     esize_t total_slices() const { return total_slices_; }
