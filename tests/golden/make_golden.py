@@ -1,10 +1,10 @@
 #!/usr/bin/env python3
 """Regenerates the golden fixtures in tests/golden/ from the reference tree.
 
-Run where the reference is mounted (its path is the REF variable below, or the
-first argument).  It converts the reference's own test fixtures to .npy, lifts
+Run where the reference is mounted (its path is the first argument, or the
+EMIDA_REFERENCE environment variable).  It converts the reference's own test fixtures to .npy, lifts
 the expected offsets out of its end-to-end test, and records the outputs of the
-reference's CPU code (built by `make -C oracle ref`) on seeded inputs, so that the
+reference's CPU code (built by `make -C oracle stage ref REF=...`) on seeded inputs, so that the
 oracle stays pinned on machines where the reference tree is absent.
 
 Sources:
@@ -26,7 +26,9 @@ import numpy as np
 
 HERE = os.path.dirname(os.path.abspath(__file__))
 REPO = os.path.dirname(os.path.dirname(HERE))
-REF = sys.argv[1] if len(sys.argv) > 1 else "/root/reference"
+REF = sys.argv[1] if len(sys.argv) > 1 else os.environ.get("EMIDA_REFERENCE", "")
+if not REF or not os.path.isdir(os.path.join(REF, "src")):
+    sys.exit("usage: %s REFERENCE_TREE (or set EMIDA_REFERENCE)" % sys.argv[0])
 
 
 def load_matrix(path, dtype):

@@ -2,9 +2,9 @@
 """Golden vectors for the deformation-gradient (projective) fit downstream of
 the path, made by running the reference's own python/process_offsets.py.
 
-Run where the reference is mounted (the REF variable below, or the first
-argument).  The script is fed seeded synthetic ROI offsets in the format it
-reads (a ROI count, then per pattern a name line and "x y dx dy" lines).  It
+Run where the reference is mounted (its path is the first argument, or the
+EMIDA_REFERENCE environment variable).  The script is fed seeded synthetic ROI
+offsets in the format it reads (a ROI count, then per pattern a name line and "x y dx dy" lines).  It
 imports `pylab` only for numpy's names; a stand-in module that re-exports numpy
 (printing at full precision) is put on its path, so the reference's own
 arithmetic produces the recorded matrices.  Output: homography_golden.npz with
@@ -19,7 +19,9 @@ import tempfile
 import numpy as np
 
 HERE = os.path.dirname(os.path.abspath(__file__))
-REF = sys.argv[1] if len(sys.argv) > 1 else "/root/reference"
+REF = sys.argv[1] if len(sys.argv) > 1 else os.environ.get("EMIDA_REFERENCE", "")
+if not REF or not os.path.isdir(os.path.join(REF, "src")):
+    sys.exit("usage: %s REFERENCE_TREE (or set EMIDA_REFERENCE)" % sys.argv[0])
 N = 873  # process_offsets.py fixes the pattern size, hence the centre (436, 436, 436)
 
 PYLAB = '''import sys
