@@ -18,12 +18,19 @@ copied), the path, and the offsets, coefficients and maxima back to the host.
 The timed steps run as one stream of batches, as a scan is processed;
 one_step_ms is a single step with the pipeline filled and drained inside it.
 e2e_ingest: the same with the other ingest modes (kernels reading each batch's
-ROI pixels in place, alternating batches, gathered ROI rows, row bands copied
-by SM loads).
+ROI pixels in place, gathered ROI rows, row bands copied by the copy engine).
+plain_reference: the reference's own staged GPU pipeline (its gpu_offset with
+cuFFT, compiled from its sources for sm_103a) on the same job, device-resident
+and end to end; over_plain_reference gives this form's ratios to it.
+fp64, tensor, serving: the job in float64 (fused form beside the reference's
+float64 pipeline), the brute policy on the tensor cores at fit size 7, and
+rows of the detector layout arriving at 100 rows/s for 4 s (p50/p99).
 
---impl reference times the reference algorithm on the host cores instead (the
-CPU FP64 oracle port of the same path; the reference's own CPU code is built
-only where its source tree is mounted).
+cpu_baseline and --impl reference time the reference's own CPU code on all host
+cores (sums_serial, cross_corr_serial over the 127 x 127 lags -- it has no CPU
+FFT path -- and subpixel_max_serial, compiled from its sources staged into
+baseline/_ref), in the GPU arm's precision, on a bounded sample of the job's
+pairs; cpu_port_fft is the oracle's FP64 FFT restatement beside it.
 
 Multi-GPU: patterns are independent, so N ranks each process their own 256
 patterns (weak scaling, no collective on the data path).
@@ -75,6 +82,8 @@ def parse():
                          "pinned host detector patterns in place (cp.async staging); the 64-, 96- "
                          "and 192-point fused kernels (1024^2, 10 x 10 ROIs of 32^2, 48^2 or 96^2)")
     ap.add_argument("--no-plain", action="store_true", help="skip the plain-form comparison")
+    ap.add_argument("--no-legs", action="store_true",
+                    help="skip the reference's staged GPU pipeline, the FP64, tensor and serving legs")
     ap.add_argument("--sample-seconds", type=float, default=0.0,
                     help="reference arm: seconds of host work per step (default: ~20 s in all)")
     ap.add_argument("--in-flight", type=int, default=3,
@@ -193,8 +202,19 @@ def well_posed(coefs, s):
     return np.repeat(((x >= 0) & (x <= s - 1) & (y >= 0) & (y <= s - 1))[:, None], 2, axis=1)
 
 
-def cpu_reference(ref, uniq, begins, seconds, threads):
-    """The reference algorithm (FP64 FFT policy, s=5) on the host cores."""
+DETECTOR_WORKLOAD = "256 x 1024^2 uint16 patterns, 100 ROIs r=32 (64x64), FFT 128x128, s=5, batch 32"
+
+
+def detector_config(P, S, world, precision):
+    """The detector workload's config object, the same in both arms."""
+    return {"workload": DETECTOR_WORKLOAD, "patterns": P, "rois": S, "radius": 32, "fitsize": 5,
+            "batch": 32, "precision": precision, "l2": "inputs larger than L2 (512 MB of patterns)",
+            "parallelism": f"patterns sharded over {world} GPU(s)"}
+
+
+def cpu_port(ref, uniq, begins, seconds, threads):
+    """The oracle's C restatement (FP64, FFT policy, s=5) on the host cores:
+    (pairs/s, pairs, seconds)."""
     from oracle import oracle as eo
     eo.lib()
     stop = time.perf_counter() + seconds
@@ -219,30 +239,95 @@ def cpu_reference(ref, uniq, begins, seconds, threads):
     return pairs / dt, pairs, dt
 
 
+class CpuReference:
+    """The reference's own CPU code on the host cores, one ROI pair per call:
+    sums_serial, generate_hanning, cross_corr_serial (127 x 127 lags; the
+    reference has no CPU FFT path) and subpixel_max_serial, in `precision`,
+    compiled from its sources into oracle/_ref (oracle/ref_harness.cpp).
+    Falls back to the oracle port where oracle/_ref was not built."""
+
+    def __init__(self, ref, uniq, begins, precision):
+        from oracle import oracle as eo
+        self.eo, self.uniq, self.begins, self.precision = eo, uniq, begins, precision
+        self.ref, self.lib = ref, eo.ref_lib()
+        self.kind = "reference" if self.lib is not None else "port"
+        if self.lib is not None:
+            self.prep = eo.ref_prepare_reference(self.lib, ref, begins, 64, precision)
+
+    def pair(self, i):
+        S = len(self.begins)
+        p, r = (i // S) % len(self.uniq), i % S
+        return self.eo.ref_brute_pattern(self.lib, self.prep[r:r + 1], self.uniq[p], self.begins[r:r + 1],
+                                         64, 127, 5, self.precision)
+
+    def parity(self, n_pairs):
+        """Max |offset - FP64 oracle| (px) and peak agreement over the first pairs."""
+        eo = self.eo
+        o_offs, _, o_peaks = eo.get_offsets(self.ref, self.uniq[:1], self.begins, 64, 64,
+                                            eo.POLICY_BRUTE, 5, 127, 127)
+        got = [self.pair(i) for i in range(n_pairs)]
+        err = max(float(np.abs(o[0] - o_offs[i]).max()) for i, o in enumerate(got))
+        match = float(np.mean([o[1][0] == o_peaks[i] for i, o in enumerate(got)]))
+        return err, match
+
+    def run(self, seconds, threads):
+        """(pairs/s, pairs, seconds) of `seconds` of work on `threads` threads."""
+        if self.lib is None:
+            return cpu_port(self.ref, self.uniq, self.begins, seconds, threads)
+        stop = time.perf_counter() + seconds
+        counter = iter(range(1 << 40))
+        lock = threading.Lock()
+        done = []
+
+        def worker(_):
+            n = 0
+            while time.perf_counter() < stop:
+                with lock:
+                    i = next(counter)
+                self.pair(i)
+                n += 1
+            with lock:
+                done.append(n)
+
+        t0 = time.perf_counter()
+        with cf.ThreadPoolExecutor(threads) as ex:
+            list(ex.map(worker, range(threads)))
+        dt = time.perf_counter() - t0
+        return sum(done) / dt, sum(done), dt
+
+
 def run_reference(args, rank, world):
+    """The reference's own CPU implementation of the path on all host cores,
+    on the detector workload's pairs, in the GPU arm's precision; each step is
+    a bounded sample of that workload."""
     if rank != 0:
         return
     ref, uniq, begins = workload()
     threads = os.cpu_count() or 1
-    per_step = args.sample_seconds or max(2.0, 20.0 / max(1, args.steps + args.warmup))
+    per_step = args.sample_seconds or max(0.5, 20.0 / max(1, args.steps + args.warmup))
+    cpu = CpuReference(ref, uniq, begins, args.precision)
+    err, match = cpu.parity(2) if cpu.kind == "reference" else (None, None)
     vals = []
     for i in range(args.warmup + args.steps):
-        v, pairs, dt = cpu_reference(ref, uniq, begins, per_step, threads)
+        v, pairs, dt = cpu.run(per_step, threads)
         if i >= args.warmup:
             vals.append((v, pairs, dt))
     value = sum(p for _, p, _ in vals) / sum(d for _, _, d in vals)
-    ref_lib = os.path.exists(os.path.join(ROOT, "oracle", "_ref", "libemida_ref.so"))
-    sample = (f"{sum(p for _, p, _ in vals)} ROI pairs of the 1024^2 / 100-ROI / FFT / s=5 "
-              f"workload over {args.steps} steps of ~{per_step:.1f} s, FP64")
+    what = (f"the reference's own CPU code (sums_serial, cross_corr_serial over 127x127 lags, "
+            f"subpixel_max_serial) in {args.precision}, one ROI pair per call on {threads} threads"
+            if cpu.kind == "reference" else "the oracle's FP64 C restatement (FFT policy)")
+    sample = (f"{sum(p for _, p, _ in vals)} ROI pairs of the workload over {args.steps} steps of "
+              f"~{per_step:.1f} s: {what}")
     line = {
         "impl": "reference", "metric": METRIC, "value": value, "unit": "ROI pairs/s",
         "n_gpus": args.gpus, "steps": args.steps, "warmup": args.warmup,
         "ms_per_step": 1000.0 * 25600 / value, "higher_is_better": True, "scaling": "weak",
-        "vs_baseline": None, "dtype": "f64", "data": "synthetic",
-        "config": {"workload": "256 x 1024^2 uint16 patterns, 100 ROIs r=32, FFT, s=5, batch 32",
-                   "patterns": 256, "rois": 100, "radius": 32, "fitsize": 5},
-        "cpu_baseline": {"value": value, "unit": "ROI pairs/s", "cores": threads,
-                         "kind": "port" if not ref_lib else "reference", "sample": sample},
+        "vs_baseline": None, "dtype": "f32" if args.precision == "float" else "f64", "data": "synthetic",
+        "config": detector_config(256, len(begins), world, args.precision),
+        "cpu_baseline": {"value": value, "unit": "ROI pairs/s", "cores": threads, "kind": cpu.kind,
+                         "sample": sample},
+        "parity": {"max_abs_err_px": err, "peak_match_rate": match,
+                   "vs": "FP64 oracle (brute), first 2 pairs"},
         "e2e": {"value": value, "unit": "ROI pairs/s", "h2d_bytes_per_step": 0,
                 "d2h_bytes_per_step": 0},
     }
@@ -367,16 +452,21 @@ def run_serving(args):
     512^2 or 1024^2 rows (50/50), each on one of 8 seeded layouts per size
     (25-225 ROIs of radius 24-48, fit 3-9).  --layout detector: 1024^2 rows on
     the 10 x 10 grid of 64 x 64 ROIs, fit 5."""
-    import time
     import __graft_entry__
     __graft_entry__.build_library()
+    print(json.dumps(serving_measure(args.precision, args.layout, args.rate, args.duration,
+                                     args.step_patterns, args.copy_rows)), flush=True)
+
+
+def serving_measure(precision, layout, rate, duration, step_patterns, copy_rows):
+    """The serving workload of run_serving; returns its JSON object."""
     from emida_gb300 import Server, synth
     from oracle import oracle as eo
     rng = np.random.default_rng(99)
-    detector = args.layout == "detector"
+    detector = layout == "detector"
     sizes = (1024,) if detector else (512, 1024)
-    srv = Server(args.precision, hbm_bytes=24 << 30, step_patterns=args.step_patterns,
-                 zero_copy=not args.copy_rows)
+    srv = Server(precision, hbm_bytes=24 << 30, step_patterns=step_patterns,
+                 zero_copy=not copy_rows)
     rows_src, layouts = {}, {}
     for size in sizes:
         ref = synth.reference_pattern(size, 90 + size)
@@ -410,7 +500,7 @@ def run_serving(args):
     srv.reset_stats()
     # arrivals
     pending, sent_pairs = [], 0
-    t_end = time.perf_counter() + args.duration
+    t_end = time.perf_counter() + duration
     with ClockSampler(0) as clk:
         t = time.perf_counter()
         while t < t_end:
@@ -419,32 +509,32 @@ def run_serving(args):
             n = int(rng.integers(32, 513))
             pending.append(srv.submit(lid, rows_src[size][1][:n]))
             sent_pairs += n * len(begins)
-            t += rng.exponential(1.0 / args.rate)
+            t += rng.exponential(1.0 / rate)
             delay = t - time.perf_counter()
             if delay > 0:
                 time.sleep(delay)
         for rid in pending:
             srv.wait(rid)
     st = srv.stats()
-    print(json.dumps({
+    srv.close()
+    return {
         "metric": "row latency p50/p99 and ROI pairs/s under a Poisson stream of scan rows",
         "value": st["pairs_per_s"], "unit": "ROI pairs/s", "n_gpus": 1,
         "latency_ms": {"p50": st["p50_ms"], "p99": st["p99_ms"]}, "rows": st["completed"],
         "pairs": sent_pairs, "higher_is_better": True,
-        "dtype": "f32" if args.precision == "float" else "f64", "data": "synthetic",
+        "dtype": "f32" if precision == "float" else "f64", "data": "synthetic",
         "config": {"workload": ("Poisson rows: 32-512 patterns of 1024^2, 100 ROIs of 64x64 (10x10 "
                                 "grid), fit 5" if detector else
                                 "Poisson rows: 32-512 patterns of 512^2 or 1024^2 (50/50), 8 layouts "
                                 "per size, 25-225 ROIs radius 24-48, fit 3-9"),
-                   "rate_rows_per_s": args.rate, "duration_s": args.duration,
-                   "hbm_arena_bytes_per_size": 24 << 30, "step_patterns": args.step_patterns,
-                   "rows": "copied into the device arena" if args.copy_rows else
+                   "rate_rows_per_s": rate, "duration_s": duration,
+                   "hbm_arena_bytes_per_size": 24 << 30, "step_patterns": step_patterns,
+                   "rows": "copied into the device arena" if copy_rows else
                            "pinned rows read in place by the kernels (no copy-engine transfer)"},
         "parity": {"max_abs_err_px": max(errs),
                    "rms_err_px": float(np.sqrt(np.concatenate(sq).mean())),
                    "vs": "FP64 oracle, one row per size"},
-        "clocks": clk.summary()}), flush=True)
-    srv.close()
+        "clocks": clk.summary()}
 
 
 def run_cli_config(args):
@@ -711,6 +801,117 @@ def run_profile_target(args):
     print(json.dumps({"profile_target": "homography", "patterns": n, "ms": ms.value / 5}))
 
 
+def parity_vs_oracle(offs, peaks, ref, pics, begins, policy, s, cross=None):
+    """Max and RMS |offset - FP64 oracle| over well-posed fits, and the peak
+    match rate, for the results of `pics`."""
+    from oracle import oracle as eo
+    pol = eo.POLICY_FFT if policy == "fft" else eo.POLICY_BRUTE
+    cw = cross or 127
+    o_offs, o_coefs, o_peaks = eo.get_offsets(ref, pics, begins, 64, 64, pol, s, cw, cw)
+    ok = well_posed(o_coefs, s)
+    d = np.abs(offs[:len(o_offs)] - o_offs)[ok]
+    return {"max_abs_err_px": float(d.max()), "rms_err_px": float(np.sqrt(np.mean(d ** 2))),
+            "peak_match_rate": float(np.mean(peaks[:len(o_peaks)] == o_peaks)),
+            "checked_pairs": len(o_offs)}
+
+
+def reference_plain(ref, pics, begins, precision, repeats):
+    """The reference's own staged GPU pipeline (its gpu_offset<T, uint16_t> with
+    cuFFT, src/gpu_offset.hpp:234-316) on the same job: device-resident
+    (get_offset_core over batches already in its input buffers) and end to
+    end (transfer, get_offset_core and finalize per batch from pinned memory)."""
+    from oracle import ref_gpu
+    if not ref_gpu.available():
+        return {"unavailable": "the reference's sources are not staged into baseline/_ref"}
+    P, S = len(pics), len(begins)
+    nb = P // 32
+    batches = []
+    for b in range(nb):
+        h = pinned_u16((32, 1024, 1024))
+        h[:] = pics[b * 32:(b + 1) * 32]
+        batches.append(h)
+    g = ref_gpu.RefGpuOffset(ref, begins, 64, 32, "fft", 5, precision, in_buffers=nb)
+    offs, _, peaks = g.run_batch(batches[0])
+    par = parity_vs_oracle(offs, peaks, ref, pics[:2], begins, "fft", 5)
+    g.time_core(batches, 1)
+    ms = g.time_core(batches, repeats) / repeats
+    e2e_ms = min(g.time_e2e(batches) for _ in range(2))
+    g.close()
+    return {"value": P * S / (ms / 1000.0), "ms_per_step": ms,
+            "e2e": {"value": P * S / (e2e_ms / 1000.0), "ms_per_step": e2e_ms},
+            "parity": par, "precision": precision,
+            "what": "the reference's gpu_offset<T, uint16_t> compiled unmodified with its six kernel "
+                    "files and cuFFT for sm_103a: value = get_offset_core per 32-pattern batch on "
+                    "batches already in device memory (host wall time, as it synchronises the "
+                    "device twice per batch); e2e = transfer_pic_to_device_async, get_offset_core "
+                    "and finalize per batch from pinned memory"}
+
+
+def fp64_leg(ref, pics, begins, d_pics, steps, warmup):
+    """The detector job in float64 on the fused form, beside the reference's
+    own staged pipeline in float64."""
+    from emida_gb300 import DeviceBuffer, GpuOffset, _lib
+    P, S = len(pics), len(begins)
+    g = GpuOffset((1024, 1024), begins, (64, 64), (127, 127), 32, "fft", 5, 1, "double", np.uint16, "fused")
+    g.allocate_memory(ref)
+    d_o, d_c, d_m = DeviceBuffer(P * S * 16), DeviceBuffer(P * S * 48), DeviceBuffer(P * S * 16)
+    g.run_device(d_pics, P, d_o, d_c, d_m)
+    _lib.call("emida_gb_synchronize")
+    offs = d_o.download(np.float64, (P * S, 2))
+    peaks = d_m.download(g.data_index, P * S)["index"]
+    par = parity_vs_oracle(offs, peaks, ref, pics[:2], begins, "fft", 5)
+    for _ in range(warmup):
+        g.run_device(d_pics, P, d_o)
+    _lib.call("emida_gb_synchronize")
+    with ClockSampler(0) as clk:
+        ms = g.time_device(d_pics, P, d_o, steps) / steps
+    g.close()
+    flop = P * S * (5 * 128 * 128 * 14 + 6 * 65 * 128 + 3 * 64 * 64)
+    plain = reference_plain(ref, pics, begins, "double", 2)
+    out = {"value": P * S / (ms / 1000.0), "ms_per_step": ms, "form": "fused", "parity": par,
+           "compute": {"fp64_tflops": flop / (ms / 1000.0) / 1e12, "fp64_peak_tflops_nominal": 1.25,
+                       "frac": flop / (ms / 1000.0) / 1e12 / 1.25},
+           "plain_reference": plain, "clocks": clk.summary()}
+    if "value" in plain:
+        out["over_plain_reference"] = out["value"] / plain["value"]
+    return out
+
+
+def tensor_leg(ref, pics, begins, d_pics, steps, warmup, s=7):
+    """The brute policy's 127 x 127-lag correlation on the tcgen05 tensor cores
+    (BF16 hi/lo split, FP32 accumulation; FP64 sums and fit) over the same job
+    at fit size 7, with the useful-flop roofline against a third of the
+    measured BF16 peak (the split issues three products)."""
+    from emida_gb300 import DeviceBuffer, GpuOffset, _lib
+    P, S = len(pics), len(begins)
+    g = GpuOffset((1024, 1024), begins, (64, 64), (127, 127), 32, "brute", s, 1, "float", np.uint16,
+                  "tensor")
+    g.allocate_memory(ref)
+    d_o, d_m = DeviceBuffer(P * S * 16), DeviceBuffer(P * S * 8)
+    g.run_device(d_pics, P, d_o, None, d_m)
+    _lib.call("emida_gb_synchronize")
+    offs = d_o.download(np.float64, (P * S, 2))
+    peaks = d_m.download(g.data_index, P * S)["index"]
+    par = parity_vs_oracle(offs, peaks, ref, pics[:2], begins, "brute", s)
+    for _ in range(warmup):
+        g.run_device(d_pics, P, d_o)
+    _lib.call("emida_gb_synchronize")
+    with ClockSampler(0) as clk:
+        ms = g.time_device(d_pics, P, d_o, steps) / steps
+    launches = g.launches_per_run()
+    g.close()
+    mp = os.path.join(ROOT, "MEASURED_PEAKS.json")
+    bf16, kind = (json.load(open(mp)).get("bf16_tflops"), "measured") if os.path.exists(mp) else (1900.0, "fallback")
+    useful = P * S * 2.0 * 64 ** 4 / (ms / 1000.0) / 1e12
+    issued = P * S * 3 * 2.0 * 128 * 128 * 4096 / (ms / 1000.0) / 1e12
+    return {"value": P * S / (ms / 1000.0), "ms_per_step": ms, "fitsize": s, "parity": par,
+            "roofline": {"bound": "tensor", "achieved": useful, "peak": bf16 / 3, "unit": "TFLOP/s",
+                         "frac": useful / (bf16 / 3), "peak_kind": kind,
+                         "note": "useful flops (2 x 64^4 per pair) against a third of the bf16 burst "
+                                 "peak, as the hi/lo split issues three products"},
+            "issued_tflops": issued, "launches_per_step": launches, "clocks": clk.summary()}
+
+
 def main():
     args = parse()
     rank, world, local = dist_env()
@@ -892,11 +1093,36 @@ def main():
     g.ingest = default_ingest
     _lib.call("emida_gb_free_host", hbuf)
 
-    cpu = None
+    # the reference's own staged GPU pipeline on the same job (the plain
+    # baseline of the fused/plain ratio), and the other legs of the path
+    legs = {}
+    if rank == 0 and world == 1 and not args.no_legs:
+        legs["plain_reference"] = reference_plain(ref, pics, begins, args.precision, 3)
+        if "value" in legs["plain_reference"]:
+            legs["over_plain_reference"] = {
+                "value": value / legs["plain_reference"]["value"],
+                "e2e": e2e_value / legs["plain_reference"]["e2e"]["value"],
+                "target": 5.0}
+        if args.precision == "float" and args.mode == "fused":
+            legs["fp64"] = fp64_leg(ref, pics, begins, d_pics, max(5, args.steps // 5), args.warmup)
+            legs["tensor"] = tensor_leg(ref, pics, begins, d_pics, max(5, args.steps // 5), args.warmup)
+            legs["serving"] = serving_measure("float", "detector", 100.0, 4.0, 128, False)
+
+    cpu = port = None
     if rank == 0 and world == 1:
-        v, pairs, dt = cpu_reference(ref, uniq, begins, 10.0, os.cpu_count() or 1)
-        cpu = {"value": v, "unit": "ROI pairs/s", "cores": os.cpu_count(), "kind": "port",
-               "sample": f"{pairs} ROI pairs (FP64, FFT policy, s=5) in {dt:.1f} s on all host cores"}
+        threads = os.cpu_count() or 1
+        cr = CpuReference(ref, uniq, begins, args.precision)
+        v, pairs, dt = cr.run(10.0, threads)
+        what = ("the reference's own CPU code (sums_serial, cross_corr_serial over 127x127 lags, "
+                f"subpixel_max_serial) in {args.precision}" if cr.kind == "reference" else
+                "the oracle's FP64 C restatement, FFT policy")
+        cpu = {"value": v, "unit": "ROI pairs/s", "cores": threads, "kind": cr.kind,
+               "sample": f"{pairs} ROI pairs in {dt:.1f} s on all host cores: {what}"}
+        if cr.kind == "reference":
+            v2, pairs2, dt2 = cpu_port(ref, uniq, begins, 5.0, threads)
+            port = {"value": v2, "unit": "ROI pairs/s", "cores": threads, "kind": "port",
+                    "sample": f"{pairs2} ROI pairs in {dt2:.1f} s: the oracle's FP64 C restatement "
+                              "of the FFT policy (no CPU FFT path exists in the reference)"}
 
     if rank == 0:
         line = {
@@ -904,11 +1130,8 @@ def main():
             "steps": args.steps, "warmup": args.warmup, "ms_per_step": ms_step,
             "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
             "dtype": "f32" if args.precision == "float" else "f64", "data": "synthetic",
-            "config": {"workload": "256 x 1024^2 uint16 patterns, 100 ROIs r=32 (64x64), FFT 128x128, "
-                                   "s=5, batch 32", "patterns": P, "rois": S, "radius": 32,
-                       "fitsize": 5, "form": g.mode, "precision": args.precision,
-                       "l2": "inputs larger than L2 (512 MB of patterns)",
-                       "parallelism": f"patterns sharded over {world} GPU(s)"},
+            "config": detector_config(P, S, world, args.precision),
+            "form": g.mode,
             "parity": {"max_abs_err_px": err, "rms_err_px": rms, "tol_px": tol,
                        "peak_match_rate": peak_match,
                        "vs": "FP64 oracle, first two patterns", "well_posed_fits": int(ok.sum()),
@@ -923,8 +1146,10 @@ def main():
                         "frac": flop / (ms_step / 1000.0) / 1e12 / fpu_peak,
                         "flop_per_pair": flop // pairs_per_step},
             "plain": plain,
+            **legs,
             "deformation_fit": deformation,
             "cpu_baseline": cpu,
+            "cpu_port_fft": port,
             "e2e": {"value": e2e_value, "unit": "ROI pairs/s",
                     "h2d_bytes_per_step": int(P * roi_rows(begins, 64) * 1024 * 2),
                     "d2h_bytes_per_step": pairs_per_step * (16 + 48 + 8),

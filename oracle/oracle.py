@@ -57,6 +57,34 @@ def ref_lib():
     return ctypes.CDLL(REF_LIB_PATH)
 
 
+def ref_brute_pattern(ref_lib, ref_prepared, pattern, begins, slice_, cross, s, precision):
+    """One pattern's ROIs through the brute path with the reference's own CPU
+    code (oracle/_ref): (offsets [n_rois][2], peaks [n_rois]).  ref_prepared
+    comes from ref_prepare_reference in the same precision."""
+    pattern = np.ascontiguousarray(pattern, dtype=np.uint16)
+    h, w = pattern.shape
+    begins = np.ascontiguousarray(begins, dtype=np.uint32).reshape(-1, 2)
+    offs = np.zeros((len(begins), 2))
+    peaks = np.zeros(len(begins), dtype=np.uint32)
+    ct = ctypes.c_float if precision == "float" else ctypes.c_double
+    fn = ref_lib.ref_brute_offsets_f32 if precision == "float" else ref_lib.ref_brute_offsets_f64
+    fn(_p(pattern, ctypes.c_uint16), _p(ref_prepared, ct), w, h, _p(begins, ctypes.c_uint32),
+       len(begins), slice_, cross, s, _p(offs), _p(peaks, ctypes.c_uint32))
+    return offs, peaks
+
+
+def ref_prepare_reference(ref_lib, ref, begins, slice_, precision):
+    """The reference ROIs prepared by the reference's CPU pieces (oracle/_ref)."""
+    ref = np.ascontiguousarray(ref, dtype=np.uint16)
+    h, w = ref.shape
+    begins = np.ascontiguousarray(begins, dtype=np.uint32).reshape(-1, 2)
+    dt, ct = (np.float32, ctypes.c_float) if precision == "float" else (np.float64, ctypes.c_double)
+    out = np.zeros((len(begins), slice_, slice_), dtype=dt)
+    fn = ref_lib.ref_prepare_reference_f32 if precision == "float" else ref_lib.ref_prepare_reference_f64
+    fn(_p(ref, ctypes.c_uint16), w, h, _p(begins, ctypes.c_uint32), len(begins), slice_, _p(out, ct))
+    return out
+
+
 def _p(a, ct=ctypes.c_double):
     return a.ctypes.data_as(ctypes.POINTER(ct))
 

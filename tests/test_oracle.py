@@ -209,6 +209,25 @@ def test_reference_lib_agrees_where_built():
         assert np.array_equal(m, eo.lstsq_matrix(s).ravel())
 
 
+@pytest.mark.parametrize("precision,tol", [("double", 1e-12), ("float", 1e-2)])
+def test_reference_cpu_brute_path_agrees_with_the_oracle(precision, tol):
+    """The reference's own CPU pieces (sums_serial, generate_hanning,
+    cross_corr_serial, subpixel_max_serial) through one pattern's ROIs, as the
+    CPU baseline runs them, against the oracle's brute path."""
+    ref_lib = eo.ref_lib()
+    if ref_lib is None:
+        pytest.skip("reference CPU code not built on this machine")
+    from emida_gb300 import synth
+    ref = synth.reference_pattern(256, seed=8)
+    pics, _ = synth.deformed_patterns(256, 8, 1, 3e-3)
+    _, begins = synth.roi_grid(256, 2, 32, margin=48)
+    prep = eo.ref_prepare_reference(ref_lib, ref, begins, 64, precision)
+    offs, peaks = eo.ref_brute_pattern(ref_lib, prep, pics[0], begins, 64, 127, 5, precision)
+    o_offs, o_coefs, o_peaks = eo.get_offsets(ref, pics, begins, 64, 64, eo.POLICY_BRUTE, 5, 127, 127)
+    assert np.array_equal(peaks, o_peaks)
+    assert np.abs(offs - o_offs).max() <= tol
+
+
 def test_homography_fit_matches_reference_script():
     # python/process_offsets.py run on seeded offsets (tests/golden/make_homography_golden.py)
     from oracle import oracle as eo
