@@ -63,6 +63,12 @@ def main():
     h5r = load_matrix(os.path.join(REF, "test/res/hann/5_res.txt"), np.float64)
     np.savez_compressed(os.path.join(HERE, "hann_5.npz"), A=h5a, res=h5r)
 
+    # the loader fixture of test/load_tiff_test.cpp:7-49, byte for byte
+    import gzip
+    with open(os.path.join(REF, "test/res/INITIAL_x0y0.tif"), "rb") as src, \
+            gzip.GzipFile(os.path.join(HERE, "INITIAL_x0y0.tif.gz"), "wb", 9, mtime=0) as dst:
+        dst.write(src.read())
+
     exp = expected_offsets()
     assert len(exp) == 49, len(exp)
     out["get_offset_single"] = {"x": 0.07583538046549165, "y": -0.0982055210473689,
