@@ -741,9 +741,14 @@ int emida_gb_set_reference(emida_gb_handle *h, const void *ref)
                        h->d_begins, h->src, h->slice, h->prep_size(), h->S, 1, h->comp));
     if (h->fft) {
         CK(run_fft_r2c(h->d_ref_prep, h->d_ref_spec, h->S, tables(h), h->dbl, h->comp));
-        if (h->d_ref_spec_cm)
+        if (h->d_ref_spec_cm) {
             CK(run_spec_to_colmajor(h->d_ref_spec, h->d_ref_spec_cm, h->S, h->w2, h->h2, h->dbl,
                                     h->comp));
+            // the one-CTA fused kernels correlate the packed DC and Nyquist
+            // slot directly, from the reference's row sums in column 0
+            if (h->w2 != 256)
+                CK(run_ref_row_sums(h->d_ref_prep, h->d_ref_spec_cm, h->S, h->w2, h->dbl, h->comp));
+        }
     }
     // the path's kernel is loaded now rather than at the first batch
     if (h->mode == EMIDA_GB_MODE_FUSED) CK(preload_fused(h->w2, h->dbl, h->in_f64));

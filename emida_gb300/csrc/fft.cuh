@@ -208,10 +208,12 @@ template <int DIR, typename C> struct rdft<3, DIR, C> {
 // A'[t][k1] is G*k1 + ((t + k1) mod G): the G lanes' writes (fixed k1) and reads
 // (fixed t) fall in G different rows or slots.
 // tw: this direction's inter-pass twiddles laid out [k1][lane],
-// tw[G*k1 + t] = W_N^{t*k1}.
+// tw[G*k1 + t] = W_N^{t*k1}.  mask: the lanes of the warp's groups that run
+// this transform together (whole groups; every lane named must call it).
 template <int N, int DIR, bool HALF_INPUT, typename T, int G, typename Line>
 __device__ __forceinline__ void group_fft(cplx<T> *v, int t, const Line &line,
-                                          const cplx<T> *__restrict__ tw)
+                                          const cplx<T> *__restrict__ tw,
+                                          unsigned mask = 0xffffffffu)
 {
     using C = cplx<T>;
     constexpr int E = N / G;
@@ -222,10 +224,10 @@ __device__ __forceinline__ void group_fft(cplx<T> *v, int t, const Line &line,
         rdft<E, DIR, C>::run(v);
 #pragma unroll
     for (int k1 = 1; k1 < E; ++k1) v[k1] = cmul(v[k1], tw[G * k1 + t]);
-    __syncwarp();
+    __syncwarp(mask);
 #pragma unroll
     for (int k1 = 0; k1 < E; ++k1) *line(G * k1 + ((t + k1) & (G - 1))) = v[k1];
-    __syncwarp();
+    __syncwarp(mask);
 #pragma unroll
     for (int i = 0; i < E / G; ++i) {
         C a[G];
@@ -235,7 +237,7 @@ __device__ __forceinline__ void group_fft(cplx<T> *v, int t, const Line &line,
 #pragma unroll
         for (int k2 = 0; k2 < G; ++k2) v[i + (E / G) * k2] = a[k2];
     }
-    __syncwarp();
+    __syncwarp(mask);
 }
 
 }  // namespace emida_gb

@@ -142,44 +142,73 @@ __device__ __forceinline__ void better(T &bv, uint32_t &bi, T v, uint32_t i)
 
 }  // namespace
 
-// The conj product of column c of the spectrum (held in v, E values per lane
-// of the 8- or 4-lane group) with its reference column, in place.  `first`:
-// warp 0 in its first column round, whose column 0 packs the DC and Nyquist
-// columns.
+// The conj product of column c (1 <= c < N/2) of the spectrum (held in v, E
+// values per lane of the group) with its reference column, in place.
 template <int N, int G, typename T>
-__device__ __forceinline__ void conj_product(cplx<T> *v, cplx<T> *S, const cplx<T> *R, int c, int t,
-                                             bool first)
+__device__ __forceinline__ void conj_product(cplx<T> *v, const cplx<T> *R, int c, int t)
 {
-    using C = cplx<T>;
-    constexpr int E = N / G, SL = N / 2;
-    const C *Rc = R + (size_t)c * N;
-    if (first) {
-        // This warp holds column 0, whose slot packs the DC and Nyquist
-        // columns: unpack X[ky] with its mirror X[N-ky], multiply each
-        // half by its own reference column, repack.  The exchange goes
-        // through the warp's columns with full-warp syncs.
+    constexpr int E = N / G;
+    const cplx<T> *Rc = R + (size_t)c * N;
 #pragma unroll
-        for (int j = 0; j < E; ++j) *sp<N>(S, t + G * j, c) = v[j];
-        __syncwarp();
+    for (int j = 0; j < E; ++j) v[j] = cmulc(v[j], __ldg(Rc + t + G * j));
+}
+
+// Slot 0 of every spectrum row packs the real DC and Nyquist columns (kx = 0
+// and N/2).  Their products with the reference and inverse column transforms
+// are two real 1-D circular correlations along ky, computed directly: with d,
+// q the DC and Nyquist outputs of the row pass (zero for y >= side) and r0, r1
+// the reference ROI's row sums and alternating row sums (staged from column 0
+// of the resident reference),
+//   IFFT(FFT(d) conj(FFT(r0)))[tau] = N sum_{b < side} d[(b + tau) mod N] r0[b],
+// the unnormalised inverse of the FFT path; likewise for q and r1.
+// Planar layout: dq[c * DQ + y] = component c (d, q) at y mod N for y < DQ, so
+// no index wraps; rs[c * N/2 + b] = r_c[b].  The 2N outputs form N/2 blocks of
+// 4 consecutive tau of one component; Q = THREADS / (N/2) consecutive lanes
+// share a block, each summing a contiguous part of the b range with a sliding
+// window of 4 values, and combine by shuffles.  Lane q's part starts at
+// b = q (mod Q): the lanes' window heads 4 * block + b then fall in distinct
+// banks.  Lane q of the block writes outputs q, q + Q, ... to slot 0.
+template <int N> constexpr int packed_dq() { return 3 * N / 2 + 4; }
+template <int N, int THREADS, typename T>
+__device__ __forceinline__ void packed_column(cplx<T> *S, const T *dq, const T *rs, int side, int tid)
+{
+    constexpr int Q = THREADS / (N / 2), DQ = packed_dq<N>();
+    static_assert(Q == 2 || Q == 4, "lanes per block of 4 lags");
+    const int q = tid % Q, blk = tid / Q;
+    const int comp = blk / (N / 4), tau0 = 4 * (blk % (N / 4));
+    const T *dv = dq + comp * DQ;
+    const T *rv = rs + comp * (N / 2);
+    auto start = [&](int k) {
+        const int b = (k * side / Q) / Q * Q + k;
+        return b < side ? b : side;
+    };
+    const int b0 = start(q), b1 = q + 1 < Q ? start(q + 1) : side;
+    T w0 = dv[tau0 + b0], w1 = dv[tau0 + b0 + 1], w2 = dv[tau0 + b0 + 2];
+    T a0 = (T)0, a1 = (T)0, a2 = (T)0, a3 = (T)0;
+#pragma unroll 4
+    for (int b = b0; b < b1; ++b) {
+        const T w3 = dv[tau0 + b + 3];
+        const T r = rv[b];
+        a0 += w0 * r;
+        a1 += w1 * r;
+        a2 += w2 * r;
+        a3 += w3 * r;
+        w0 = w1;
+        w1 = w2;
+        w2 = w3;
+    }
 #pragma unroll
-        for (int j = 0; j < E; ++j) {
-            const int ky = t + G * j;
-            if (c == 0) {
-                C x = v[j];
-                C xm = *sp<N>(S, ky == 0 ? 0 : N - ky, 0);
-                C p0 = cmake<C>((x.x + xm.x) * (T)0.5, (x.y - xm.y) * (T)0.5);
-                C p64 = cmake<C>((x.y + xm.y) * (T)0.5, (xm.x - x.x) * (T)0.5);
-                C q0 = cmulc(p0, __ldg(R + ky));
-                C q64 = cmulc(p64, __ldg(R + (size_t)SL * N + ky));
-                v[j] = cmake<C>(q0.x - q64.y, q0.y + q64.x);
-            } else {
-                v[j] = cmulc(v[j], __ldg(Rc + ky));
-            }
-        }
-        __syncwarp();
-    } else {
+    for (int o = 1; o < Q; o <<= 1) {
+        a0 += __shfl_xor_sync(0xffffffffu, a0, o);
+        a1 += __shfl_xor_sync(0xffffffffu, a1, o);
+        a2 += __shfl_xor_sync(0xffffffffu, a2, o);
+        a3 += __shfl_xor_sync(0xffffffffu, a3, o);
+    }
 #pragma unroll
-        for (int j = 0; j < E; ++j) v[j] = cmulc(v[j], __ldg(Rc + t + G * j));
+    for (int k = 0; k < 4; k += Q) {
+        const int j = k + q;  // this lane's output of the block
+        const T v = j == 0 ? a0 : j == 1 ? a1 : j == 2 ? a2 : a3;
+        reinterpret_cast<T *>(sp<N>(S, tau0 + j, 0))[comp] = v * (T)N;
     }
 }
 
@@ -233,7 +262,9 @@ template <int N, int G, typename T> struct fused_layout {
     static constexpr size_t tw_fwd = spectrum + (size_t)N * (N / 2) * sizeof(C);
     static constexpr size_t tw_inv = tw_fwd + (size_t)N * sizeof(C);      // G*E = N entries
     static constexpr size_t hann = tw_inv + (size_t)N * sizeof(C);
-    static constexpr size_t red_val = hann + (size_t)N * sizeof(T);       // hx, hy
+    static constexpr size_t dq = hann + (size_t)N * sizeof(T);            // hx, hy
+    static constexpr size_t rsum = dq + (size_t)packed_dq<N>() * sizeof(C);  // DC, Nyquist
+    static constexpr size_t red_val = rsum + (size_t)(N / 2) * sizeof(C); // reference row sums
     static constexpr size_t red_idx = red_val + 32 * sizeof(T);
     static constexpr size_t red_sum = up(red_idx + 32 * sizeof(uint32_t), 8);
     static constexpr size_t barrier = red_sum + 32 * sizeof(double);
@@ -273,6 +304,9 @@ __global__ void __launch_bounds__(N * G / 4, fused_min_blocks(N, sizeof(T)))
     C *twi = reinterpret_cast<C *>(smem + L::tw_inv);   // [E][G] inverse
     T *hx = reinterpret_cast<T *>(smem + L::hann);      // hx[H] then hy[H]
     T *hy = hx + a.side;
+    constexpr int DQ = packed_dq<N>();
+    T *dq = reinterpret_cast<T *>(smem + L::dq);         // the row pass's DC and Nyquist outputs
+    T *rs = reinterpret_cast<T *>(smem + L::rsum);       // the reference's row sums (this ROI)
     T *red_v = reinterpret_cast<T *>(smem + L::red_val);
     uint32_t *red_i = reinterpret_cast<uint32_t *>(smem + L::red_idx);
     double *red_s = reinterpret_cast<double *>(smem + L::red_sum);
@@ -298,6 +332,13 @@ __global__ void __launch_bounds__(N * G / 4, fused_min_blocks(N, sizeof(T)))
     }
     const T *ghann = reinterpret_cast<const T *>(a.hann);
     for (int i = tid; i < 2 * a.side; i += THREADS) hx[i] = ghann[i];  // hx then hy
+    // rows N/2..N-1 of the DC and Nyquist columns are the zero padding, as is
+    // the tail past their copy at N..3N/2-1; the row pass writes rows
+    // 0..N/2-1 and that copy for every pair
+    for (int i = tid; i < 2 * DQ; i += THREADS) {
+        const int y = i % DQ;
+        if ((y >= N / 2 && y < N) || y >= 3 * N / 2) dq[i] = (T)0;
+    }
     const bool tma = U16 && a.stage == STAGE_TMA;
     const bool cpa = U16 && a.stage == STAGE_ASYNC;
     if (tid == 0) {
@@ -409,6 +450,12 @@ __global__ void __launch_bounds__(N * G / 4, fused_min_blocks(N, sizeof(T)))
         }
 
         // ---- forward rows: pairs of real rows as one complex FFT ----------
+        const C *R = reinterpret_cast<const C *>(a.ref_spec) + (size_t)roi * (SL + 1) * N;
+        for (int i = tid; i < side; i += THREADS) {  // column 0: the row sums
+            const C r = __ldg(R + i);
+            rs[i] = r.x;
+            rs[N / 2 + i] = r.y;
+        }
         {
             const int ra = 2 * g, rb = ra + 1;
             const bool live = ra < side;  // side is even: rb < side too
@@ -444,8 +491,10 @@ __global__ void __launch_bounds__(N * G / 4, fused_min_blocks(N, sizeof(T)))
                 const int k = t + G * j;
                 if (k == 0) {
                     C zh = v[E / 2];
-                    *sp<N>(S, ra, 0) = cmake<C>(z.x, zh.x);
-                    *sp<N>(S, rb, 0) = cmake<C>(z.y, zh.y);
+                    dq[ra] = dq[N + ra] = z.x;
+                    dq[DQ + ra] = dq[DQ + N + ra] = zh.x;
+                    dq[rb] = dq[N + rb] = z.y;
+                    dq[DQ + rb] = dq[DQ + N + rb] = zh.y;
                 } else {
                     *sp<N>(S, ra, k) = cmake<C>((z.x + zm.x) * (T)0.5, (z.y - zm.y) * (T)0.5);
                     *sp<N>(S, rb, k) = cmake<C>((z.y + zm.y) * (T)0.5, (zm.x - z.x) * (T)0.5);
@@ -458,42 +507,48 @@ __global__ void __launch_bounds__(N * G / 4, fused_min_blocks(N, sizeof(T)))
         if (cpa && pair + gridDim.x < a.n_pairs) issue_chunks(pair + gridDim.x);
 
         // ---- columns: forward FFT, conj product, inverse FFT --------------
-        const C *R = reinterpret_cast<const C *>(a.ref_spec) + (size_t)roi * (SL + 1) * N;
+        // Columns 1..N/2-1 by the groups (the last round leaves the last group
+        // without a column); slot 0, the packed DC and Nyquist columns, is
+        // packed_column's direct correlation, by every thread.
 #pragma unroll 1
-        for (int rnd = 0; rnd < SL / GROUPS; ++rnd) {
-            const int c = g + rnd * GROUPS;
-            C v[E];
+        for (int rnd = 0; rnd < (SL - 1 + GROUPS - 1) / GROUPS; ++rnd) {
+            const int c = 1 + g + rnd * GROUPS;
+            const unsigned mask = __ballot_sync(0xffffffffu, c < SL);
+            if (c < SL) {
+                C v[E];
 #pragma unroll
-            for (int m = 0; m < E / 2; ++m) v[m] = *sp<N>(S, t + G * m, c);
-            col_line<N, C> line{S, c};
-            if constexpr (E % 3 != 0) {
-                group_fft<N, -1, true, T, G>(v, t, line, twf);
-                conj_product<N, G, T>(v, S, R, c, t, warp == 0 && rnd == 0);
-                group_fft<N, +1, false, T, G>(v, t, line, twi);
-            } else {
-                // Prime-factor lengths gain nothing from the zero half of the
-                // input, so both transforms run one copy of the code: the
-                // inverse as conj(forward(conj(.))).  The negations are exact,
-                // so only the pairing of multiply-adds can differ from a direct
-                // inverse.  Half the column code keeps the loop in the
-                // instruction cache.
+                for (int m = 0; m < E / 2; ++m) v[m] = *sp<N>(S, t + G * m, c);
+                col_line<N, C> line{S, c};
+                if constexpr (E % 3 != 0) {
+                    group_fft<N, -1, true, T, G>(v, t, line, twf, mask);
+                    conj_product<N, G, T>(v, R, c, t);
+                    group_fft<N, +1, false, T, G>(v, t, line, twi, mask);
+                } else {
+                    // Prime-factor lengths gain nothing from the zero half of
+                    // the input, so both transforms run one copy of the code:
+                    // the inverse as conj(forward(conj(.))).  The negations are
+                    // exact, so only the pairing of multiply-adds can differ
+                    // from a direct inverse.  Half the column code keeps the
+                    // loop in the instruction cache.
 #pragma unroll
-                for (int m = E / 2; m < E; ++m) v[m] = cmake<C>((T)0, (T)0);
+                    for (int m = E / 2; m < E; ++m) v[m] = cmake<C>((T)0, (T)0);
 #pragma unroll 1
-                for (int pass = 0; pass < 2; ++pass) {
-                    group_fft<N, -1, false, T, G>(v, t, line, twf);
-                    if (pass == 0) {
-                        conj_product<N, G, T>(v, S, R, c, t, warp == 0 && rnd == 0);
+                    for (int pass = 0; pass < 2; ++pass) {
+                        group_fft<N, -1, false, T, G>(v, t, line, twf, mask);
+                        if (pass == 0) {
+                            conj_product<N, G, T>(v, R, c, t);
 #pragma unroll
-                        for (int j = 0; j < E; ++j) v[j].y = -v[j].y;
+                            for (int j = 0; j < E; ++j) v[j].y = -v[j].y;
+                        }
                     }
+#pragma unroll
+                    for (int j = 0; j < E; ++j) v[j].y = -v[j].y;
                 }
 #pragma unroll
-                for (int j = 0; j < E; ++j) v[j].y = -v[j].y;
+                for (int j = 0; j < E; ++j) *sp<N>(S, t + G * j, c) = v[j];
             }
-#pragma unroll
-            for (int j = 0; j < E; ++j) *sp<N>(S, t + G * j, c) = v[j];
         }
+        packed_column<N, THREADS, T>(S, dq, rs, side, tid);
         __syncthreads();
 
         // ---- inverse rows: pairs of half spectra -> two real rows ---------

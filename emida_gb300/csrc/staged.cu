@@ -369,6 +369,30 @@ __global__ void __launch_bounds__(BLOCK) k_to_colmajor(const cplx<T> *__restrict
     out[map * per + (uint64_t)kx * h2 + ky] = in[i];
 }
 
+// Column 0 of a column-major reference spectrum, replaced by the spatial
+// sequences the fused kernel correlates directly for its packed DC and Nyquist
+// slot: entry y of ROI m = (sum_x p[y][x], sum_x (-1)^x p[y][x]) of the
+// prepared n x n reference ROI (zero-padded rows give zeros), summed in FP64.
+template <typename T>
+__global__ void __launch_bounds__(BLOCK) k_ref_row_sums(const T *__restrict__ prep, cplx<T> *spec_cm,
+                                                        uint32_t n, uint64_t per_map, uint64_t total)
+{
+    const uint64_t i = (uint64_t)blockIdx.x * BLOCK + threadIdx.x;
+    if (i >= total) return;
+    const uint64_t map = i / n, y = i % n;
+    const T *row = prep + (map * n + y) * n;
+    double s0 = 0, s1 = 0;
+    for (uint32_t x = 0; x < n; ++x) {
+        const double v = (double)row[x];
+        s0 += v;
+        s1 += (x & 1) ? -v : v;
+    }
+    cplx<T> out;
+    out.x = (T)s0;
+    out.y = (T)s1;
+    spec_cm[map * per_map + y] = out;
+}
+
 // One thread per ROI row: the 16-byte chunks of the source row that hold the
 // row's pixels (CH at most), all loads issued before the stores, so that a
 // row costs one round trip (over the host link a read takes microseconds).
@@ -646,6 +670,20 @@ cudaError_t run_fit(const void *neigh, const void *maxes, uint32_t n, int s, siz
             reinterpret_cast<const float *>(neigh), reinterpret_cast<const data_index<float> *>(maxes),
             n, s, cross, policy, lstsq, offsets, coefs, out_base, n_rois,
             reinterpret_cast<data_index<float> *>(maxes_out));
+    return cudaGetLastError();
+}
+
+cudaError_t run_ref_row_sums(const void *prep, void *spec_cm, uint32_t maps, uint32_t n, bool dbl,
+                             cudaStream_t st)
+{
+    const uint64_t total = (uint64_t)maps * n, per = (uint64_t)(n / 2 + 1) * n;
+    if (total == 0) return cudaSuccess;
+    if (dbl)
+        k_ref_row_sums<double><<<grid_for(total), BLOCK, 0, st>>>(
+            reinterpret_cast<const double *>(prep), reinterpret_cast<double2 *>(spec_cm), n, per, total);
+    else
+        k_ref_row_sums<float><<<grid_for(total), BLOCK, 0, st>>>(
+            reinterpret_cast<const float *>(prep), reinterpret_cast<float2 *>(spec_cm), n, per, total);
     return cudaGetLastError();
 }
 

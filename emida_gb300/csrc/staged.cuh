@@ -93,6 +93,11 @@ cudaError_t run_copy_bands(const void *src, void *dst, const uint2 *runs, uint32
 
 // Reference spectra from cuFFT layout [S][h2][w2/2+1] to the fused kernel's
 // column-major layout [S][w2/2+1][h2].
+// Column 0 of each column-major n x (n/2 + 1) reference spectrum, replaced by
+// the prepared reference ROI's row sums and alternating row sums (the inputs
+// of the fused kernel's direct DC/Nyquist correlation); prep is [maps][n][n].
+cudaError_t run_ref_row_sums(const void *prep, void *spec_cm, uint32_t maps, uint32_t n, bool dbl,
+                             cudaStream_t st);
 cudaError_t run_spec_to_colmajor(const void *spec, void *out, uint32_t maps, uint32_t w2,
                                  uint32_t h2, bool dbl, cudaStream_t st);
 
