@@ -55,9 +55,9 @@ from emida_gb300.shard import dist_env, max_over_ranks, whole_job_rate  # noqa: 
 METRIC = "ROI pairs/s at <=0.01 px vs FP64 oracle"
 UNIQUE = 32
 # DRAM traffic of the fused FP32 kernel on this workload, from one ncu capture
-# (dram__bytes_read.sum + dram__bytes_write.sum) of a 12,800-pair launch: 178.4 MB,
+# (dram__bytes_read.sum + dram__bytes_write.sum) of a 12,800-pair launch: 177.9 MB,
 # of which 6.66 MB are the once-per-launch reference spectra; scaled by pairs.
-TRAFFIC_PER_PAIR = (178.4e6 - 6.66e6) / 12800
+TRAFFIC_PER_PAIR = (177.9e6 - 6.66e6) / 12800
 TRAFFIC_PER_LAUNCH = 6.66e6
 
 

@@ -390,11 +390,13 @@ __global__ void __launch_bounds__(N * G / 4, fused_min_blocks(N, sizeof(T)))
     uint32_t *red_u = reinterpret_cast<uint32_t *>(red_s);  // next tile's partial sums
     bool summed = false;  // this pair's tile was summed ahead (uniform over the CTA)
     uint32_t iter = 0;
+    // each pair's ROI corner is loaded during the pair before it
+    uint2 beg_next = blockIdx.x < a.n_pairs ? a.begins[item(blockIdx.x).y] : make_uint2(0, 0);
     for (uint32_t pair = blockIdx.x; pair < a.n_pairs; pair += gridDim.x, ++iter) {
         const uint4 it = item(pair);
         const uint32_t pic = it.x, roi = it.y, out = it.z;
         const int s = (int)it.w, s2 = s * s;
-        const uint2 beg = a.begins[roi];
+        const uint2 beg = beg_next;
 
         // ---- gather the ROI and sum it (sum.cu:109-158) -------------------
         T mean;
@@ -451,11 +453,10 @@ __global__ void __launch_bounds__(N * G / 4, fused_min_blocks(N, sizeof(T)))
 
         // ---- forward rows: pairs of real rows as one complex FFT ----------
         const C *R = reinterpret_cast<const C *>(a.ref_spec) + (size_t)roi * (SL + 1) * N;
-        for (int i = tid; i < side; i += THREADS) {  // column 0: the row sums
-            const C r = __ldg(R + i);
-            rs[i] = r.x;
-            rs[N / 2 + i] = r.y;
-        }
+        static_assert(N / 2 <= THREADS, "one reference row sum per thread");
+        // column 0 of the reference: its row sums, stored after the row FFT
+        // (the load's latency hides behind it)
+        const C rsum = tid < side ? __ldg(R + tid) : cmake<C>((T)0, (T)0);
         {
             const int ra = 2 * g, rb = ra + 1;
             const bool live = ra < side;  // side is even: rb < side too
@@ -501,7 +502,12 @@ __global__ void __launch_bounds__(N * G / 4, fused_min_blocks(N, sizeof(T)))
                 }
             }
         }
+        if (tid < side) {
+            rs[tid] = rsum.x;
+            rs[N / 2 + tid] = rsum.y;
+        }
         __syncthreads();
+        if (pair + gridDim.x < a.n_pairs) beg_next = a.begins[item(pair + gridDim.x).y];
         // the tile is free: fetch the next pair's ROI behind the remaining passes
         if (tma && tid == 0 && pair + gridDim.x < a.n_pairs) issue_tile(pair + gridDim.x);
         if (cpa && pair + gridDim.x < a.n_pairs) issue_chunks(pair + gridDim.x);
@@ -651,7 +657,7 @@ __global__ void __launch_bounds__(N * G / 4, fused_min_blocks(N, sizeof(T)))
             // the next tile was requested after this pair's row pass: wait for it
             // and sum it over the other warps' threads
             if (!mbar_wait(bar, (iter + 1) & 1)) atomicOr(a.err, DEV_ERR_TMA_TIMEOUT);
-            const int nxo = (int)(a.begins[item(pair + gridDim.x).y].x & 7u);
+            const int nxo = (int)(beg_next.x & 7u);
             const int u = tid - 32;
             uint32_t acc = 0;
             for (int r = u >> 2; r < side; r += (THREADS - 32) >> 2)

@@ -163,13 +163,21 @@ __global__ void __launch_bounds__(BLOCK)
     C *b0 = buf + (size_t)l * 2 * n, *b1 = b0 + n;
     const uint32_t map = live ? line / lines_per_map : 0, li = live ? line % lines_per_map : 0;
 
-    if (live) {
+    if (mode == LM_C2C_COLS) {
+        // Columns: the block's lpb consecutive columns are loaded row by row by
+        // all its threads, so consecutive threads read consecutive columns.
+        for (int i = threadIdx.x; i < lpb * n; i += BLOCK) {
+            const int l2 = i % lpb, e = i / lpb;
+            const uint32_t line2 = blockIdx.x * lpb + l2;
+            if (line2 >= n_lines) continue;
+            const C *src = reinterpret_cast<const C *>(in) + (size_t)(line2 / lines_per_map) * map_len_in +
+                           line2 % lines_per_map;
+            buf[(size_t)l2 * 2 * n + e] = src[(size_t)e * half];
+        }
+    } else if (live) {
         if (mode == LM_R2C_ROWS) {
             const T *src = reinterpret_cast<const T *>(in) + (size_t)map * map_len_in + (size_t)li * n;
             for (int e = lt; e < n; e += tpl) b0[e] = cmake<C>(src[e], (T)0);
-        } else if (mode == LM_C2C_COLS) {
-            const C *src = reinterpret_cast<const C *>(in) + (size_t)map * map_len_in + li;
-            for (int e = lt; e < n; e += tpl) b0[e] = src[(size_t)e * half];
         } else {
             const C *src = reinterpret_cast<const C *>(in) + (size_t)map * map_len_in + (size_t)li * half;
             for (int e = lt; e < n; e += tpl)
@@ -220,13 +228,21 @@ __global__ void __launch_bounds__(BLOCK)
         nxt = tmp;
         m *= R;
     }
-    if (live) {
+    if (mode == LM_C2C_COLS) {
+        // stored row by row across the block's columns, as they were loaded
+        const size_t res = (size_t)(cur - b0);  // n or 0: the pass count's parity
+        for (int i = threadIdx.x; i < lpb * n; i += BLOCK) {
+            const int l2 = i % lpb, e = i / lpb;
+            const uint32_t line2 = blockIdx.x * lpb + l2;
+            if (line2 >= n_lines) continue;
+            C *dst = reinterpret_cast<C *>(out) + (size_t)(line2 / lines_per_map) * map_len_out +
+                     line2 % lines_per_map;
+            dst[(size_t)e * half] = buf[(size_t)l2 * 2 * n + res + e];
+        }
+    } else if (live) {
         if (mode == LM_R2C_ROWS) {
             C *dst = reinterpret_cast<C *>(out) + (size_t)map * map_len_out + (size_t)li * half;
             for (int e = lt; e < (int)half; e += tpl) dst[e] = cur[e];
-        } else if (mode == LM_C2C_COLS) {
-            C *dst = reinterpret_cast<C *>(out) + (size_t)map * map_len_out + li;
-            for (int e = lt; e < n; e += tpl) dst[(size_t)e * half] = cur[e];
         } else {
             T *dst = reinterpret_cast<T *>(out) + (size_t)map * map_len_out + (size_t)li * n;
             for (int e = lt; e < n; e += tpl) dst[e] = cur[e].x;
@@ -242,6 +258,14 @@ cudaError_t launch_lines(const void *in, void *out, int mode, int dir, int n, ui
     using C = cplx<T>;
     line_plan plan = make_plan(n);
     int lpb = n >= 512 ? 1 : 512 / n;
+    if (mode == LM_C2C_COLS) {
+        // more columns per block make each row of the block's loads and stores
+        // a longer contiguous run: up to 32, in at most 96 KB of shared memory
+        const int fit = (int)(((96 * 1024) / sizeof(C) - (size_t)n) / (2 * (size_t)n));
+        int want = 32;
+        while (want > 1 && want > fit) want >>= 1;
+        if (want > lpb) lpb = want;
+    }
     if (lpb > BLOCK) lpb = BLOCK;
     while (BLOCK % lpb) --lpb;
     const size_t smem = sizeof(C) * ((size_t)n + 2 * (size_t)n * lpb);
@@ -372,25 +396,34 @@ __global__ void __launch_bounds__(BLOCK) k_to_colmajor(const cplx<T> *__restrict
 // Column 0 of a column-major reference spectrum, replaced by the spatial
 // sequences the fused kernel correlates directly for its packed DC and Nyquist
 // slot: entry y of ROI m = (sum_x p[y][x], sum_x (-1)^x p[y][x]) of the
-// prepared n x n reference ROI (zero-padded rows give zeros), summed in FP64.
+// prepared n x n reference ROI (zero-padded rows give zeros), summed in FP64
+// by one warp per row.
 template <typename T>
 __global__ void __launch_bounds__(BLOCK) k_ref_row_sums(const T *__restrict__ prep, cplx<T> *spec_cm,
-                                                        uint32_t n, uint64_t per_map, uint64_t total)
+                                                        uint32_t n, uint64_t per_map, uint64_t rows)
 {
-    const uint64_t i = (uint64_t)blockIdx.x * BLOCK + threadIdx.x;
-    if (i >= total) return;
-    const uint64_t map = i / n, y = i % n;
-    const T *row = prep + (map * n + y) * n;
+    const uint64_t r = ((uint64_t)blockIdx.x * BLOCK + threadIdx.x) >> 5;
+    const int lane = threadIdx.x & 31;
+    if (r >= rows) return;  // whole warps leave together
+    const uint64_t map = r / n, y = r % n;
+    const T *row = prep + r * n;
     double s0 = 0, s1 = 0;
-    for (uint32_t x = 0; x < n; ++x) {
+    for (uint32_t x = lane; x < n; x += 32) {
         const double v = (double)row[x];
         s0 += v;
         s1 += (x & 1) ? -v : v;
     }
-    cplx<T> out;
-    out.x = (T)s0;
-    out.y = (T)s1;
-    spec_cm[map * per_map + y] = out;
+#pragma unroll
+    for (int o = 16; o; o >>= 1) {
+        s0 += __shfl_xor_sync(0xffffffffu, s0, o);
+        s1 += __shfl_xor_sync(0xffffffffu, s1, o);
+    }
+    if (lane == 0) {
+        cplx<T> out;
+        out.x = (T)s0;
+        out.y = (T)s1;
+        spec_cm[map * per_map + y] = out;
+    }
 }
 
 // One thread per ROI row: the 16-byte chunks of the source row that hold the
@@ -676,14 +709,14 @@ cudaError_t run_fit(const void *neigh, const void *maxes, uint32_t n, int s, siz
 cudaError_t run_ref_row_sums(const void *prep, void *spec_cm, uint32_t maps, uint32_t n, bool dbl,
                              cudaStream_t st)
 {
-    const uint64_t total = (uint64_t)maps * n, per = (uint64_t)(n / 2 + 1) * n;
-    if (total == 0) return cudaSuccess;
+    const uint64_t rows = (uint64_t)maps * n, per = (uint64_t)(n / 2 + 1) * n;
+    if (rows == 0) return cudaSuccess;
     if (dbl)
-        k_ref_row_sums<double><<<grid_for(total), BLOCK, 0, st>>>(
-            reinterpret_cast<const double *>(prep), reinterpret_cast<double2 *>(spec_cm), n, per, total);
+        k_ref_row_sums<double><<<grid_for(rows * 32), BLOCK, 0, st>>>(
+            reinterpret_cast<const double *>(prep), reinterpret_cast<double2 *>(spec_cm), n, per, rows);
     else
-        k_ref_row_sums<float><<<grid_for(total), BLOCK, 0, st>>>(
-            reinterpret_cast<const float *>(prep), reinterpret_cast<float2 *>(spec_cm), n, per, total);
+        k_ref_row_sums<float><<<grid_for(rows * 32), BLOCK, 0, st>>>(
+            reinterpret_cast<const float *>(prep), reinterpret_cast<float2 *>(spec_cm), n, per, rows);
     return cudaGetLastError();
 }
 
