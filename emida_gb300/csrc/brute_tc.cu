@@ -17,6 +17,11 @@
 //   * B: the reference ROI is stored once per ROI with its rows reversed and
 //     64 zero rows either side; the operand of pattern row a is the same
 //     buffer at a start offset of -a rows.
+//   * Pattern row a meets the reference only at lags dy in [a, a + 63]; the
+//     other 64 columns of its B operand are zero rows.  Row 0 runs the full
+//     N = 128 (its first product initialises every accumulator column); rows
+//     a >= 1 run N = 80 MMAs on the columns [a & ~15, (a & ~15) + 80), which
+//     hold that window, at 0.63 of the full tile's products.
 //
 // Products are BF16 with FP32 accumulation.  Every value is split as
 // v = hi + lo (hi = bf16(v), lo = bf16(v - hi)) and D accumulates
@@ -190,11 +195,14 @@ __device__ void producer(const brute_tc_args &a, unsigned char *smem, const barr
     }
 }
 
-// Lane 0 of warp 8: 64 pattern rows x 4 K-steps x 3 split products per pair.
+// Lane 0 of warp 8: 64 pattern rows x 4 K-steps x 3 split products per pair,
+// on the accumulator columns that pattern row can reach.
+constexpr int TN_WIN = 80;  // lag columns of a pattern row's window: 64 + 15, rounded to 16
 __device__ void mma_issuer(const brute_tc_args &a, unsigned char *smem, const barriers &bar,
                            uint64_t q0, uint64_t q1, uint32_t tmem)
 {
     constexpr uint32_t idesc = idesc_bf16_f32(TM, TN);
+    constexpr uint32_t idesc_win = idesc_bf16_f32(TM, TN_WIN);
     // Every operand address is a base plus a constant, and a descriptor's low
     // 14 bits are the address / 16, so each descriptor below is a base
     // descriptor plus a small integer: the single issuing thread spends a few
@@ -216,16 +224,19 @@ __device__ void mma_issuer(const brute_tc_args &a, unsigned char *smem, const ba
             const uint64_t dAs = dA0 + (uint64_t)((s * STAGE) >> 4);
 #pragma unroll
             for (int rr = 0; rr < RPS; ++rr) {
-                const uint64_t row = (uint64_t)(st * RPS + rr);  // B starts row rows earlier
+                const int row = st * RPS + rr;  // B starts row rows earlier
+                // row 0: all 128 lag columns; later rows: the 80 from row & ~15
+                const uint32_t dy0 = row == 0 ? 0u : (uint32_t)(row & ~15);
+                const uint32_t id = row == 0 ? idesc : idesc_win;
 #pragma unroll
                 for (int ks = 0; ks < SIDE / 16; ++ks) {
                     const uint64_t dah = dAs + ((rr * 2 * A_ROW + ks * 256) >> 4);
                     const uint64_t dal = dah + (A_ROW >> 4);
-                    const uint64_t dbh = dBh0 - row + ((ks * 2 * B_KBLK) >> 4);
-                    const uint64_t dbl = dBl0 - row + ((ks * 2 * B_KBLK) >> 4);
-                    mma_bf16(d, dah, dbh, idesc, (st | rr | ks) != 0);
-                    mma_bf16(d, dah, dbl, idesc, 1);
-                    mma_bf16(d, dal, dbh, idesc, 1);
+                    const uint64_t dbh = dBh0 - (uint64_t)row + dy0 + ((ks * 2 * B_KBLK) >> 4);
+                    const uint64_t dbl = dBl0 - (uint64_t)row + dy0 + ((ks * 2 * B_KBLK) >> 4);
+                    mma_bf16(d + dy0, dah, dbh, id, (row | ks) != 0);
+                    mma_bf16(d + dy0, dah, dbl, id, 1);
+                    mma_bf16(d + dy0, dal, dbh, id, 1);
                 }
             }
             mma_commit(&bar.empty[s]);
