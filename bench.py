@@ -99,8 +99,8 @@ def parse():
     ap.add_argument("--layout", default="mixed", choices=["mixed", "detector"],
                     help="serving: mixed sizes and layouts, or the detector grid at 1024^2")
     ap.add_argument("--step-patterns", type=int, default=128, help="serving: patterns per step")
-    ap.add_argument("--copy-rows", action="store_true",
-                    help="serving: copy every row into the device arena (no in-place reads)")
+    ap.add_argument("--in-place-rows", action="store_true",
+                    help="serving: the kernels read every pinned row in place (no copy into the arena)")
     return ap.parse_args()
 
 
@@ -455,10 +455,10 @@ def run_serving(args):
     import __graft_entry__
     __graft_entry__.build_library()
     print(json.dumps(serving_measure(args.precision, args.layout, args.rate, args.duration,
-                                     args.step_patterns, args.copy_rows)), flush=True)
+                                     args.step_patterns, args.in_place_rows)), flush=True)
 
 
-def serving_measure(precision, layout, rate, duration, step_patterns, copy_rows):
+def serving_measure(precision, layout, rate, duration, step_patterns, in_place):
     """The serving workload of run_serving; returns its JSON object."""
     from emida_gb300 import Server, synth
     from oracle import oracle as eo
@@ -466,7 +466,7 @@ def serving_measure(precision, layout, rate, duration, step_patterns, copy_rows)
     detector = layout == "detector"
     sizes = (1024,) if detector else (512, 1024)
     srv = Server(precision, hbm_bytes=24 << 30, step_patterns=step_patterns,
-                 zero_copy=not copy_rows)
+                 zero_copy=bool(in_place))
     rows_src, layouts = {}, {}
     for size in sizes:
         ref = synth.reference_pattern(size, 90 + size)
@@ -516,11 +516,19 @@ def serving_measure(precision, layout, rate, duration, step_patterns, copy_rows)
         for rid in pending:
             srv.wait(rid)
     st = srv.stats()
+    tr = srv.trace()
     srv.close()
+    # where the slowest 1 % of rows spent their time: queued before admission,
+    # waiting for their first step, between first and last step, and from the
+    # last step's launch to completion
+    slow = tr[np.argsort(tr[:, 4])[-max(1, len(tr) // 100):]] if len(tr) else tr
+    tail = [{"patterns": int(r[0]), "admit_ms": r[1], "first_launch_ms": r[2], "last_launch_ms": r[3],
+             "done_ms": r[4]} for r in slow]
     return {
         "metric": "row latency p50/p99 and ROI pairs/s under a Poisson stream of scan rows",
         "value": st["pairs_per_s"], "unit": "ROI pairs/s", "n_gpus": 1,
         "latency_ms": {"p50": st["p50_ms"], "p99": st["p99_ms"]}, "rows": st["completed"],
+        "slowest_rows": tail,
         "pairs": sent_pairs, "higher_is_better": True,
         "dtype": "f32" if precision == "float" else "f64", "data": "synthetic",
         "config": {"workload": ("Poisson rows: 32-512 patterns of 1024^2, 100 ROIs of 64x64 (10x10 "
@@ -529,8 +537,8 @@ def serving_measure(precision, layout, rate, duration, step_patterns, copy_rows)
                                 "per size, 25-225 ROIs radius 24-48, fit 3-9"),
                    "rate_rows_per_s": rate, "duration_s": duration,
                    "hbm_arena_bytes_per_size": 24 << 30, "step_patterns": step_patterns,
-                   "rows": "copied into the device arena" if copy_rows else
-                           "pinned rows read in place by the kernels (no copy-engine transfer)"},
+                   "rows": "pinned rows read in place by the kernels" if in_place else
+                           "row bands copied into the device arena by SM loads beside the steps"},
         "parity": {"max_abs_err_px": max(errs),
                    "rms_err_px": float(np.sqrt(np.concatenate(sq).mean())),
                    "vs": "FP64 oracle, one row per size"},

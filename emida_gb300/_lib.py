@@ -77,6 +77,7 @@ SIGNATURES = {
     "emida_gb_server_wait": [_VP, ctypes.c_uint64, _DP, _DP, _DP],
     "emida_gb_server_stats": [_VP, _DP, _DP, _DP, ctypes.POINTER(ctypes.c_uint64)],
     "emida_gb_server_reset_stats": [_VP],
+    "emida_gb_server_trace": [_VP, _DP, ctypes.c_uint64, ctypes.POINTER(ctypes.c_uint64)],
     "emida_gb_server_destroy": [_VP],
     "emida_gb_resolved_mode": [_VP],
     "emida_gb_ingest": [_VP],

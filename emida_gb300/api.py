@@ -444,7 +444,7 @@ class Server:
     per size) and computed in shared steps of up to `step_patterns` patterns.
     """
 
-    def __init__(self, precision="float", hbm_bytes=8 << 30, step_patterns=64, zero_copy=True):
+    def __init__(self, precision="float", hbm_bytes=8 << 30, step_patterns=64, zero_copy=False):
         self.precision = _precision(precision)
         h = ctypes.c_void_p()
         _lib.call("emida_gb_server_create", self.precision, int(hbm_bytes), int(step_patterns),
@@ -453,7 +453,8 @@ class Server:
         self.rois = []
         self._rows = {}
         # True: every pinned row read in place; "sparse": rows of layouts whose
-        # ROIs cover at most half of the pattern; False: every row copied
+        # ROIs cover at most half of the pattern; False: every row copied into
+        # the arena (by SM loads beside the running steps where aligned)
         level = 1 if zero_copy == "sparse" else 2 if zero_copy else 0
         _lib.call("emida_gb_server_set_zero_copy", h, level)
 
@@ -497,6 +498,17 @@ class Server:
                   ctypes.byref(rate), ctypes.byref(done))
         return {"p50_ms": p50.value, "p99_ms": p99.value, "pairs_per_s": rate.value,
                 "completed": done.value}
+
+    def trace(self):
+        """Per completed row (completion order): [patterns, ms to admission,
+        ms to its first step's launch, ms to its last step's launch, ms to
+        completion], all from its submission."""
+        n = ctypes.c_uint64()
+        _lib.call("emida_gb_server_trace", self._h, None, 0, ctypes.byref(n))
+        out = np.zeros((n.value, 5))
+        if n.value:
+            _lib.call("emida_gb_server_trace", self._h, _dptr(out), n.value, ctypes.byref(n))
+        return out
 
     def reset_stats(self):
         _lib.call("emida_gb_server_reset_stats", self._h)

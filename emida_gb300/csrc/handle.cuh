@@ -77,6 +77,13 @@ int run_any(emida_gb_handle *h, const void *pics, uint32_t pats, void *maxes, vo
 int check_device_error(emida_gb_handle *h, uint32_t *word = nullptr);
 // EMIDA_GB_OK for no flags, else EMIDA_GB_DEVICE_CHECK with the flags named.
 int device_flags_status(uint32_t flags);
+// CTA slots that a multi-layout planner's default one-wave launches leave free
+// for kernels running beside them (0: none).
+int multi_reserve_ctas(emida_gb_multi *m, int ctas);
+// Sizes every work set of a multi-layout planner for runs of up to `patterns`
+// patterns of its registered layouts, so that such runs allocate (and free,
+// which waits for the whole device) nothing.
+int multi_reserve_work(emida_gb_multi *m, uint32_t patterns);
 // Recomputes the test hooks' reference spectra (fused and tensor forms) from
 // the registered reference pattern; nothing when no hook buffers exist.
 int stage_hooks_reference(emida_gb_handle *h);

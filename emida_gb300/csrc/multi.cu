@@ -33,8 +33,11 @@ struct emida_gb_multi {
         void *d_spec = nullptr;  // [rois][n/2 + 1][n] complex, column-major per ROI
         size_t spec_cap = 0;     // in ROIs
         const void *hann = nullptr, *twiddles = nullptr;  // owned by the class's first layout
-        int grid = 0;  // 0: one wave of resident CTAs
+        int grid = 0;  // 0: one wave of resident CTAs (less `reserve`)
     };
+    // CTA slots a default (one-wave) launch leaves free for kernels that run
+    // beside it, such as the request loop's SM copies of the next rows
+    int reserve = 0;
     // Work lists of a run, per size class.  Plain runs rotate through RING
     // sets, so uploading one run's lists waits only for the run RING back, not
     // for the stream; the last set belongs to the captured graph.
@@ -314,7 +317,7 @@ int launch_plan(emida_gb_multi *m, const plan &pl, const work_set &ws, const voi
                 a.stage = STAGE_TMA;
         }
         if (a.stage == STAGE_PLAIN && use_async) a.stage = STAGE_ASYNC;
-        const int grid = grid_override >= 0 ? grid_override : k.grid;
+        const int grid = grid_override >= 0 ? grid_override : k.grid ? k.grid : -m->reserve;
         CK(launch_fused(k.n, m->dbl, false, a, &map, grid, m->stream));
     }
     if (only_class >= 0) return EMIDA_GB_OK;
@@ -332,6 +335,47 @@ int launch_plan(emida_gb_multi *m, const plan &pl, const work_set &ws, const voi
 }
 
 }  // namespace
+
+int emida_gb::host::multi_reserve_work(emida_gb_multi *m, uint32_t patterns)
+{
+    if (!m) return fail(EMIDA_GB_INVALID_ARGUMENT, "null planner");
+    std::lock_guard<std::mutex> lk(m->mu);
+    // the largest layout of each size class bounds a run's work list there
+    std::vector<uint32_t> most(m->classes.size(), 0);
+    for (const auto &L : m->layouts) most[L.cls] = std::max(most[L.cls], L.n_rois);
+    // no set may be regrown under a run still reading it
+    CK(cudaStreamSynchronize(m->stream));
+    for (auto &ws : m->sets) {
+        ws.pending = false;
+        ws.d_items.resize(m->classes.size(), nullptr);
+        ws.cap.resize(m->classes.size(), 0);
+        size_t staging = 3 * 16 + 2 * (size_t)patterns * sizeof(void *) + (size_t)patterns * sizeof(uint32_t);
+        for (size_t c = 0; c < m->classes.size(); ++c) {
+            const size_t need = (size_t)patterns * most[c] * sizeof(uint4);
+            if (m->classes[c].fused && need) CKS(grow((void **)&ws.d_items[c], &ws.cap[c], need, 0));
+            staging += need;
+        }
+        CKS(grow((void **)&ws.d_ptrs, &ws.ptrs_cap, (size_t)patterns * sizeof(void *), 0));
+        CKS(grow((void **)&ws.d_sptrs, &ws.sptrs_cap, (size_t)patterns * sizeof(void *), 0));
+        CKS(grow((void **)&ws.d_sbase, &ws.sbase_cap, (size_t)patterns * sizeof(uint32_t), 0));
+        if (staging > ws.h_cap) {
+            if (ws.h_stage) CK(cudaFreeHost(ws.h_stage));
+            ws.h_stage = nullptr;
+            CK(cudaMallocHost((void **)&ws.h_stage, staging));
+            ws.h_cap = staging;
+        }
+    }
+    return EMIDA_GB_OK;
+}
+
+int emida_gb::host::multi_reserve_ctas(emida_gb_multi *m, int ctas)
+{
+    if (!m || ctas < 0) return fail(EMIDA_GB_INVALID_ARGUMENT, "bad argument");
+    std::lock_guard<std::mutex> lk(m->mu);
+    m->reserve = ctas;
+    drop_graph(m);  // captured with the grids chosen before
+    return EMIDA_GB_OK;
+}
 
 extern "C" {
 

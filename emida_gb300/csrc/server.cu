@@ -12,6 +12,7 @@
 // load / GPU / finalize thread pipeline of src/process_files.hpp:79-237, which
 // runs one layout and one row at a time.
 #include <algorithm>
+#include <array>
 #include <chrono>
 #include <condition_variable>
 #include <cstring>
@@ -35,6 +36,10 @@ constexpr uint32_t COPY_CHUNK = 16;
 // the loop, few enough that queuing them never blocks the loop (a full driver
 // queue would hold it, and with it every submit, for the copies' duration).
 constexpr uint32_t COPY_WINDOW = 8;
+// CTAs of the SM copies of a row's bands: host reads over NVLink-C2C reach the
+// link's rate from 16 CTAs; the steps' one-wave launches leave that many CTA
+// slots free so that the copy of the next chunk runs beside them.
+constexpr int COPY_CTAS = 16;
 
 struct request {
     uint64_t id = 0;
@@ -52,7 +57,10 @@ struct request {
     bool in_place = false;
     bool admitted = false, complete = false;
     int status = EMIDA_GB_OK;
-    clock_t_::time_point t_submit, t_done;
+    // when the row was submitted, admitted, had its first and its last step
+    // launched, and completed (its last step's results handed over)
+    clock_t_::time_point t_submit, t_admit, t_first_launch, t_last_launch, t_done;
+    bool launched = false;
 };
 
 struct step {
@@ -94,11 +102,18 @@ struct emida_gb_server {
         uint32_t pool, id, rois;
         bool sparse;  // ROIs cover at most half of the pattern: rows may be read in place
         std::vector<std::pair<uint32_t, uint32_t>> bands;  // (first row, rows) holding ROI pixels
+        // the bands as (first 16-byte chunk, chunks) runs of a pattern, for SM
+        // copies (null when a pattern row is not a whole number of chunks)
+        uint2 *d_runs = nullptr;
+        uint32_t n_runs = 0;
     };
     std::vector<layout_ref> layouts;
     std::map<uint64_t, std::unique_ptr<request>> requests;
     uint64_t next_id = 1;
     std::vector<double> latencies;  // ms, completed rows
+    // per completed row: patterns, then ms from submission to admission, to
+    // its first step's launch, to its last step's launch, to completion
+    std::vector<std::array<double, 5>> traces;
     uint64_t pairs_done = 0;
     clock_t_::time_point t_first;
     bool started = false;
@@ -108,9 +123,10 @@ struct emida_gb_server {
     bool stop = false;
     int error = EMIDA_GB_OK;
     std::string error_msg;
-    // which pinned rows the kernels read in place: 0 none, 1 rows of sparse
-    // layouts, 2 every pinned row (no copy-engine transfer on the row path)
-    int zero_copy = 2;
+    // which pinned rows the kernels read in place: 0 none (default: rows are
+    // copied into the arena, by SM loads where their alignment allows), 1
+    // rows of sparse layouts, 2 every pinned row
+    int zero_copy = 0;
 };
 
 namespace {
@@ -122,6 +138,7 @@ int admit(emida_gb_server *, pool &p)
         if (r->in_place) {
             p.pending.pop_front();
             r->admitted = true;
+            r->t_admit = clock_t_::now();
             p.active.push_back(r);
             continue;
         }
@@ -131,6 +148,7 @@ int admit(emida_gb_server *, pool &p)
         p.free_slots.resize(p.free_slots.size() - r->n);
         std::sort(r->slots.begin(), r->slots.end());  // consecutive slots copy as one
         r->admitted = true;
+        r->t_admit = clock_t_::now();
         p.active.push_back(r);
     }
     return EMIDA_GB_OK;
@@ -150,7 +168,11 @@ int issue_copies(emida_gb_server *sv, pool &p)
     const size_t row = (size_t)p.w * 2, pat = row * p.h;
     for (request *r : p.active) {
         if (r->in_place) continue;
-        const auto &bands = sv->layouts[r->layout].bands;
+        const auto &L = sv->layouts[r->layout];
+        const auto &bands = L.bands;
+        // pinned, 16-byte aligned rows of whole-chunk pattern rows: SM copies
+        // beside the running steps; otherwise the copy engine
+        const bool sm_copy = L.d_runs && (uintptr_t)r->host % 16 == 0;
         while (in_flight < COPY_WINDOW && r->chunks.size() * COPY_CHUNK < r->n) {
             const uint32_t c0 = (uint32_t)r->chunks.size() * COPY_CHUNK;
             const uint32_t c1 = std::min(r->n, c0 + COPY_CHUNK);
@@ -160,9 +182,12 @@ int issue_copies(emida_gb_server *sv, pool &p)
                 // patterns a..b-1 go to consecutive slots: one pitched copy per ROI row band
                 const char *src = reinterpret_cast<const char *>(r->host) + a * pat;
                 char *dst = reinterpret_cast<char *>(p.arena) + r->slots[a] * pat;
-                for (const auto &bd : bands)
-                    CK(cudaMemcpy2DAsync(dst + bd.first * row, pat, src + bd.first * row, pat,
-                                         bd.second * row, b - a, cudaMemcpyHostToDevice, p.copy));
+                if (sm_copy)
+                    CK(run_copy_bands(src, dst, L.d_runs, L.n_runs, pat / 16, b - a, COPY_CTAS, 0, p.copy));
+                else
+                    for (const auto &bd : bands)
+                        CK(cudaMemcpy2DAsync(dst + bd.first * row, pat, src + bd.first * row, pat,
+                                             bd.second * row, b - a, cudaMemcpyHostToDevice, p.copy));
                 a = b;
             }
             cudaEvent_t e;
@@ -259,6 +284,12 @@ int launch_step(emida_gb_server *sv, pool &p, step &st, bool other_busy)
     else
         CKS(emida_gb_multi_run_slots(p.m, p.arena, p.slots, (uint32_t)st.slots.size(), st.slots.data(),
                                      layout_of.data(), st.d_offs, st.d_coefs, nullptr));
+    const auto now = clock_t_::now();
+    for (const auto &part : st.parts) {
+        if (!part.r->launched) part.r->t_first_launch = now;
+        part.r->launched = true;
+        part.r->t_last_launch = now;
+    }
     cudaStream_t ms = (cudaStream_t)emida_gb_multi_stream(p.m);
     CK(cudaEventRecord(st.done, ms));
     CK(cudaStreamWaitEvent(p.out, st.done, 0));
@@ -286,8 +317,12 @@ void retire_step(emida_gb_server *sv, pool &p, step &st)
         if (r->done == r->n) {
             r->complete = true;
             r->t_done = clock_t_::now();
-            sv->latencies.push_back(
-                std::chrono::duration<double, std::milli>(r->t_done - r->t_submit).count());
+            auto ms = [&](clock_t_::time_point t) {
+                return std::chrono::duration<double, std::milli>(t - r->t_submit).count();
+            };
+            sv->latencies.push_back(ms(r->t_done));
+            sv->traces.push_back({(double)r->n, ms(r->t_admit), ms(r->t_first_launch), ms(r->t_last_launch),
+                                  ms(r->t_done)});
             p.active.erase(std::find(p.active.begin(), p.active.end(), r));
             for (cudaEvent_t e : r->chunks) cudaEventDestroy(e);
             r->chunks.clear();
@@ -378,7 +413,11 @@ int emida_gb_server_add_layout(emida_gb_server *sv, uint32_t src_w, uint32_t src
         CKS(emida_gb_multi_create(src_w, src_h, sv->precision, &p->m));
         CK(cudaMalloc((void **)&p->arena, (size_t)p->slots * bytes));
         for (uint32_t s = 0; s < p->slots; ++s) p->free_slots.push_back(p->slots - 1 - s);
-        CK(cudaStreamCreateWithFlags(&p->copy, cudaStreamNonBlocking));
+        // copies go first: their CTAs are dispatched ahead of a step's pending CTAs
+        int least = 0, greatest = 0;
+        CK(cudaDeviceGetStreamPriorityRange(&least, &greatest));
+        CK(cudaStreamCreateWithPriority(&p->copy, cudaStreamNonBlocking, greatest));
+        CKS(multi_reserve_ctas(p->m, COPY_CTAS));
         CK(cudaStreamCreateWithFlags(&p->out, cudaStreamNonBlocking));
         sv->pools.push_back(std::move(p));
     }
@@ -396,8 +435,22 @@ int emida_gb_server_add_layout(emida_gb_server *sv, uint32_t src_w, uint32_t src
             bands.push_back(v);
     }
     for (auto &b : bands) b.second -= b.first;
-    sv->layouts.push_back({pi, id, n_rois, sparse, bands});
-    sv->pools[pi]->max_rois = std::max(sv->pools[pi]->max_rois, n_rois);
+    emida_gb_server::layout_ref L{pi, id, n_rois, sparse, bands};
+    if (((size_t)src_w * 2) % 16 == 0) {
+        const uint32_t row16 = src_w * 2 / 16;
+        std::vector<uint2> runs;
+        for (const auto &b : bands) runs.push_back(make_uint2(b.first * row16, b.second * row16));
+        CK(cudaMalloc((void **)&L.d_runs, runs.size() * sizeof(uint2)));
+        CK(cudaMemcpy(L.d_runs, runs.data(), runs.size() * sizeof(uint2), cudaMemcpyHostToDevice));
+        L.n_runs = (uint32_t)runs.size();
+    }
+    sv->layouts.push_back(std::move(L));
+    pool &pp = *sv->pools[pi];
+    pp.max_rois = std::max(pp.max_rois, n_rois);
+    // sized now for the largest step, so that serving allocates and frees
+    // nothing (a free waits for the whole device)
+    CKS(multi_reserve_work(pp.m, sv->step_patterns));
+    for (auto &st : pp.steps) CKS(ensure_step_buffers(st, (size_t)sv->step_patterns * pp.max_rois));
     *layout_id = (uint32_t)sv->layouts.size() - 1;
     return EMIDA_GB_OK;
 }
@@ -492,11 +545,23 @@ int emida_gb_server_stats(emida_gb_server *sv, double *p50_ms, double *p99_ms, d
     return EMIDA_GB_OK;
 }
 
+int emida_gb_server_trace(emida_gb_server *sv, double *rows, uint64_t capacity, uint64_t *count)
+{
+    if (!sv || !count) return fail(EMIDA_GB_INVALID_ARGUMENT, "null argument");
+    std::lock_guard<std::mutex> lk(sv->mu);
+    *count = sv->traces.size();
+    if (rows)
+        for (uint64_t i = 0; i < sv->traces.size() && i < capacity; ++i)
+            std::memcpy(rows + 5 * i, sv->traces[i].data(), 5 * sizeof(double));
+    return EMIDA_GB_OK;
+}
+
 int emida_gb_server_reset_stats(emida_gb_server *sv)
 {
     if (!sv) return fail(EMIDA_GB_INVALID_ARGUMENT, "null argument");
     std::lock_guard<std::mutex> lk(sv->mu);
     sv->latencies.clear();
+    sv->traces.clear();
     sv->pairs_done = 0;
     sv->started = false;
     return EMIDA_GB_OK;
@@ -515,6 +580,8 @@ void emida_gb_server_destroy(emida_gb_server *sv)
         if (pp->copy) cudaStreamSynchronize(pp->copy);
     for (auto &kv : sv->requests)
         for (cudaEvent_t e : kv.second->chunks) cudaEventDestroy(e);
+    for (auto &L : sv->layouts)
+        if (L.d_runs) cudaFree(L.d_runs);
     for (auto &pp : sv->pools) {
         pool &p = *pp;
         if (p.m) emida_gb_multi_synchronize(p.m);

@@ -265,9 +265,12 @@ void emida_gb_multi_destroy(emida_gb_multi *m);
  * and computed in steps of up to step_patterns patterns drawn from every
  * admitted row in turn, so rows that arrive while others run share the next
  * steps.  The host patterns must stay valid until the request is waited for;
- * pinned memory lets the copies overlap.  A pinned row is not copied at all:
- * the kernels read its ROI pixels in place (emida_gb_server_set_zero_copy sets
- * which rows).  Results are per row, pattern-major. */
+ * pinned memory lets the copies overlap.  A row's ROI row bands are copied in
+ * chunks of 16 patterns, by SM loads on 16 CTAs beside the running steps when
+ * the row is pinned and 16-byte aligned and a pattern row is a whole number of
+ * 16-byte chunks (the steps leave those CTA slots free), else by the copy
+ * engine.  emida_gb_server_set_zero_copy can instead have the kernels read
+ * pinned rows' ROI pixels in place.  Results are per row, pattern-major. */
 typedef struct emida_gb_server emida_gb_server;
 int emida_gb_server_create(int32_t precision, uint64_t hbm_bytes, uint32_t step_patterns,
                            emida_gb_server **out);
@@ -277,10 +280,11 @@ int emida_gb_server_add_layout(emida_gb_server *s, uint32_t src_w, uint32_t src_
 int emida_gb_server_submit(emida_gb_server *s, uint32_t layout_id, const uint16_t *patterns,
                            uint32_t n, uint64_t *request_id);
 /* Which pinned rows submitted later are read in place rather than copied into
- * the arena: 2 every pinned row (default), 1 rows of layouts whose ROIs cover
- * at most half of the pattern, 0 none.  Reading in place keeps the row path
- * off the copy engine, whose transfers stalled for tens of milliseconds at
- * times on a shared host. */
+ * the arena: 2 every pinned row, 1 rows of layouts whose ROIs cover at most
+ * half of the pattern, 0 none (default).  A row read in place needs no arena
+ * slots, but its steps run at the host link's rate for scattered ROI rows
+ * (about 11 M ROI pairs/s at 1024^2 with 100 ROIs of 64^2); copied rows run
+ * at the device-resident rate while the next rows' copies proceed beside them. */
 int emida_gb_server_set_zero_copy(emida_gb_server *s, int enable);
 /* Blocks until the row is done; offsets [n*rois][2], coefs [n*rois][6] may be
  * NULL; latency_ms = submission to completion. */
@@ -289,6 +293,12 @@ int emida_gb_server_wait(emida_gb_server *s, uint64_t request_id, double *offset
 /* p50/p99 row latency of completed rows and ROI pairs/s since the first submission. */
 int emida_gb_server_stats(emida_gb_server *s, double *p50_ms, double *p99_ms,
                           double *pairs_per_s, uint64_t *completed);
+/* Per-row timeline of the rows completed since the last reset, in completion
+ * order: rows[i][0..4] = patterns, then ms from submission to admission, to
+ * the launch of the row's first step, to the launch of its last step, and to
+ * completion.  Writes min(count, capacity) rows (rows may be NULL to ask for
+ * the count only). */
+int emida_gb_server_trace(emida_gb_server *s, double *rows, uint64_t capacity, uint64_t *count);
 int emida_gb_server_reset_stats(emida_gb_server *s);
 void emida_gb_server_destroy(emida_gb_server *s);
 
