@@ -563,6 +563,13 @@ int emida_gb_subpixel_max(const double *neigh, int s, uint32_t n, double *sub, d
 
 int emida_gb_create(const emida_gb_params *p, emida_gb_handle **out)
 {
+    return create_handle(p, 0, out);
+}
+
+}  // extern "C"
+
+int emida_gb::host::create_handle(const emida_gb_params *p, uint32_t fused_len, emida_gb_handle **out)
+{
     if (!out) return fail(EMIDA_GB_INVALID_ARGUMENT, "null output handle");
     *out = nullptr;
     CKS(validate(p));
@@ -594,7 +601,16 @@ int emida_gb_create(const emida_gb_params *p, emida_gb_handle **out)
     // The fused kernel takes square ROIs up to 96 pixels (64 in FP64); a ROI
     // whose 2*side is not one of its transform lengths is zero-padded into the
     // next one, which leaves every lag of the 2*side-1 window unchanged.
-    const uint32_t fn = h->fft ? fused_size_for(p->slice_w, h->dbl, h->in_f64) : 0;
+    uint32_t fn = h->fft ? fused_size_for(p->slice_w, h->dbl, h->in_f64) : 0;
+    if (fused_len && fn) {
+        // a longer fused transform chosen by the caller (the multi-layout autotuner)
+        if (fused_len < 2 * p->slice_w || !fused_supported(fused_len, h->dbl, h->in_f64)) {
+            delete h;
+            return fail(EMIDA_GB_UNSUPPORTED, "no fused %u-point transform for ROI side %u", fused_len,
+                        p->slice_w);
+        }
+        fn = fused_len;
+    }
     const bool fusable = fn != 0;
     if (p->mode == EMIDA_GB_MODE_FUSED && !fusable) {
         delete h;
@@ -724,6 +740,8 @@ int emida_gb_create(const emida_gb_params *p, emida_gb_handle **out)
     *out = h;
     return EMIDA_GB_OK;
 }
+
+extern "C" {
 
 int emida_gb_set_reference(emida_gb_handle *h, const void *ref)
 {

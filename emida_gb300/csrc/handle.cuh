@@ -77,6 +77,9 @@ int run_any(emida_gb_handle *h, const void *pics, uint32_t pats, void *maxes, vo
 int check_device_error(emida_gb_handle *h, uint32_t *word = nullptr);
 // EMIDA_GB_OK for no flags, else EMIDA_GB_DEVICE_CHECK with the flags named.
 int device_flags_status(uint32_t flags);
+// emida_gb_create with the fused transform length forced to fused_len (0: the
+// smallest that holds the ROI), for the multi-layout autotuner.
+int create_handle(const emida_gb_params *p, uint32_t fused_len, emida_gb_handle **out);
 // CTA slots that a multi-layout planner's default one-wave launches leave free
 // for kernels running beside them (0: none).
 int multi_reserve_ctas(emida_gb_multi *m, int ctas);

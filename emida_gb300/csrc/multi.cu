@@ -336,6 +336,79 @@ int launch_plan(emida_gb_multi *m, const plan &pl, const work_set &ws, const voi
 
 }  // namespace
 
+namespace {
+
+// The parameters of a layout's handle (reference spectra, and the staged
+// pipeline for sides without a fused kernel).
+emida_gb_params layout_params(const emida_gb_multi *m, const uint32_t *begins, uint32_t n_rois, uint32_t side,
+                              int32_t fitsize)
+{
+    emida_gb_params p{};
+    p.src_w = m->src_w;
+    p.src_h = m->src_h;
+    p.begins = begins;
+    p.n_rois = n_rois;
+    p.slice_w = p.slice_h = side;
+    p.cross_w = p.cross_h = 2 * side - 1;
+    // layouts without a fused kernel run the staged pipeline over up to
+    // STAGED_BATCH of their patterns per launch sequence
+    p.batch_size = fused_size_for(side, m->dbl) ? 1 : STAGED_BATCH;
+    p.policy = EMIDA_GB_FFT;
+    p.precision = m->precision;
+    p.fitsize = fitsize;
+    p.in_type = EMIDA_GB_IN_U16;
+    p.mode = EMIDA_GB_MODE_AUTO;
+    p.in_buffers = 1;
+    return p;
+}
+
+// Handles of the given layouts at fused length n (their reference spectra
+// computed from the reference pattern their current handles hold).
+int class_handles(emida_gb_multi *m, const std::vector<size_t> &members, uint32_t n,
+                  std::vector<emida_gb_handle *> &out)
+{
+    for (emida_gb_handle *h : out) emida_gb_destroy(h);
+    out.clear();
+    std::vector<uint16_t> ref((size_t)m->src_w * m->src_h);
+    for (size_t i : members) {
+        const auto &L = m->layouts[i];
+        CK(cudaMemcpy(ref.data(), L.h->d_ref_in, ref.size() * sizeof(uint16_t), cudaMemcpyDeviceToHost));
+        const emida_gb_params p = layout_params(m, L.h->begins.data(), L.n_rois, L.side, L.fitsize);
+        emida_gb_handle *h = nullptr;
+        CKS(create_handle(&p, n, &h));
+        out.push_back(h);
+        CKS(emida_gb_set_reference(h, ref.data()));
+    }
+    return EMIDA_GB_OK;
+}
+
+// Class c's resident spectra (and twiddles, window) at fused length n, from
+// `hs` (one handle per member, in member order) or, when empty, from the
+// members' own handles.
+int install_class_spectra(emida_gb_multi *m, size_t c, const std::vector<size_t> &members,
+                          const std::vector<emida_gb_handle *> &hs, uint32_t n)
+{
+    auto &k = m->classes[c];
+    CK(cudaStreamSynchronize(m->stream));  // no run may read the spectra being replaced
+    const size_t per = spec_bytes_per_roi(n, m->dbl);
+    size_t cap = k.spec_cap * spec_bytes_per_roi(k.n, m->dbl);
+    CKS(grow(&k.d_spec, &cap, k.begins.size() * per, 0));
+    k.spec_cap = cap / per;
+    for (size_t j = 0; j < members.size(); ++j) {
+        const auto &L = m->layouts[members[j]];
+        emida_gb_handle *h = hs.empty() ? L.h : hs[j];
+        CK(cudaMemcpy((char *)k.d_spec + (size_t)L.roi_base * per, h->d_ref_spec_cm, (size_t)L.n_rois * per,
+                      cudaMemcpyDeviceToDevice));
+    }
+    emida_gb_handle *first = hs.empty() ? m->layouts[members.front()].h : hs.front();
+    k.n = n;
+    k.hann = first->d_hann_fused;
+    k.twiddles = first->d_tw_row;
+    return EMIDA_GB_OK;
+}
+
+}  // namespace
+
 int emida_gb::host::multi_reserve_work(emida_gb_multi *m, uint32_t patterns)
 {
     if (!m) return fail(EMIDA_GB_INVALID_ARGUMENT, "null planner");
@@ -409,22 +482,7 @@ int emida_gb_multi_add_layout(emida_gb_multi *m, const uint32_t *begins, uint32_
 {
     if (!m || !begins || !ref || !layout_id) return fail(EMIDA_GB_INVALID_ARGUMENT, "null argument");
     std::lock_guard<std::mutex> lk(m->mu);
-    emida_gb_params p{};
-    p.src_w = m->src_w;
-    p.src_h = m->src_h;
-    p.begins = begins;
-    p.n_rois = n_rois;
-    p.slice_w = p.slice_h = side;
-    p.cross_w = p.cross_h = 2 * side - 1;
-    // layouts without a fused kernel run the staged pipeline over up to
-    // STAGED_BATCH of their patterns per launch sequence
-    p.batch_size = fused_size_for(side, m->dbl) ? 1 : STAGED_BATCH;
-    p.policy = EMIDA_GB_FFT;
-    p.precision = m->precision;
-    p.fitsize = fitsize;
-    p.in_type = EMIDA_GB_IN_U16;
-    p.mode = EMIDA_GB_MODE_AUTO;
-    p.in_buffers = 1;
+    const emida_gb_params p = layout_params(m, begins, n_rois, side, fitsize);
     emida_gb_handle *h = nullptr;
     CKS(emida_gb_create(&p, &h));
     int st = emida_gb_set_reference(h, ref);
@@ -607,31 +665,79 @@ int emida_gb_multi_autotune(emida_gb_multi *m, const void *dev_patterns, uint32_
     cudaEvent_t a, b;
     CK(cudaEventCreate(&a));
     CK(cudaEventCreate(&b));
-    for (size_t c = 0; c < m->classes.size(); ++c) {
+    auto time_grid = [&](size_t c, int grid, float &ms) -> int {
+        CKS(launch_plan(m, pl, ws, dev_patterns, patterns, dev_offsets, nullptr, nullptr, (int)c, grid));
+        CK(cudaEventRecord(a, m->stream));
+        for (int r = 0; r < 3; ++r)
+            CKS(launch_plan(m, pl, ws, dev_patterns, patterns, dev_offsets, nullptr, nullptr, (int)c, grid));
+        CK(cudaEventRecord(b, m->stream));
+        CK(cudaEventSynchronize(b));
+        CK(cudaEventElapsedTime(&ms, a, b));
+        ms /= 3;
+        return EMIDA_GB_OK;
+    };
+    int st = EMIDA_GB_OK;
+    for (size_t c = 0; c < m->classes.size() && st == EMIDA_GB_OK; ++c) {
         auto &k = m->classes[c];
         if (!k.fused || pl.items[c].empty()) continue;
+        // tile shapes: the transform lengths that hold the ROI (its own and the
+        // next one, which zero-pads it further), each with 1..6 CTAs per SM
+        std::vector<uint32_t> lens;
+        for (uint32_t n : {64u, 96u, 128u, 192u, 256u})
+            if (n >= 2 * k.side && fused_supported(n, m->dbl) && lens.size() < 2) lens.push_back(n);
+        std::vector<size_t> members;
+        for (size_t i = 0; i < m->layouts.size(); ++i)
+            if (m->layouts[i].cls == (int)c) members.push_back(i);
+        const uint32_t n0 = k.n;
         float best = 1e30f;
         int best_grid = 0;
-        for (int per_sm = 1; per_sm <= 6; ++per_sm) {
-            const int grid = per_sm * sms;
-            CKS(launch_plan(m, pl, ws, dev_patterns, patterns, dev_offsets, nullptr, nullptr, (int)c, grid));
-            CK(cudaEventRecord(a, m->stream));
-            for (int r = 0; r < 3; ++r)
-                CKS(launch_plan(m, pl, ws, dev_patterns, patterns, dev_offsets, nullptr, nullptr, (int)c,
-                                grid));
-            CK(cudaEventRecord(b, m->stream));
-            CK(cudaEventSynchronize(b));
-            float ms = 0;
-            CK(cudaEventElapsedTime(&ms, a, b));
-            if (ms < best * 0.98f) {
-                best = ms;
-                best_grid = grid;
+        uint32_t best_n = n0;
+        std::string tried;
+        std::vector<emida_gb_handle *> alt;  // the other length's handles, one per member
+        for (uint32_t n : lens) {
+            if (n != n0) {
+                st = class_handles(m, members, n, alt);
+                if (st == EMIDA_GB_OK) st = install_class_spectra(m, c, members, alt, n);
+            } else if (k.n != n0) {
+                st = install_class_spectra(m, c, members, {}, n0);  // the members' own length again
+            }
+            if (st != EMIDA_GB_OK) break;
+            float nbest = 1e30f;
+            int ngrid = 0;
+            for (int per_sm = 1; per_sm <= 6 && st == EMIDA_GB_OK; ++per_sm) {
+                float ms = 0;
+                st = time_grid(c, per_sm * sms, ms);
+                if (st == EMIDA_GB_OK && ms < nbest * 0.98f) {
+                    nbest = ms;
+                    ngrid = per_sm * sms;
+                }
+            }
+            if (st != EMIDA_GB_OK) break;
+            char t[48];
+            snprintf(t, sizeof t, "%sn=%u %.3f ms", tried.empty() ? "" : ", ", n, nbest);
+            tried += t;
+            if (nbest < best * 0.98f) {
+                best = nbest;
+                best_grid = ngrid;
+                best_n = n;
             }
         }
+        // keep the winning length's spectra and handles
+        std::vector<emida_gb_handle *> orig;
+        for (size_t i : members) orig.push_back(m->layouts[i].h);
+        if (st == EMIDA_GB_OK && best_n != n0) {
+            for (size_t j = 0; j < members.size(); ++j) m->layouts[members[j]].h = alt[j];
+            alt.swap(orig);
+        }
+        int st2 = install_class_spectra(m, c, members, {}, best_n);
+        if (st == EMIDA_GB_OK) st = st2;
+        CK(cudaStreamSynchronize(m->stream));
+        for (emida_gb_handle *h : alt) emida_gb_destroy(h);
+        if (st != EMIDA_GB_OK) break;
         k.grid = best_grid;
-        char line[160];
-        snprintf(line, sizeof line, "side %u (n=%u): %zu pairs, grid %d (%d per SM), %.3f ms\n",
-                 k.side, k.n, pl.items[c].size(), best_grid, best_grid / std::max(1, sms), best / 3);
+        char line[256];
+        snprintf(line, sizeof line, "side %u (n=%u): %zu pairs, grid %d (%d per SM), %.3f ms [%s]\n", k.side,
+                 k.n, pl.items[c].size(), best_grid, best_grid / std::max(1, sms), best, tried.c_str());
         rep += line;
     }
     cudaEventDestroy(a);
@@ -642,7 +748,7 @@ int emida_gb_multi_autotune(emida_gb_multi *m, const void *dev_patterns, uint32_
         std::strncpy(report, rep.c_str(), report_len - 1);
         report[report_len - 1] = 0;
     }
-    return EMIDA_GB_OK;
+    return st;
 }
 
 void emida_gb_multi_destroy(emida_gb_multi *m)

@@ -128,3 +128,47 @@ def test_multi_autotune_and_errors(scene):
     with pytest.raises(EmidaError, match="unknown layout"):
         m.run(d_pics, [99], d_offs, graph=False)
     m.close()
+
+
+def test_autotune_transform_lengths_keep_parity():
+    """Zero-padded ROI sides have two fused transform lengths to choose from
+    (side 24: 64 or 96 points, side 40: 96 or 128, side 56: 128 or 192); the
+    autotuner times both with 1..6 CTAs per SM, keeps the faster, and the
+    results stay the oracle's whichever length it kept."""
+    from emida_gb300 import DeviceBuffer, MultiLayout, synth
+    from tests.test_gpu_synthetic import well_posed
+    from oracle import oracle as eo
+    ref = synth.reference_pattern(512, seed=23)
+    pics, _ = synth.deformed_patterns(512, 23, 4, sigma_eps=3e-3)
+    layouts = []
+    for i, (side, s, n) in enumerate([(24, 3, 12), (40, 5, 9), (56, 7, 6)]):
+        _, b = synth.random_layout(512, 300 + i, side // 2, n, margin=4)
+        layouts.append((b, side, s))
+    layout_of = np.array([0, 1, 2, 1], dtype=np.uint32)
+    m = MultiLayout((512, 512), "float")
+    for b, side, s in layouts:
+        m.add_layout(b, side, s, ref)
+    total = m.count(layout_of)
+    d_pics = DeviceBuffer.from_array(pics)
+    d_offs, d_coefs = DeviceBuffer(total * 16), DeviceBuffer(total * 48)
+    d_max = DeviceBuffer(total * m.data_index.itemsize)
+    report = m.autotune(d_pics, layout_of, d_offs)
+    lines = report.strip().splitlines()
+    assert len(lines) == 3
+    for line, (a, b) in zip(lines, [(64, 96), (96, 128), (128, 192)]):
+        assert f"n={a} " in line and f"n={b} " in line, line
+    m.run(d_pics, layout_of, d_offs, d_coefs, d_max, graph=False)
+    m.synchronize()
+    offs = d_offs.download(np.float64, (total, 2))
+    coefs = d_coefs.download(np.float64, (total, 6))
+    peaks = d_max.download(m.data_index, total)["index"]
+    m.close()
+    start = 0
+    for p, lid in enumerate(layout_of):
+        b, side, s = layouts[lid]
+        o, c, k = eo.get_offsets(ref, pics[p:p + 1], b, side, side, eo.POLICY_FFT, s)
+        sl = slice(start, start + len(b))
+        assert np.array_equal(peaks[sl], k), (p, side)
+        ok = well_posed(c, s)
+        assert (np.abs(offs[sl] - o)[ok] <= 1e-3).all(), (p, side)
+        start += len(b)
