@@ -762,10 +762,9 @@ int emida_gb_set_reference(emida_gb_handle *h, const void *ref)
         if (h->d_ref_spec_cm) {
             CK(run_spec_to_colmajor(h->d_ref_spec, h->d_ref_spec_cm, h->S, h->w2, h->h2, h->dbl,
                                     h->comp));
-            // the one-CTA fused kernels correlate the packed DC and Nyquist
-            // slot directly, from the reference's row sums in column 0
-            if (h->w2 != 256)
-                CK(run_ref_row_sums(h->d_ref_prep, h->d_ref_spec_cm, h->S, h->w2, h->dbl, h->comp));
+            // the fused kernels correlate the packed DC and Nyquist slot
+            // directly, from the reference's row sums in column 0
+            CK(run_ref_row_sums(h->d_ref_prep, h->d_ref_spec_cm, h->S, h->w2, h->dbl, h->comp));
         }
     }
     // the path's kernel is loaded now rather than at the first batch

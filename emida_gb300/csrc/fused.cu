@@ -169,13 +169,17 @@ __device__ __forceinline__ void conj_product(cplx<T> *v, const cplx<T> *R, int c
 // b = q (mod Q): the lanes' window heads 4 * block + b then fall in distinct
 // banks.  Lane q of the block writes outputs q, q + Q, ... to slot 0.
 template <int N> constexpr int packed_dq() { return 3 * N / 2 + 4; }
-template <int N, int THREADS, typename T>
-__device__ __forceinline__ void packed_column(cplx<T> *S, const T *dq, const T *rs, int side, int tid)
+// NCOMP components from comp_first on; slot0(tau) is the slot-0 entry of row
+// tau (in this CTA's spectrum, or in the partner's through distributed shared
+// memory).
+template <int N, int THREADS, int NCOMP, typename T, typename Slot0>
+__device__ __forceinline__ void packed_column(const Slot0 &slot0, const T *dq, const T *rs, int side, int tid,
+                                              int comp_first)
 {
-    constexpr int Q = THREADS / (N / 2), DQ = packed_dq<N>();
+    constexpr int Q = THREADS / (NCOMP * N / 4), DQ = packed_dq<N>();
     static_assert(Q == 2 || Q == 4, "lanes per block of 4 lags");
     const int q = tid % Q, blk = tid / Q;
-    const int comp = blk / (N / 4), tau0 = 4 * (blk % (N / 4));
+    const int comp = comp_first + blk / (N / 4), tau0 = 4 * (blk % (N / 4));
     const T *dv = dq + comp * DQ;
     const T *rv = rs + comp * (N / 2);
     auto start = [&](int k) {
@@ -208,7 +212,7 @@ __device__ __forceinline__ void packed_column(cplx<T> *S, const T *dq, const T *
     for (int k = 0; k < 4; k += Q) {
         const int j = k + q;  // this lane's output of the block
         const T v = j == 0 ? a0 : j == 1 ? a1 : j == 2 ? a2 : a3;
-        reinterpret_cast<T *>(sp<N>(S, tau0 + j, 0))[comp] = v * (T)N;
+        reinterpret_cast<T *>(slot0(tau0 + j))[comp] = v * (T)N;
     }
 }
 
@@ -554,7 +558,7 @@ __global__ void __launch_bounds__(N * G / 4, fused_min_blocks(N, sizeof(T)))
                 for (int j = 0; j < E; ++j) *sp<N>(S, t + G * j, c) = v[j];
             }
         }
-        packed_column<N, THREADS, T>(S, dq, rs, side, tid);
+        packed_column<N, THREADS, 2, T>([&](int tau) { return sp<N>(S, tau, 0); }, dq, rs, side, tid, 0);
         __syncthreads();
 
         // ---- inverse rows: pairs of half spectra -> two real rows ---------
@@ -710,7 +714,9 @@ struct layout {
     static constexpr size_t tw_fwd = xch + (size_t)GROUPS * N * 8;
     static constexpr size_t tw_inv = tw_fwd + (size_t)N * 8;
     static constexpr size_t hann = tw_inv + (size_t)N * 8;              // hx[side], hy[side]
-    static constexpr size_t red_val = hann + (size_t)N * 4;
+    static constexpr size_t dq = hann + (size_t)N * 4;                  // DC, Nyquist lines
+    static constexpr size_t rsum = dq + (size_t)2 * packed_dq<N>() * 4;  // reference row sums
+    static constexpr size_t red_val = rsum + (size_t)N * 4;
     static constexpr size_t red_idx = red_val + 32 * 4;
     static constexpr size_t psum = red_idx + 32 * 4;                    // partial sums [2]
     static constexpr size_t pbest_v = psum + 16;                        // CTA maxima [2]
@@ -748,6 +754,10 @@ __global__ void __cluster_dims__(2, 1, 1) __launch_bounds__(cl::THREADS, 1)
     C *twi = reinterpret_cast<C *>(smem + L::tw_inv);
     T *hx = reinterpret_cast<T *>(smem + L::hann);
     T *hy = hx + side;
+    constexpr int DQ = packed_dq<N>();
+    T *dq = reinterpret_cast<T *>(smem + L::dq);        // DC and Nyquist outputs of both CTAs' rows
+    T *dq_p = cluster.map_shared_rank(dq, peer);
+    T *rs = reinterpret_cast<T *>(smem + L::rsum);      // the reference's row sums (this ROI)
     T *red_v = reinterpret_cast<T *>(smem + L::red_val);
     uint32_t *red_i = reinterpret_cast<uint32_t *>(smem + L::red_idx);
     uint32_t *psum = reinterpret_cast<uint32_t *>(smem + L::psum);
@@ -779,6 +789,12 @@ __global__ void __cluster_dims__(2, 1, 1) __launch_bounds__(cl::THREADS, 1)
     }
     const T *ghann = reinterpret_cast<const T *>(a.hann);
     for (int i = tid; i < 2 * side; i += THREADS) hx[i] = ghann[i];
+    // the zero padding of the DC and Nyquist lines (the rows pass writes rows
+    // 0..N/2-1 and their copy at N..3N/2-1, in both CTAs)
+    for (int i = tid; i < 2 * DQ; i += THREADS) {
+        const int y = i % DQ;
+        if ((y >= N / 2 && y < N) || y >= 3 * N / 2) dq[i] = (T)0;
+    }
     const bool tma = a.stage == STAGE_TMA;
     if (tid == 0) {
         mbar_init(bar, 1);
@@ -841,6 +857,10 @@ __global__ void __cluster_dims__(2, 1, 1) __launch_bounds__(cl::THREADS, 1)
         const T mean = (T)(psum[0] + psum[1]) / (T)(side * side);
 
         // ---- forward rows: pairs of real rows as one complex FFT -----------
+        const C *R = reinterpret_cast<const C *>(a.ref_spec) + (size_t)roi * (H + 1) * N;
+        static_assert(N / 2 <= THREADS, "one reference row sum per thread");
+        // column 0 of the reference: its row sums, stored after the row FFTs
+        const C rsum = tid < side ? __ldg(R + tid) : cmake<C>((T)0, (T)0);
 #pragma unroll 1
         for (int rnd = 0; rnd < ROWS / 2 / GROUPS; ++rnd) {
             const int rl = 2 * (g + GROUPS * rnd), ra = r0 + rl, rb = ra + 1;
@@ -867,63 +887,58 @@ __global__ void __cluster_dims__(2, 1, 1) __launch_bounds__(cl::THREADS, 1)
                 const int k = t + G * j;
                 C *D = owner(k);
                 if (k == 0) {
+                    // the DC and Nyquist outputs go to both CTAs' lines
                     C zh = v[E / 2];
-                    *csp(D, ra, 0) = cmake<C>(z.x, zh.x);
-                    *csp(D, rb, 0) = cmake<C>(z.y, zh.y);
+                    for (T *line : {dq, dq_p}) {
+                        line[ra] = line[N + ra] = z.x;
+                        line[DQ + ra] = line[DQ + N + ra] = zh.x;
+                        line[rb] = line[N + rb] = z.y;
+                        line[DQ + rb] = line[DQ + N + rb] = zh.y;
+                    }
                 } else {
                     *csp(D, ra, k & 63) = cmake<C>((z.x + zm.x) * (T)0.5, (z.y - zm.y) * (T)0.5);
                     *csp(D, rb, k & 63) = cmake<C>((z.y + zm.y) * (T)0.5, (zm.x - z.x) * (T)0.5);
                 }
             }
         }
+        if (tid < side) {
+            rs[tid] = rsum.x;
+            rs[N / 2 + tid] = rsum.y;
+        }
         __syncthreads();
         if (tma && tid == 0 && pair + clusters < a.n_pairs) issue_tile(pair + clusters);
-        cluster.sync();  // B1: every spectrum row is complete in both CTAs
+        cluster.sync();  // B1: every spectrum row and both DC/Nyquist lines are complete
 
         // ---- columns: forward FFT, conj product, inverse FFT (local) -------
-        const C *R = reinterpret_cast<const C *>(a.ref_spec) + (size_t)roi * (H + 1) * N;
+        // CTA 0's slot 0 packs the DC and Nyquist columns: it is the direct
+        // correlation of packed_column, CTA 0 the DC half and CTA 1 the
+        // Nyquist half; CTA 0's groups take its columns 1..63 (the last round
+        // leaves its last group without one), CTA 1's groups all 64 of theirs.
+        const int c_first = rank == 0 ? 1 : 0;
 #pragma unroll 1
         for (int rnd = 0; rnd < SLOTS / GROUPS; ++rnd) {
-            const int c = g + rnd * GROUPS, kx = SLOTS * rank + c;
-            C v[E];
+            const int c = c_first + g + rnd * GROUPS, kx = SLOTS * rank + c;
+            const unsigned mask = __ballot_sync(0xffffffffu, c < SLOTS);
+            if (c < SLOTS) {
+                C v[E];
 #pragma unroll
-            for (int m = 0; m < E / 2; ++m) v[m] = *csp(S, t + G * m, c);
-            struct cline {
-                C *S;
-                int c;
-                __device__ __forceinline__ C *operator()(int q) const { return csp(S, q, c); }
-            } line{S, c};
-            group_fft<N, -1, true, T, G>(v, t, line, twf);
-            const C *Rc = R + (size_t)kx * N;
-            if (rank == 0 && warp == 0 && rnd == 0) {
-                // column 0 packs the DC and Nyquist columns (see the one-CTA kernel)
-#pragma unroll
-                for (int j = 0; j < E; ++j) *csp(S, t + G * j, c) = v[j];
-                __syncwarp();
-#pragma unroll
-                for (int j = 0; j < E; ++j) {
-                    const int ky = t + G * j;
-                    if (c == 0) {
-                        C x = v[j];
-                        C xm = *csp(S, ky == 0 ? 0 : N - ky, 0);
-                        C p0 = cmake<C>((x.x + xm.x) * (T)0.5, (x.y - xm.y) * (T)0.5);
-                        C pn = cmake<C>((x.y + xm.y) * (T)0.5, (xm.x - x.x) * (T)0.5);
-                        C q0 = cmulc(p0, __ldg(R + ky));
-                        C qn = cmulc(pn, __ldg(R + (size_t)H * N + ky));
-                        v[j] = cmake<C>(q0.x - qn.y, q0.y + qn.x);
-                    } else {
-                        v[j] = cmulc(v[j], __ldg(Rc + ky));
-                    }
-                }
-                __syncwarp();
-            } else {
+                for (int m = 0; m < E / 2; ++m) v[m] = *csp(S, t + G * m, c);
+                struct cline {
+                    C *S;
+                    int c;
+                    __device__ __forceinline__ C *operator()(int q) const { return csp(S, q, c); }
+                } line{S, c};
+                group_fft<N, -1, true, T, G>(v, t, line, twf, mask);
+                const C *Rc = R + (size_t)kx * N;
 #pragma unroll
                 for (int j = 0; j < E; ++j) v[j] = cmulc(v[j], __ldg(Rc + t + G * j));
-            }
-            group_fft<N, +1, false, T, G>(v, t, line, twi);
+                group_fft<N, +1, false, T, G>(v, t, line, twi, mask);
 #pragma unroll
-            for (int j = 0; j < E; ++j) *csp(S, t + G * j, c) = v[j];
+                for (int j = 0; j < E; ++j) *csp(S, t + G * j, c) = v[j];
+            }
         }
+        C *S0 = owner(0);  // CTA 0's spectrum, which holds slot 0
+        packed_column<N, THREADS, 1, T>([&](int tau) { return csp(S0, tau, 0); }, dq, rs, side, tid, rank);
         cluster.sync();  // B2: every column is back in the spectrum
 
         // ---- inverse rows 128r..128r+127: two Hermitian rows per FFT -------
