@@ -160,6 +160,8 @@ __global__ void __launch_bounds__(BLOCK)
     const int tpl = BLOCK / lpb, l = threadIdx.x / tpl, lt = threadIdx.x % tpl;
     const uint32_t line = blockIdx.x * lpb + l;
     const bool live = l < lpb && line < n_lines;
+    // rows of up to 32 threads a line stay inside one warp between passes
+    const bool warp_lines = mode != LM_C2C_COLS && tpl <= 32;
     C *b0 = buf + (size_t)l * 2 * n, *b1 = b0 + n;
     const uint32_t map = live ? line / lines_per_map : 0, li = live ? line % lines_per_map : 0;
 
@@ -222,7 +224,10 @@ __global__ void __launch_bounds__(BLOCK)
                 }
             }
         }
-        __syncthreads();
+        if (warp_lines)
+            __syncwarp();
+        else
+            __syncthreads();
         C *tmp = cur;
         cur = nxt;
         nxt = tmp;
@@ -257,8 +262,11 @@ cudaError_t launch_lines(const void *in, void *out, int mode, int dir, int n, ui
 {
     using C = cplx<T>;
     line_plan plan = make_plan(n);
-    int lpb = n >= 512 ? 1 : 512 / n;
+    // rows: n/4 threads a line, one per radix-4 butterfly (a warp per
+    // 128-point row)
+    int lpb = n >= 1024 ? 1 : 1024 / n;
     if (mode == LM_C2C_COLS) {
+        lpb = n >= 512 ? 1 : 512 / n;
         // more columns per block make each row of the block's loads and stores
         // a longer contiguous run: up to 32, in at most 96 KB of shared memory
         const int fit = (int)(((96 * 1024) / sizeof(C) - (size_t)n) / (2 * (size_t)n));
