@@ -250,8 +250,12 @@ int emida_gb_multi_run_table(emida_gb_multi *m, const void *const *patterns, uin
 /* The planner's stream (a cudaStream_t) and a wait for its work. */
 void *emida_gb_multi_stream(emida_gb_multi *m);
 int emida_gb_multi_synchronize(emida_gb_multi *m);
-/* Times each fused transform size with 1..4 resident CTAs per SM on these
- * patterns and keeps the fastest grid; writes a one-line-per-size report. */
+/* Per ROI size class with a fused kernel, times on these patterns each
+ * candidate transform length (the smallest that holds the ROI and the next
+ * one, which zero-pads it further) with grids of 1..6 times the SM count
+ * (clusters of two CTAs at 256 points), keeps the fastest length and grid,
+ * rebuilds the class's resident reference spectra at that length, and writes
+ * a one-line-per-class report. */
 int emida_gb_multi_autotune(emida_gb_multi *m, const void *dev_patterns, uint32_t patterns,
                             const uint32_t *layout_of, double *dev_offsets, char *report,
                             size_t report_len);
