@@ -1,5 +1,6 @@
-"""The multi-GPU bookkeeping (sharding, max-over-ranks timing, whole-job
-rate) with two gloo ranks on the CPU."""
+"""The multi-GPU host side with two gloo ranks on the CPU: sharding,
+max-over-ranks timing, the whole-job rate, and each rank loading the library
+and gathering its shard's results."""
 import os
 import socket
 
