@@ -222,8 +222,14 @@ __device__ __forceinline__ void packed_column(const Slot0 &slot0, const T *dq, c
 // warps share an SM (65 M pairs/s at side 32, against 52 M with 4).
 __host__ __device__ constexpr int fused_min_blocks(int N, int tsize)
 {
-    return N == 192 ? 1 : N == 128 ? (tsize == 4 ? 2 : 1) : N == 64 && tsize == 4 ? 6 : (tsize == 4 ? 4 : 2);
+    return N == 192 || (N == 96 && tsize == 4) ? 1 : N == 128 ? (tsize == 4 ? 2 : 1) : N == 64 && tsize == 4 ? 6 : (tsize == 4 ? 4 : 2);
 }
+// Pairs one CTA carries side by side.  The FP32 96-point kernel's 3-warp
+// pairs ran 4 CTAs per SM, each in its own pass of the loop, and their
+// instruction working set outgrew the instruction cache; 4 pairs per CTA
+// keep the SM's warps in the same pass.  Each pair has its own shared-memory
+// block, barrier and warps; the CTA's barriers are common.
+template <int N, typename T> constexpr int fused_pairs_per_cta() { return N == 96 && sizeof(T) == 4 ? 4 : 1; }
 
 // Lane l fits buffered pair l: coefficients as sequential FP64 dot products
 // and the closed-form extremum (src/subpixel_max.hpp:14-29, :76-97), offset
@@ -276,7 +282,10 @@ template <int N, int G, typename T> struct fused_layout {
     static constexpr size_t fit_meta = up(fit_vals + 32 * 81 * sizeof(T), 4);
     static constexpr size_t fit_peak = up(fit_meta + 32 * 4 * sizeof(uint32_t), sizeof(T));
     static constexpr size_t tile = up(fit_peak + 32 * sizeof(T), 128);
-    static constexpr size_t bytes = tile + (size_t)(N / 2) * (N / 2 + 8) * sizeof(uint16_t);
+    static constexpr size_t pair_end = tile + (size_t)(N / 2) * (N / 2 + 8) * sizeof(uint16_t);
+    static constexpr int PPC = fused_pairs_per_cta<N, T>();
+    static constexpr size_t pair_bytes = up(pair_end, 1024);  // one pair's block
+    static constexpr size_t bytes = PPC == 1 ? pair_end : PPC * pair_bytes;
     static_assert(G * (N / G) == N, "group width must divide the transform length");
     // the FP64-input ROI is staged in the spectrum's upper half
     static_assert((size_t)(N / 2) * (N / 2) * sizeof(double) <=
@@ -284,7 +293,7 @@ template <int N, int G, typename T> struct fused_layout {
 };
 
 template <int N, int G, typename T, typename IN>
-__global__ void __launch_bounds__(N * G / 4, fused_min_blocks(N, sizeof(T)))
+__global__ void __launch_bounds__(N * G / 4 * fused_pairs_per_cta<N, T>(), fused_min_blocks(N, sizeof(T)))
     fused_fft_kernel(const fused_args a, const __grid_constant__ CUtensorMap tmap)
 {
     using C = cplx<T>;
@@ -302,31 +311,38 @@ __global__ void __launch_bounds__(N * G / 4, fused_min_blocks(N, sizeof(T)))
     constexpr bool U16 = sizeof(IN) == 2;
 
     using L = fused_layout<N, G, T>;
+    constexpr int PPC = L::PPC;
     extern __shared__ __align__(1024) unsigned char smem[];
-    C *S = reinterpret_cast<C *>(smem + L::spectrum);
-    C *twf = reinterpret_cast<C *>(smem + L::tw_fwd);   // [E][G] forward inter-pass twiddles
-    C *twi = reinterpret_cast<C *>(smem + L::tw_inv);   // [E][G] inverse
-    T *hx = reinterpret_cast<T *>(smem + L::hann);      // hx[H] then hy[H]
+    // this thread's pair of the CTA's PPC and that pair's shared-memory block
+    const int sub = PPC == 1 ? 0 : (int)threadIdx.x / THREADS;
+    unsigned char *base = smem + (size_t)sub * L::pair_bytes;
+    C *S = reinterpret_cast<C *>(base + L::spectrum);
+    C *twf = reinterpret_cast<C *>(base + L::tw_fwd);   // [E][G] forward inter-pass twiddles
+    C *twi = reinterpret_cast<C *>(base + L::tw_inv);   // [E][G] inverse
+    T *hx = reinterpret_cast<T *>(base + L::hann);      // hx[H] then hy[H]
     T *hy = hx + a.side;
     constexpr int DQ = packed_dq<N>();
-    T *dq = reinterpret_cast<T *>(smem + L::dq);         // the row pass's DC and Nyquist outputs
-    T *rs = reinterpret_cast<T *>(smem + L::rsum);       // the reference's row sums (this ROI)
-    T *red_v = reinterpret_cast<T *>(smem + L::red_val);
-    uint32_t *red_i = reinterpret_cast<uint32_t *>(smem + L::red_idx);
-    double *red_s = reinterpret_cast<double *>(smem + L::red_sum);
-    uint64_t *bar = reinterpret_cast<uint64_t *>(smem + L::barrier);
+    T *dq = reinterpret_cast<T *>(base + L::dq);         // the row pass's DC and Nyquist outputs
+    T *rs = reinterpret_cast<T *>(base + L::rsum);       // the reference's row sums (this ROI)
+    T *red_v = reinterpret_cast<T *>(base + L::red_val);
+    uint32_t *red_i = reinterpret_cast<uint32_t *>(base + L::red_idx);
+    double *red_s = reinterpret_cast<double *>(base + L::red_sum);
+    uint64_t *bar = reinterpret_cast<uint64_t *>(base + L::barrier);
     // neighbourhoods of up to 32 pairs wait here for one lane-per-pair fit
-    T *fbuf = reinterpret_cast<T *>(smem + L::fit_vals);            // [32][81]
-    uint32_t *fmeta = reinterpret_cast<uint32_t *>(smem + L::fit_meta);  // [32][4]
-    T *fval = reinterpret_cast<T *>(smem + L::fit_peak);            // [32]
+    T *fbuf = reinterpret_cast<T *>(base + L::fit_vals);            // [32][81]
+    uint32_t *fmeta = reinterpret_cast<uint32_t *>(base + L::fit_meta);  // [32][4]
+    T *fval = reinterpret_cast<T *>(base + L::fit_peak);            // [32]
     // uint16 ROIs: a tile of their own (128-byte aligned), refilled by TMA for
     // the next pair while this pair is in its column and inverse passes.
     // FP64 ROIs: staged in the spectrum's upper half, unused until the columns.
-    uint16_t *t16 = reinterpret_cast<uint16_t *>(smem + L::tile);
+    uint16_t *t16 = reinterpret_cast<uint16_t *>(base + L::tile);
     double *t64 = reinterpret_cast<double *>(S + H * SL);
 
-    const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
+    // thread index within the pair (threads of one pair share no warp with another's)
+    const int tid = PPC == 1 ? (int)threadIdx.x : (int)threadIdx.x % THREADS;
+    const int lane = tid & 31, warp = tid >> 5;
     const int t = lane & (G - 1), g = tid / G;
+    static_assert(THREADS % 32 == 0, "whole warps per pair");
 
     const C *gtw = reinterpret_cast<const C *>(a.twiddles);
     for (int i = tid; i < G * E; i += THREADS) {
@@ -384,8 +400,11 @@ __global__ void __launch_bounds__(N * G / 4, fused_min_blocks(N, sizeof(T)))
         }
         cp_async_arrive(bar);
     };
-    if (tma && tid == 0 && blockIdx.x < a.n_pairs) issue_tile(blockIdx.x);
-    if (cpa && blockIdx.x < a.n_pairs) issue_chunks(blockIdx.x);
+    // the CTA's pairs: PPC consecutive ones per round, rounds gridDim.x * PPC apart
+    const uint32_t stride = gridDim.x * PPC;
+    const uint32_t first = blockIdx.x * PPC + sub;
+    if (tma && tid == 0 && first < a.n_pairs) issue_tile(first);
+    if (cpa && first < a.n_pairs) issue_chunks(first);
 
     // uint16 tiles staged ahead (TMA or cp.async): warps 1..WARPS-1 sum the next
     // pair's tile while warp 0 finishes the current pair, so the next pair
@@ -395,8 +414,13 @@ __global__ void __launch_bounds__(N * G / 4, fused_min_blocks(N, sizeof(T)))
     bool summed = false;  // this pair's tile was summed ahead (uniform over the CTA)
     uint32_t iter = 0;
     // each pair's ROI corner is loaded during the pair before it
-    uint2 beg_next = blockIdx.x < a.n_pairs ? a.begins[item(blockIdx.x).y] : make_uint2(0, 0);
-    for (uint32_t pair = blockIdx.x; pair < a.n_pairs; pair += gridDim.x, ++iter) {
+    uint2 beg_next = first < a.n_pairs ? a.begins[item(first).y] : make_uint2(0, 0);
+    for (uint32_t round0 = blockIdx.x * PPC; round0 < a.n_pairs; round0 += stride, ++iter) {
+        // only the last round can leave some of the CTA's pairs without one:
+        // they run it on a copy of the last pair and write nothing
+        const uint32_t mine = round0 + sub;
+        const bool live = mine < a.n_pairs;
+        const uint32_t pair = live ? mine : a.n_pairs - 1;
         const uint4 it = item(pair);
         const uint32_t pic = it.x, roi = it.y, out = it.z;
         const int s = (int)it.w, s2 = s * s;
@@ -407,7 +431,11 @@ __global__ void __launch_bounds__(N * G / 4, fused_min_blocks(N, sizeof(T)))
         const int xo = U16 ? (int)(beg.x & 7u) : 0;
         if constexpr (U16) {
             if (tma || cpa) {
-                if (!mbar_wait(bar, iter & 1)) {
+                const bool ok = !live || mbar_wait(bar, iter & 1);
+                bool stop = !ok;
+                // the CTA's pairs leave together, so no barrier waits for a pair gone
+                if constexpr (PPC > 1) stop = __syncthreads_or(stop);
+                if (stop) {
                     if (tid == 0) atomicOr(a.err, DEV_ERR_TMA_TIMEOUT);
                     return;
                 }
@@ -511,10 +539,10 @@ __global__ void __launch_bounds__(N * G / 4, fused_min_blocks(N, sizeof(T)))
             rs[N / 2 + tid] = rsum.y;
         }
         __syncthreads();
-        if (pair + gridDim.x < a.n_pairs) beg_next = a.begins[item(pair + gridDim.x).y];
+        if (mine + stride < a.n_pairs) beg_next = a.begins[item(mine + stride).y];
         // the tile is free: fetch the next pair's ROI behind the remaining passes
-        if (tma && tid == 0 && pair + gridDim.x < a.n_pairs) issue_tile(pair + gridDim.x);
-        if (cpa && pair + gridDim.x < a.n_pairs) issue_chunks(pair + gridDim.x);
+        if (tma && tid == 0 && mine + stride < a.n_pairs) issue_tile(mine + stride);
+        if (cpa && mine + stride < a.n_pairs) issue_chunks(mine + stride);
 
         // ---- columns: forward FFT, conj product, inverse FFT --------------
         // Columns 1..N/2-1 by the groups (the last round leaves the last group
@@ -618,7 +646,7 @@ __global__ void __launch_bounds__(N * G / 4, fused_min_blocks(N, sizeof(T)))
         __syncthreads();
 
         // ---- neighbourhood (warp 0); the FP64 fit runs every 32 pairs ----
-        if (warp == 0) {
+        if (warp == 0 && live) {
             T pv = red_v[0];
             uint32_t pk = red_i[0];
             for (int w = 1; w < WARPS; ++w) better(pv, pk, red_v[w], red_i[w]);
@@ -653,10 +681,10 @@ __global__ void __launch_bounds__(N * G / 4, fused_min_blocks(N, sizeof(T)))
                 fval[slot] = 2 * side != N ? pv * ((T)(4 * side * side) / (T)(N * N)) : pv;
             }
             __syncwarp();
-            const bool last = pair + gridDim.x >= a.n_pairs;
+            const bool last = mine + stride >= a.n_pairs;
             if (slot == 31 || last) fit_batch<T>(a, fbuf, fmeta, fval, (int)slot + 1, lane, N - 1);
         }
-        const bool ahead = sum_ahead && pair + gridDim.x < a.n_pairs;
+        const bool ahead = sum_ahead && mine + stride < a.n_pairs;
         if (ahead && warp != 0) {
             // the next tile was requested after this pair's row pass: wait for it
             // and sum it over the other warps' threads
@@ -1070,7 +1098,8 @@ static cudaError_t launch_one(const fused_args &a, const CUtensorMap *tmap, int 
                               cudaStream_t st)
 {
     auto k = fused_fft_kernel<N, G, T, IN>;
-    constexpr int threads = N * G / 4;
+    constexpr int ppc = fused_layout<N, G, T>::PPC;
+    constexpr int threads = N * G / 4 * ppc;
     const size_t smem = fused_layout<N, G, T>::bytes;
     cudaError_t e = cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
     if (e != cudaSuccess) return e;
@@ -1084,7 +1113,8 @@ static cudaError_t launch_one(const fused_args &a, const CUtensorMap *tmap, int 
         grid += per_sm * sms;  // less the CTAs left free
         if (grid < 1) grid = 1;
     }
-    if ((uint32_t)grid > a.n_pairs) grid = (int)a.n_pairs;
+    const uint32_t rounds = (a.n_pairs + ppc - 1) / ppc;  // CTAs with a pair to start on
+    if ((uint32_t)grid > rounds) grid = (int)rounds;
     if (grid < 1) return cudaSuccess;
     k<<<grid, threads, smem, st>>>(a, *tmap);
     return cudaGetLastError();
