@@ -220,15 +220,17 @@ __device__ __forceinline__ void packed_column(const Slot0 &slot0, const T *dq, c
 // as many): FP32 128-point and 192-point transforms are register-heavy; the
 // FP32 64-point kernel (8 values per lane) fits 80 registers, so 6 CTAs of 4
 // warps share an SM (65 M pairs/s at side 32, against 52 M with 4).
-__host__ __device__ constexpr int fused_min_blocks(int N, int tsize)
+__host__ __device__ constexpr int fused_min_blocks(int N, int tsize, int ppc = 1)
 {
-    return N == 192 || (N == 96 && tsize == 4) ? 1 : N == 128 ? (tsize == 4 ? 2 : 1) : N == 64 && tsize == 4 ? 6 : (tsize == 4 ? 4 : 2);
+    return N == 96 && tsize == 4 ? 4 / ppc
+           : N == 192 ? 1 : N == 128 ? (tsize == 4 ? 2 : 1) : N == 64 && tsize == 4 ? 6 : (tsize == 4 ? 4 : 2);
 }
 // Pairs one CTA carries side by side.  The FP32 96-point kernel's 3-warp
 // pairs ran 4 CTAs per SM, each in its own pass of the loop, and their
 // instruction working set outgrew the instruction cache; 4 pairs per CTA
 // keep the SM's warps in the same pass.  Each pair has its own shared-memory
-// block, barrier and warps; the CTA's barriers are common.
+// block, barrier and warps; the CTA's barriers are common.  That kernel is
+// also built with 1 and 2 pairs per CTA, for the multi-layout autotuner.
 template <int N, typename T> constexpr int fused_pairs_per_cta() { return N == 96 && sizeof(T) == 4 ? 4 : 1; }
 
 // Lane l fits buffered pair l: coefficients as sequential FP64 dot products
@@ -265,7 +267,7 @@ __device__ __forceinline__ void fit_batch(const fused_args &a, const T *fbuf, co
 
 // Shared-memory layout of the fused kernel, in bytes from the (1024-aligned)
 // dynamic base.  The kernel and the launcher's size both come from here.
-template <int N, int G, typename T> struct fused_layout {
+template <int N, int G, typename T, int PPC_ = fused_pairs_per_cta<N, T>()> struct fused_layout {
     using C = cplx<T>;
     static constexpr size_t up(size_t v, size_t a) { return (v + a - 1) / a * a; }
     static constexpr size_t spectrum = 0;                                  // N x N/2 C
@@ -283,7 +285,7 @@ template <int N, int G, typename T> struct fused_layout {
     static constexpr size_t fit_peak = up(fit_meta + 32 * 4 * sizeof(uint32_t), sizeof(T));
     static constexpr size_t tile = up(fit_peak + 32 * sizeof(T), 128);
     static constexpr size_t pair_end = tile + (size_t)(N / 2) * (N / 2 + 8) * sizeof(uint16_t);
-    static constexpr int PPC = fused_pairs_per_cta<N, T>();
+    static constexpr int PPC = PPC_;
     static constexpr size_t pair_bytes = up(pair_end, 1024);  // one pair's block
     static constexpr size_t bytes = PPC == 1 ? pair_end : PPC * pair_bytes;
     static_assert(G * (N / G) == N, "group width must divide the transform length");
@@ -292,8 +294,8 @@ template <int N, int G, typename T> struct fused_layout {
                       (size_t)(N / 2) * (N / 2) * sizeof(C), "FP64 tile must fit");
 };
 
-template <int N, int G, typename T, typename IN>
-__global__ void __launch_bounds__(N * G / 4 * fused_pairs_per_cta<N, T>(), fused_min_blocks(N, sizeof(T)))
+template <int N, int G, typename T, typename IN, int PPC_>
+__global__ void __launch_bounds__(N * G / 4 * PPC_, fused_min_blocks(N, sizeof(T), PPC_))
     fused_fft_kernel(const fused_args a, const __grid_constant__ CUtensorMap tmap)
 {
     using C = cplx<T>;
@@ -310,7 +312,7 @@ __global__ void __launch_bounds__(N * G / 4 * fused_pairs_per_cta<N, T>(), fused
     const int TW = (side + 14) & ~7;
     constexpr bool U16 = sizeof(IN) == 2;
 
-    using L = fused_layout<N, G, T>;
+    using L = fused_layout<N, G, T, PPC_>;
     constexpr int PPC = L::PPC;
     extern __shared__ __align__(1024) unsigned char smem[];
     // this thread's pair of the CTA's PPC and that pair's shared-memory block
@@ -1093,14 +1095,14 @@ static cudaError_t launch_cluster(const fused_args &a, const CUtensorMap *tmap, 
     return cudaGetLastError();
 }
 
-template <int N, int G, typename T, typename IN>
+template <int N, int G, typename T, typename IN, int PPC = fused_pairs_per_cta<N, T>()>
 static cudaError_t launch_one(const fused_args &a, const CUtensorMap *tmap, int grid,
                               cudaStream_t st)
 {
-    auto k = fused_fft_kernel<N, G, T, IN>;
-    constexpr int ppc = fused_layout<N, G, T>::PPC;
+    auto k = fused_fft_kernel<N, G, T, IN, PPC>;
+    constexpr int ppc = PPC;
     constexpr int threads = N * G / 4 * ppc;
-    const size_t smem = fused_layout<N, G, T>::bytes;
+    const size_t smem = fused_layout<N, G, T, PPC>::bytes;
     cudaError_t e = cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
     if (e != cudaSuccess) return e;
     if (grid <= 0) {
@@ -1167,8 +1169,13 @@ static cudaError_t launch_n(bool dbl, bool in_f64, const fused_args &a, const CU
     if (dbl)
         return in_f64 ? launch_one<N, G, double, double>(a, tmap, grid, st)
                       : launch_one<N, G, double, uint16_t>(a, tmap, grid, st);
-    return in_f64 ? launch_one<N, G, float, double>(a, tmap, grid, st)
-                  : launch_one<N, G, float, uint16_t>(a, tmap, grid, st);
+    if (in_f64) return launch_one<N, G, float, double>(a, tmap, grid, st);
+    if constexpr (N == 96) {
+        // the autotuner's other tile shapes: 1 or 2 pairs per CTA
+        if (a.pairs_per_cta == 1) return launch_one<N, G, float, uint16_t, 1>(a, tmap, grid, st);
+        if (a.pairs_per_cta == 2) return launch_one<N, G, float, uint16_t, 2>(a, tmap, grid, st);
+    }
+    return launch_one<N, G, float, uint16_t>(a, tmap, grid, st);
 }
 
 cudaError_t launch_fused(uint32_t fft_n, bool dbl, bool in_f64, const fused_args &a,

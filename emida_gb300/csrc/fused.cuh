@@ -45,6 +45,9 @@ struct fused_args {
     // Optional table of pattern base pointers: the pattern of item/pair p is
     // pattern_ptrs[pattern index] instead of pics + index * src_w * src_h.
     const void *const *pattern_ptrs;
+    // ROI pairs per CTA: 0 for the length's default; the FP32 96-point kernel
+    // with uint16 input also takes 1 or 2 (its default is 4)
+    uint32_t pairs_per_cta;
 };
 
 // Offset of the s x s table inside lstsq_all (6*9, 6*25, 6*49, 6*81 doubles).

@@ -34,6 +34,7 @@ struct emida_gb_multi {
         size_t spec_cap = 0;     // in ROIs
         const void *hann = nullptr, *twiddles = nullptr;  // owned by the class's first layout
         int grid = 0;  // 0: one wave of resident CTAs (less `reserve`)
+        uint32_t ppc = 0;  // ROI pairs per CTA (0: the kernel's default)
     };
     // CTA slots a default (one-wave) launch leaves free for kernels that run
     // beside it, such as the request loop's SM copies of the next rows
@@ -303,6 +304,7 @@ int launch_plan(emida_gb_multi *m, const plan &pl, const work_set &ws, const voi
         a.err = m->d_err;
         a.items = ws.d_items[c];
         a.pattern_ptrs = table ? ws.d_ptrs : nullptr;
+        a.pairs_per_cta = k.ppc;
         a.stage = STAGE_PLAIN;
         if (use_tma) {
             const uint32_t side = k.side;
@@ -691,7 +693,7 @@ int emida_gb_multi_autotune(emida_gb_multi *m, const void *dev_patterns, uint32_
         const uint32_t n0 = k.n;
         float best = 1e30f;
         int best_grid = 0;
-        uint32_t best_n = n0;
+        uint32_t best_n = n0, best_ppc = 0;
         std::string tried;
         std::vector<emida_gb_handle *> alt;  // the other length's handles, one per member
         for (uint32_t n : lens) {
@@ -702,25 +704,38 @@ int emida_gb_multi_autotune(emida_gb_multi *m, const void *dev_patterns, uint32_
                 st = install_class_spectra(m, c, members, {}, n0);  // the members' own length again
             }
             if (st != EMIDA_GB_OK) break;
-            float nbest = 1e30f;
-            int ngrid = 0;
-            for (int per_sm = 1; per_sm <= 6 && st == EMIDA_GB_OK; ++per_sm) {
-                float ms = 0;
-                st = time_grid(c, per_sm * sms, ms);
-                if (st == EMIDA_GB_OK && ms < nbest * 0.98f) {
-                    nbest = ms;
-                    ngrid = per_sm * sms;
+            // tile shapes of this length: pairs per CTA (the FP32 96-point
+            // kernel is built with 4, its default, 2 and 1)
+            std::vector<uint32_t> ppcs = {0};
+            if (n == 96 && !m->dbl) ppcs = {0, 2, 1};
+            for (uint32_t ppc : ppcs) {
+                k.ppc = ppc;
+                float nbest = 1e30f;
+                int ngrid = 0;
+                for (int per_sm = 1; per_sm <= 6 && st == EMIDA_GB_OK; ++per_sm) {
+                    float ms = 0;
+                    st = time_grid(c, per_sm * sms, ms);
+                    if (st == EMIDA_GB_OK && ms < nbest * 0.98f) {
+                        nbest = ms;
+                        ngrid = per_sm * sms;
+                    }
+                }
+                if (st != EMIDA_GB_OK) break;
+                char t[64];
+                if (ppc)
+                    snprintf(t, sizeof t, "%sn=%u/%u per CTA %.3f ms", tried.empty() ? "" : ", ", n, ppc, nbest);
+                else
+                    snprintf(t, sizeof t, "%sn=%u %.3f ms", tried.empty() ? "" : ", ", n, nbest);
+                tried += t;
+                if (nbest < best * 0.98f) {
+                    best = nbest;
+                    best_grid = ngrid;
+                    best_n = n;
+                    best_ppc = ppc;
                 }
             }
+            k.ppc = 0;
             if (st != EMIDA_GB_OK) break;
-            char t[48];
-            snprintf(t, sizeof t, "%sn=%u %.3f ms", tried.empty() ? "" : ", ", n, nbest);
-            tried += t;
-            if (nbest < best * 0.98f) {
-                best = nbest;
-                best_grid = ngrid;
-                best_n = n;
-            }
         }
         // keep the winning length's spectra and handles
         std::vector<emida_gb_handle *> orig;
@@ -735,9 +750,12 @@ int emida_gb_multi_autotune(emida_gb_multi *m, const void *dev_patterns, uint32_
         for (emida_gb_handle *h : alt) emida_gb_destroy(h);
         if (st != EMIDA_GB_OK) break;
         k.grid = best_grid;
+        k.ppc = best_ppc;
         char line[256];
-        snprintf(line, sizeof line, "side %u (n=%u): %zu pairs, grid %d (%d per SM), %.3f ms [%s]\n", k.side,
-                 k.n, pl.items[c].size(), best_grid, best_grid / std::max(1, sms), best, tried.c_str());
+        const uint32_t shown_ppc = k.ppc ? k.ppc : (k.n == 96 && !m->dbl ? 4u : 1u);
+        snprintf(line, sizeof line, "side %u (n=%u): %zu pairs, grid %d (%d per SM), %u pair%s per CTA, %.3f ms [%s]\n",
+                 k.side, k.n, pl.items[c].size(), best_grid, best_grid / std::max(1, sms), shown_ppc,
+                 shown_ppc == 1 ? "" : "s", best, tried.c_str());
         rep += line;
     }
     cudaEventDestroy(a);

@@ -133,8 +133,11 @@ def test_multi_autotune_and_errors(scene):
 def test_autotune_transform_lengths_keep_parity():
     """Zero-padded ROI sides have two fused transform lengths to choose from
     (side 24: 64 or 96 points, side 40: 96 or 128, side 56: 128 or 192); the
-    autotuner times both with 1..6 CTAs per SM, keeps the faster, and the
-    results stay the oracle's whichever length it kept."""
+    autotuner times both with 1..6 CTAs per SM (and the 96-point kernel with
+    4, 2 and 1 pairs per CTA), keeps the fastest, and the results stay the
+    oracle's whichever shape it kept.  Every timed candidate writes the whole
+    class's offsets, so right after tuning they are the last candidate's, which
+    must be the oracle's too."""
     from emida_gb300 import DeviceBuffer, MultiLayout, synth
     from tests.test_gpu_synthetic import well_posed
     from oracle import oracle as eo
@@ -157,6 +160,9 @@ def test_autotune_transform_lengths_keep_parity():
     assert len(lines) == 3
     for line, (a, b) in zip(lines, [(64, 96), (96, 128), (128, 192)]):
         assert f"n={a} " in line and f"n={b} " in line, line
+        if 96 in (a, b):
+            assert "n=96/2 per CTA" in line and "n=96/1 per CTA" in line, line
+    tuned = d_offs.download(np.float64, (total, 2))
     m.run(d_pics, layout_of, d_offs, d_coefs, d_max, graph=False)
     m.synchronize()
     offs = d_offs.download(np.float64, (total, 2))
@@ -171,4 +177,5 @@ def test_autotune_transform_lengths_keep_parity():
         assert np.array_equal(peaks[sl], k), (p, side)
         ok = well_posed(c, s)
         assert (np.abs(offs[sl] - o)[ok] <= 1e-3).all(), (p, side)
+        assert (np.abs(tuned[sl] - o)[ok] <= 1e-3).all(), (p, side)
         start += len(b)
