@@ -252,10 +252,12 @@ void *emida_gb_multi_stream(emida_gb_multi *m);
 int emida_gb_multi_synchronize(emida_gb_multi *m);
 /* Per ROI size class with a fused kernel, times on these patterns each
  * candidate transform length (the smallest that holds the ROI and the next
- * one, which zero-pads it further) with grids of 1..6 times the SM count
- * (clusters of two CTAs at 256 points), keeps the fastest length and grid,
- * rebuilds the class's resident reference spectra at that length, and writes
- * a one-line-per-class report. */
+ * one, which zero-pads it further), each tile shape of that length's kernel
+ * (ROI pairs per CTA: 4, 2 or 1 for the FP32 96-point kernel, 1 elsewhere),
+ * with grids of 1..6 times the SM count (clusters of two CTAs at 256
+ * points); keeps the fastest length, shape and grid, rebuilds the class's
+ * resident reference spectra at that length, and writes a one-line-per-class
+ * report. */
 int emida_gb_multi_autotune(emida_gb_multi *m, const void *dev_patterns, uint32_t patterns,
                             const uint32_t *layout_of, double *dev_offsets, char *report,
                             size_t report_len);
