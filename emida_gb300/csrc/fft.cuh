@@ -207,9 +207,14 @@ template <int DIR, typename C> struct rdft<3, DIR, C> {
 // through `line`), then pass 2: E/G G-point DFTs over t.  The exchange slot of
 // A'[t][k1] is G*k1 + ((t + k1) mod G): the G lanes' writes (fixed k1) and reads
 // (fixed t) fall in G different rows or slots.
-// tw: this direction's inter-pass twiddles laid out [k1][lane],
-// tw[G*k1 + t] = W_N^{t*k1}.  mask: the lanes of the warp's groups that run
-// this transform together (whole groups; every lane named must call it).
+// tw: this direction's inter-pass twiddles laid out [lane][k1] with the row
+// stride tw_stride, tw[t * TS + k1] = W_N^{t*k1}.  FP32 rows hold an even
+// number of slots, so that two twiddles arrive in one 16-byte load, and the
+// strides keep the G rows a group reads in distinct banks.  mask: the lanes of
+// the warp's groups that run this transform together (whole groups; every
+// lane named must call it).
+template <int N, int G, typename C> constexpr int tw_stride() { return N / G + (sizeof(C) == 8 ? 2 : 1); }
+
 template <int N, int DIR, bool HALF_INPUT, typename T, int G, typename Line>
 __device__ __forceinline__ void group_fft(cplx<T> *v, int t, const Line &line,
                                           const cplx<T> *__restrict__ tw,
@@ -222,8 +227,20 @@ __device__ __forceinline__ void group_fft(cplx<T> *v, int t, const Line &line,
         rdft<E, DIR, C>::run_half(v);
     else
         rdft<E, DIR, C>::run(v);
+    constexpr int TS = tw_stride<N, G, C>();
+    const C *twt = tw + t * TS;
+    if constexpr (sizeof(C) == 8) {
+        static_assert(E % 2 == 0, "twiddles come in pairs");
 #pragma unroll
-    for (int k1 = 1; k1 < E; ++k1) v[k1] = cmul(v[k1], tw[G * k1 + t]);
+        for (int k1 = 0; k1 < E; k1 += 2) {
+            const float4 w = *reinterpret_cast<const float4 *>(twt + k1);
+            if (k1 > 0) v[k1] = cmul(v[k1], cmake<C>(w.x, w.y));
+            v[k1 + 1] = cmul(v[k1 + 1], cmake<C>(w.z, w.w));
+        }
+    } else {
+#pragma unroll
+        for (int k1 = 1; k1 < E; ++k1) v[k1] = cmul(v[k1], twt[k1]);
+    }
     __syncwarp(mask);
 #pragma unroll
     for (int k1 = 0; k1 < E; ++k1) *line(G * k1 + ((t + k1) & (G - 1))) = v[k1];

@@ -272,8 +272,9 @@ template <int N, int G, typename T, int PPC_ = fused_pairs_per_cta<N, T>()> stru
     static constexpr size_t up(size_t v, size_t a) { return (v + a - 1) / a * a; }
     static constexpr size_t spectrum = 0;                                  // N x N/2 C
     static constexpr size_t tw_fwd = spectrum + (size_t)N * (N / 2) * sizeof(C);
-    static constexpr size_t tw_inv = tw_fwd + (size_t)N * sizeof(C);      // G*E = N entries
-    static constexpr size_t hann = tw_inv + (size_t)N * sizeof(C);
+    static constexpr size_t tw_bytes = (size_t)G * tw_stride<N, G, C>() * sizeof(C);  // [G][TS]
+    static constexpr size_t tw_inv = tw_fwd + tw_bytes;
+    static constexpr size_t hann = tw_inv + tw_bytes;
     static constexpr size_t dq = hann + (size_t)N * sizeof(T);            // hx, hy
     static constexpr size_t rsum = dq + (size_t)packed_dq<N>() * sizeof(C);  // DC, Nyquist
     static constexpr size_t red_val = rsum + (size_t)(N / 2) * sizeof(C); // reference row sums
@@ -286,7 +287,7 @@ template <int N, int G, typename T, int PPC_ = fused_pairs_per_cta<N, T>()> stru
     static constexpr size_t tile = up(fit_peak + 32 * sizeof(T), 128);
     static constexpr size_t pair_end = tile + (size_t)(N / 2) * (N / 2 + 8) * sizeof(uint16_t);
     static constexpr int PPC = PPC_;
-    static constexpr size_t pair_bytes = up(pair_end, 1024);  // one pair's block
+    static constexpr size_t pair_bytes = up(pair_end, 128);  // one pair's block
     static constexpr size_t bytes = PPC == 1 ? pair_end : PPC * pair_bytes;
     static_assert(G * (N / G) == N, "group width must divide the transform length");
     // the FP64-input ROI is staged in the spectrum's upper half
@@ -319,8 +320,8 @@ __global__ void __launch_bounds__(N * G / 4 * PPC_, fused_min_blocks(N, sizeof(T
     const int sub = PPC == 1 ? 0 : (int)threadIdx.x / THREADS;
     unsigned char *base = smem + (size_t)sub * L::pair_bytes;
     C *S = reinterpret_cast<C *>(base + L::spectrum);
-    C *twf = reinterpret_cast<C *>(base + L::tw_fwd);   // [E][G] forward inter-pass twiddles
-    C *twi = reinterpret_cast<C *>(base + L::tw_inv);   // [E][G] inverse
+    C *twf = reinterpret_cast<C *>(base + L::tw_fwd);   // [G][TS] forward inter-pass twiddles
+    C *twi = reinterpret_cast<C *>(base + L::tw_inv);   // [G][TS] inverse
     T *hx = reinterpret_cast<T *>(base + L::hann);      // hx[H] then hy[H]
     T *hy = hx + a.side;
     constexpr int DQ = packed_dq<N>();
@@ -347,8 +348,10 @@ __global__ void __launch_bounds__(N * G / 4 * PPC_, fused_min_blocks(N, sizeof(T
     static_assert(THREADS % 32 == 0, "whole warps per pair");
 
     const C *gtw = reinterpret_cast<const C *>(a.twiddles);
-    for (int i = tid; i < G * E; i += THREADS) {
-        const C w = gtw[(i % G) * (i / G)];  // W_N^{t k1}, t = i mod G, k1 = i / G
+    constexpr int TS = tw_stride<N, G, C>();
+    for (int i = tid; i < G * TS; i += THREADS) {
+        const int k1 = i % TS;  // W_N^{t k1}, t = i / TS (the row's padding is zero)
+        const C w = k1 < E ? gtw[(i / TS) * k1] : cmake<C>((T)0, (T)0);
         twf[i] = w;
         twi[i] = cconj(w);
     }
@@ -742,8 +745,9 @@ struct layout {
     static constexpr size_t spectrum = 0;                               // N x SLOTS float2
     static constexpr size_t xch = spectrum + (size_t)N * SLOTS * 8;     // GROUPS x N float2
     static constexpr size_t tw_fwd = xch + (size_t)GROUPS * N * 8;
-    static constexpr size_t tw_inv = tw_fwd + (size_t)N * 8;
-    static constexpr size_t hann = tw_inv + (size_t)N * 8;              // hx[side], hy[side]
+    static constexpr size_t tw_bytes = (size_t)G * tw_stride<N, G, float2>() * 8;  // [G][TS]
+    static constexpr size_t tw_inv = tw_fwd + tw_bytes;
+    static constexpr size_t hann = tw_inv + tw_bytes;                   // hx[side], hy[side]
     static constexpr size_t dq = hann + (size_t)N * 4;                  // DC, Nyquist lines
     static constexpr size_t rsum = dq + (size_t)2 * packed_dq<N>() * 4;  // reference row sums
     static constexpr size_t red_val = rsum + (size_t)N * 4;
@@ -812,8 +816,10 @@ __global__ void __cluster_dims__(2, 1, 1) __launch_bounds__(cl::THREADS, 1)
     auto owner = [&](int k) -> C * { return (k >> 6) == rank ? S : Sp; };
 
     const C *gtw = reinterpret_cast<const C *>(a.twiddles);
-    for (int i = tid; i < G * E; i += THREADS) {
-        const C w = gtw[(i % G) * (i / G)];
+    constexpr int TS = tw_stride<N, G, C>();
+    for (int i = tid; i < G * TS; i += THREADS) {
+        const int k1 = i % TS;
+        const C w = k1 < E ? gtw[(i / TS) * k1] : cmake<C>((T)0, (T)0);
         twf[i] = w;
         twi[i] = cconj(w);
     }
