@@ -52,6 +52,15 @@ __device__ __forceinline__ C *sp(C *S, int row, int slot)
     return S + row * (N / 2) + (slot ^ f);
 }
 
+// The correlation map replaces the spectrum: map rows 2p and 2p + 1 at column x
+// are one complex slot, (map[2p][x], map[2p + 1][x]), in spectrum rows 2p
+// (x < N/2) and 2p + 1 (x >= N/2): one 8- or 16-byte store per lane and
+// column instead of two.
+template <int N, typename C> __device__ __forceinline__ C *map_pair(C *S, int row2, int x)
+{
+    return x >= N / 2 ? sp<N>(S, row2 + 1, x - N / 2) : sp<N>(S, row2, x);
+}
+
 template <int N, typename C> struct col_line {
     C *S;
     int c;
@@ -618,23 +627,20 @@ __global__ void __launch_bounds__(N * G / 4 * PPC_, fused_min_blocks(N, sizeof(T
             row_line<N, C> line{S, ra};
             group_fft<N, +1, false, T, G>(v, t, line, twi);
 #pragma unroll
-            for (int j = 0; j < E; ++j) {
-                const int x = t + G * j;
-                reinterpret_cast<T *>(sp<N>(S, ra, x >> 1))[x & 1] = v[j].x;
+            for (int j = 0; j < E; ++j) *map_pair<N>(S, ra, t + G * j) = v[j];
+            // map indices in increasing order: row ra, then row rb
+#pragma unroll
+            for (int j = 0; j < E; ++j)
                 if (v[j].x > bv) {
                     bv = v[j].x;
-                    bi = (uint32_t)(ra * N + x);
+                    bi = (uint32_t)(ra * N + t + G * j);
                 }
-            }
 #pragma unroll
-            for (int j = 0; j < E; ++j) {
-                const int x = t + G * j;
-                reinterpret_cast<T *>(sp<N>(S, rb, x >> 1))[x & 1] = v[j].y;
+            for (int j = 0; j < E; ++j)
                 if (v[j].y > bv) {
                     bv = v[j].y;
-                    bi = (uint32_t)(rb * N + x);
+                    bi = (uint32_t)(rb * N + t + G * j);
                 }
-            }
         }
 
         // ---- argmax over the N x N map (maxarg.cu, first maximum) ---------
@@ -664,7 +670,7 @@ __global__ void __launch_bounds__(N * G / 4 * PPC_, fused_min_blocks(N, sizeof(T
                 neighbour_pos(mx, my, l % s, l / s, s, N - 1, N - 1, x, y);
                 const uint32_t q = (uint32_t)policy_index(POLICY_FFT, x, y, N - 1, N - 1);
                 const uint32_t qy = q / N, qx = q % N;
-                T val = reinterpret_cast<T *>(sp<N>(S, qy, qx >> 1))[qx & 1];
+                T val = reinterpret_cast<const T *>(map_pair<N>(S, (int)(qy & ~1u), (int)qx))[qy & 1];
                 // an unnormalised inverse of length N scales values by N^2:
                 // report them at the reference's (2*side)^2
                 if (2 * side != N) val *= (T)(4 * side * side) / (T)(N * N);
