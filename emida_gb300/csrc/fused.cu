@@ -725,7 +725,8 @@ __global__ void __launch_bounds__(N * G / 4 * PPC_, fused_min_blocks(N, sizeof(T
 //   column pass   local: forward FFT, conj product, inverse FFT of its 64 columns;
 //   inverse rows  CTA r produces map rows 128r..128r+127, reading the partner's
 //                 64 slots of each row; the real map goes back over the same
-//                 slots (map columns x < 128 in CTA 0, x >= 128 in CTA 1);
+//                 two rows, map rows (2p, 2p+1) at column x as one slot: slot
+//                 x mod 128 of row 2p (x < 128) or 2p+1, in its owner CTA;
 //   peak, fit     CTA 0 merges both maxima, reads the neighbourhood from either
 //                 CTA and runs the batched FP64 fit.
 // Every thread of both CTAs passes the same cluster barriers in every pair and
@@ -1005,24 +1006,26 @@ __global__ void __cluster_dims__(2, 1, 1) __launch_bounds__(cl::THREADS, 1)
                 }
             }
             group_fft<N, +1, false, T, G>(v, t, xl, twi);
+            // map rows ra and rb at column x as one slot: slot x mod 128 of
+            // spectrum row ra (x < 128) or rb, in the CTA that owns that slot
 #pragma unroll
             for (int j = 0; j < E; ++j) {
-                const int x = t + G * j, q = x >> 1;
-                reinterpret_cast<T *>(csp(owner(q), ra, q & 63))[x & 1] = v[j].x;
+                const int x = t + G * j, q = x & (H - 1);
+                *csp(owner(q), ra + (x >= H), q & 63) = v[j];
+            }
+            // map indices in increasing order: row ra, then row rb
+#pragma unroll
+            for (int j = 0; j < E; ++j)
                 if (v[j].x > bv) {
                     bv = v[j].x;
-                    bi = (uint32_t)(ra * N + x);
+                    bi = (uint32_t)(ra * N + t + G * j);
                 }
-            }
 #pragma unroll
-            for (int j = 0; j < E; ++j) {
-                const int x = t + G * j, q = x >> 1;
-                reinterpret_cast<T *>(csp(owner(q), rb, q & 63))[x & 1] = v[j].y;
+            for (int j = 0; j < E; ++j)
                 if (v[j].y > bv) {
                     bv = v[j].y;
-                    bi = (uint32_t)(rb * N + x);
+                    bi = (uint32_t)(rb * N + t + G * j);
                 }
-            }
         }
 #pragma unroll
         for (int o = 16; o; o >>= 1) {
@@ -1059,8 +1062,8 @@ __global__ void __cluster_dims__(2, 1, 1) __launch_bounds__(cl::THREADS, 1)
                 uint32_t x, y;
                 neighbour_pos(mx, my, l % s, l / s, s, N - 1, N - 1, x, y);
                 const uint32_t qm = (uint32_t)policy_index(POLICY_FFT, x, y, N - 1, N - 1);
-                const int qy = (int)(qm / N), qx = (int)(qm % N), q = qx >> 1;
-                T val = reinterpret_cast<T *>(csp(owner(q), qy, q & 63))[qx & 1];
+                const int qy = (int)(qm / N), qx = (int)(qm % N), q = qx & (H - 1);
+                T val = reinterpret_cast<const T *>(csp(owner(q), (qy & ~1) + (qx >= H), q & 63))[qy & 1];
                 if (2 * side != N) val *= scale;
                 fbuf[slot * 81 + l] = val;
                 if (a.neigh) reinterpret_cast<T *>(a.neigh)[(size_t)out * s2 + l] = val;
