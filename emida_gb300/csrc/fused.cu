@@ -61,6 +61,15 @@ template <int N, typename C> __device__ __forceinline__ C *map_pair(C *S, int ro
     return x >= N / 2 ? sp<N>(S, row2 + 1, x - N / 2) : sp<N>(S, row2, x);
 }
 
+// Rows 2p and 2p+1 differ in one swizzle bit (every length but 96), so for the
+// slots t + 8j a lane touches in both rows, the second row's address is the
+// first's plus a per-lane constant: (slot ^ f(2p) ^ d) - (slot ^ f(2p)) is +-d
+// by bit d of slot ^ f(2p), and that bit does not depend on j.
+template <int N, typename C> __device__ __forceinline__ ptrdiff_t pair_row_delta(C *S, int row2, int slot)
+{
+    return sp<N>(S, row2 + 1, slot) - sp<N>(S, row2, slot);
+}
+
 template <int N, typename C> struct col_line {
     C *S;
     int c;
@@ -543,8 +552,10 @@ __global__ void __launch_bounds__(N * G / 4 * PPC_, fused_min_blocks(N, sizeof(T
                     dq[rb] = dq[N + rb] = z.y;
                     dq[DQ + rb] = dq[DQ + N + rb] = zh.y;
                 } else {
-                    *sp<N>(S, ra, k) = cmake<C>((z.x + zm.x) * (T)0.5, (z.y - zm.y) * (T)0.5);
-                    *sp<N>(S, rb, k) = cmake<C>((z.y + zm.y) * (T)0.5, (zm.x - z.x) * (T)0.5);
+                    C *pa = sp<N>(S, ra, k);
+                    C *pb = N == 96 ? sp<N>(S, rb, k) : pa + pair_row_delta<N>(S, ra, t);
+                    *pa = cmake<C>((z.x + zm.x) * (T)0.5, (z.y - zm.y) * (T)0.5);
+                    *pb = cmake<C>((z.y + zm.y) * (T)0.5, (zm.x - z.x) * (T)0.5);
                 }
             }
         }
@@ -611,16 +622,20 @@ __global__ void __launch_bounds__(N * G / 4 * PPC_, fused_min_blocks(N, sizeof(T
 #pragma unroll 1
         for (int rnd = 0; rnd < (N / 2) / GROUPS; ++rnd) {
             const int ra = 2 * (g + rnd * GROUPS), rb = ra + 1;
+            // row rb's slots t + G j and (N - t - G j) mod N as row ra's plus a constant
+            const ptrdiff_t dn = pair_row_delta<N>(S, ra, t), dk = pair_row_delta<N>(S, ra, (N - t) % SL);
             C v[E];
 #pragma unroll
             for (int j = 0; j < E; ++j) {
                 const int n = t + G * j;
                 if (j < E / 2) {
-                    C ga = *sp<N>(S, ra, n), gb = *sp<N>(S, rb, n);
+                    const C *pa = sp<N>(S, ra, n);
+                    const C ga = *pa, gb = N == 96 ? *sp<N>(S, rb, n) : pa[dn];
                     v[j] = (n == 0) ? cmake<C>(ga.x, gb.x) : cmake<C>(ga.x - gb.y, ga.y + gb.x);
                 } else {
                     const int k = (n == H) ? 0 : N - n;
-                    C ga = *sp<N>(S, ra, k), gb = *sp<N>(S, rb, k);
+                    const C *pa = sp<N>(S, ra, k);
+                    const C ga = *pa, gb = N == 96 ? *sp<N>(S, rb, k) : pa[dk];
                     v[j] = (n == H) ? cmake<C>(ga.y, gb.y) : cmake<C>(ga.x + gb.y, gb.x - ga.y);
                 }
             }
