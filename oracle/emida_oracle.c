@@ -1,7 +1,7 @@
 /*
  * emida_oracle.c -- CPU FP64 restatement of emida's ROI cross-correlation path.
  *
- * TEST INFRASTRUCTURE ONLY (the checker).  Only tests/, smoke() and bench.py's
+ * TEST INFRASTRUCTURE ONLY (the oracle).  Only tests/, smoke() and bench.py's
  * CPU-baseline / reference arm may load this library; the product never does.
  *
  * Each function cites the reference file:line whose behaviour it restates.

@@ -1,7 +1,7 @@
 /*
  * emida_oracle.h -- CPU FP64 restatement of emida's ROI cross-correlation path.
  *
- * TEST INFRASTRUCTURE ONLY.  This library is the checker: only tests/, the
+ * TEST INFRASTRUCTURE ONLY.  This library is the oracle: only tests/, the
  * smoke() entry point and bench.py's CPU-baseline / reference arm may load it.
  * The product (libemida_gb.so) never links or calls it.
  *

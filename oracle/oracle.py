@@ -1,6 +1,6 @@
 """ctypes front end of the CPU FP64 oracle (oracle/_build/libemida_oracle.so).
 
-TEST INFRASTRUCTURE ONLY: the checker.  Only tests/, __graft_entry__.smoke()
+TEST INFRASTRUCTURE ONLY: the oracle.  Only tests/, __graft_entry__.smoke()
 and bench.py's CPU-baseline / reference arm import this module.  It builds the
 library with `make -C oracle oracle` on first use when it is missing.
 
