@@ -375,16 +375,21 @@ def run_batching(args):
     """4096 patterns of 1024^2 on 32 seeded layouts (radius 16..64, 25-400 ROIs,
     fit size 3..9): one multi-layout run per step, replayed from a CUDA graph,
     grids autotuned per ROI size."""
-    import time
     import __graft_entry__
     __graft_entry__.build_library()
+    print(json.dumps(batching_measure(args.precision, args.steps, args.warmup)), flush=True)
+
+
+def batching_measure(precision, steps, warmup):
+    """The batching workload of run_batching; returns its JSON object."""
+    import time
     from emida_gb300 import DeviceBuffer, MultiLayout, _lib, synth
     from oracle import oracle as eo
     P, L = 4096, 32
     ref = synth.reference_pattern(1024, 77)
     uniq, _ = synth.deformed_patterns(1024, 77, L, sigma_eps=5e-3)
     layouts = random_layouts(1024, L, 77, [16, 24, 32, 48, 64], (25, 400))
-    m = MultiLayout((1024, 1024), args.precision)
+    m = MultiLayout((1024, 1024), precision)
     for begins, side, fs in layouts:
         m.add_layout(begins, side, fs, ref)
     layout_of = np.arange(P, dtype=np.uint32) % L
@@ -421,29 +426,30 @@ def run_batching(args):
     rms = float(np.sqrt(sum(r[3] for r in res) / max(1, sum(r[4] for r in res))))
     peak_match = sum(r[5] for r in res) / sum(r[2] for r in res)
     assert err <= 1e-2, f"offset error {err} px"
-    for _ in range(args.warmup):
+    for _ in range(warmup):
         m.run(d_pics, layout_of, d_offs, d_coefs, graph=True)
     m.synchronize()
     with ClockSampler(0) as clk:
         t0 = time.perf_counter()
-        for _ in range(args.steps):
+        for _ in range(steps):
             m.run(d_pics, layout_of, d_offs, d_coefs, graph=True)
         m.synchronize()
-        dt = (time.perf_counter() - t0) / args.steps
+        dt = (time.perf_counter() - t0) / steps
     radii = sorted({l[1] // 2 for l in layouts})
-    print(json.dumps({
+    out = {
         "metric": "ROI pairs/s, patterns on uneven ROI layouts (one graph-replayed multi-layout run)",
-        "value": total / dt, "unit": "ROI pairs/s", "n_gpus": 1, "steps": args.steps,
-        "warmup": args.warmup, "ms_per_step": dt * 1000, "higher_is_better": True,
-        "dtype": "f32" if args.precision == "float" else "f64", "data": "synthetic",
+        "value": total / dt, "unit": "ROI pairs/s", "n_gpus": 1, "steps": steps,
+        "warmup": warmup, "ms_per_step": dt * 1000, "higher_is_better": True,
+        "dtype": "f32" if precision == "float" else "f64", "data": "synthetic",
         "config": {"workload": f"{P} x 1024^2 uint16 patterns on {L} seeded layouts, radius "
                                f"{radii}, 25-400 ROIs, fit 3-9", "patterns": P, "pairs": int(total)},
         "autotune": report.strip().splitlines(),
         "parity": {"max_abs_err_px": err, "rms_err_px": rms, "peak_match_rate": peak_match,
                    "well_posed_fits": sum(r[1] for r in res), "checked_pairs": sum(r[2] for r in res),
                    "vs": "FP64 oracle, one pattern per layout"},
-        "clocks": clk.summary()}), flush=True)
+        "clocks": clk.summary()}
     m.close()
+    return out
 
 
 def run_serving(args):
@@ -1115,6 +1121,9 @@ def main():
             legs["fp64"] = fp64_leg(ref, pics, begins, d_pics, max(5, args.steps // 5), args.warmup)
             legs["tensor"] = tensor_leg(ref, pics, begins, d_pics, max(5, args.steps // 5), args.warmup)
             legs["serving"] = serving_measure("float", "detector", 100.0, 4.0, 128, False)
+            bm = batching_measure("float", 5, args.warmup)
+            legs["batching"] = {k: bm[k] for k in ("metric", "value", "unit", "ms_per_step", "config",
+                                                  "autotune", "parity", "clocks")}
 
     cpu = port = None
     if rank == 0 and world == 1:
