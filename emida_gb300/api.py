@@ -418,6 +418,10 @@ class MultiLayout:
         _lib.call("emida_gb_multi_synchronize", self._h)
 
     def autotune(self, dev_pics, layout_of, dev_offsets):
+        """emida_gb_multi_autotune: per ROI size class, times the candidate
+        transform lengths, the tile shapes of each (ROI pairs per CTA) and
+        grids of 1..6 CTAs per SM on these patterns, keeps the fastest, and
+        returns the one-line-per-class report."""
         lo = np.ascontiguousarray(layout_of, dtype=np.uint32)
         buf = ctypes.create_string_buffer(4096)
         _lib.call("emida_gb_multi_autotune", self._h, dev_pics.ptr, len(lo),
