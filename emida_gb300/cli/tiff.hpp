@@ -127,14 +127,20 @@ public:
         }
         const uint64_t total = (uint64_t)info.width * info.height * 2;
         uint64_t at = 0;
-        for (size_t s = 0; s < info.strip_offsets.size() && at < total; ++s) {
-            uint64_t n = info.strip_bytes[s];
+        // strips that follow each other in the file are read with one call
+        for (size_t s = 0; s < info.strip_offsets.size() && at < total;) {
+            const uint64_t off = info.strip_offsets[s];
+            uint64_t n = 0;
+            size_t e = s;
+            while (e < info.strip_offsets.size() && at + n < total && info.strip_offsets[e] == off + n)
+                n += info.strip_bytes[e++];
             if (at + n > total) n = total - at;
-            if (!rd(info.strip_offsets[s], (unsigned char *)raster + at, (size_t)n)) {
+            if (!rd(off, (unsigned char *)raster + at, (size_t)n)) {
                 err = "truncated strip data";
                 return false;
             }
             at += n;
+            s = e;
         }
         if (at != total) {
             err = "strip data shorter than the image";
