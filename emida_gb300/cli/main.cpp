@@ -17,6 +17,7 @@
 #include <condition_variable>
 #include <cstdio>
 #include <fstream>
+#include <future>
 #include <iostream>
 #include <limits>
 #include <map>
@@ -438,17 +439,53 @@ int process(const params &a)
         }
     });
     // finalize stage (src/process_files.hpp:219-264)
+    // One pattern's lines: "%f %f %llu %s\n", then per ROI "%lu %lu %f %f"
+    // (+ 6 x " %f" with -q).
+    auto pattern_text = [&](const offsets_t<double> &r, esize_t first, esize_t j, std::string &text) {
+        using emida_cli::put_f;
+        using emida_cli::put_u;
+        put_f(text, work[j].x);
+        text += ' ';
+        put_f(text, work[j].y);
+        text += ' ';
+        put_u(text, (unsigned long long)S);
+        text += ' ';
+        text += work[j].fname;
+        text += '\n';
+        const esize_t it = j - first;
+        for (esize_t i = it * S; i < (it + 1) * S; ++i) {
+            const esize_t bi = i % S;
+            double ox = r.offsets[i].x, oy = r.offsets[i].y;
+            if (std::isnan(ox)) ox = std::numeric_limits<double>::quiet_NaN();
+            if (std::isnan(oy)) oy = std::numeric_limits<double>::quiet_NaN();
+            put_u(text, (unsigned long)a.mids[bi].x);
+            text += ' ';
+            put_u(text, (unsigned long)a.mids[bi].y);
+            text += ' ';
+            put_f(text, ox);
+            text += ' ';
+            put_f(text, oy);
+            if (a.write_coefs)
+                for (int k = 0; k < 6; ++k) {
+                    text += ' ';
+                    put_f(text, r.coefs[i][k]);
+                }
+            text += '\n';
+        }
+    };
+    // a batch's text is formatted in up to TEXT_PARTS ranges of its patterns
+    // at once (three helper threads and this one), then written in order
+    constexpr esize_t TEXT_PARTS = 4;
     std::thread fin([&]() {
-        std::string text;  // one batch's lines, written at once
+        std::vector<std::string> parts(TEXT_PARTS);
         for (esize_t b = 0; b < n_batches; ++b) {
             stopwatch fsw;
             auto f = done.pop();
             fsw.tick("Finalize wait");
             if (f->files == 0) continue;  // a batch that failed to load is skipped
             auto r = offs.finalize(f->maxes.data(), f->neigh.data());
-            text.reserve((size_t)f->files * S * (a.write_coefs ? 120 : 40));
-            for (esize_t j = f->first; j < f->first + f->files; ++j) {
-                if (bin) {
+            if (bin) {
+                for (esize_t j = f->first; j < f->first + f->files; ++j) {
                     // the same content, unrounded: pattern header, then one record per ROI
                     const uint32_t n = (uint32_t)S, len = (uint32_t)work[j].fname.size();
                     fwrite(&work[j].x, sizeof(double), 1, bin);
@@ -464,42 +501,24 @@ int process(const params &a)
                         fwrite(o, sizeof o, 1, bin);
                         fwrite(r.coefs[i].data(), sizeof(double), 6, bin);
                     }
-                    continue;
                 }
-                // "%f %f %llu %s\n", then per ROI "%lu %lu %f %f" (+ 6 x " %f" with -q)
-                using emida_cli::put_f;
-                using emida_cli::put_u;
-                put_f(text, work[j].x);
-                text += ' ';
-                put_f(text, work[j].y);
-                text += ' ';
-                put_u(text, (unsigned long long)S);
-                text += ' ';
-                text += work[j].fname;
-                text += '\n';
-                const esize_t it = j - f->first;
-                for (esize_t i = it * S; i < (it + 1) * S; ++i) {
-                    const esize_t bi = i % S;
-                    double ox = r.offsets[i].x, oy = r.offsets[i].y;
-                    if (std::isnan(ox)) ox = std::numeric_limits<double>::quiet_NaN();
-                    if (std::isnan(oy)) oy = std::numeric_limits<double>::quiet_NaN();
-                    put_u(text, (unsigned long)a.mids[bi].x);
-                    text += ' ';
-                    put_u(text, (unsigned long)a.mids[bi].y);
-                    text += ' ';
-                    put_f(text, ox);
-                    text += ' ';
-                    put_f(text, oy);
-                    if (a.write_coefs)
-                        for (int k = 0; k < 6; ++k) {
-                            text += ' ';
-                            put_f(text, r.coefs[i][k]);
-                        }
-                    text += '\n';
-                }
+                fsw.tick("Finalize");
+                continue;
             }
-            if (!text.empty()) fwrite(text.data(), 1, text.size(), stdout);
-            text.clear();
+            const esize_t nparts = std::min<esize_t>(TEXT_PARTS, f->files);
+            auto format = [&](esize_t p) {
+                const esize_t j0 = f->first + f->files * p / nparts;
+                const esize_t j1 = f->first + f->files * (p + 1) / nparts;
+                parts[p].clear();
+                parts[p].reserve((size_t)(j1 - j0) * S * (a.write_coefs ? 120 : 40));
+                for (esize_t j = j0; j < j1; ++j) pattern_text(r, f->first, j, parts[p]);
+            };
+            std::vector<std::future<void>> helpers;
+            for (esize_t p = 1; p < nparts; ++p) helpers.push_back(std::async(std::launch::async, format, p));
+            format(0);
+            for (auto &h : helpers) h.get();
+            for (esize_t p = 0; p < nparts; ++p)
+                if (!parts[p].empty()) fwrite(parts[p].data(), 1, parts[p].size(), stdout);
             fsw.tick("Finalize");
         }
     });
