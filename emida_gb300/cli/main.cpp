@@ -384,6 +384,27 @@ int process(const params &a)
     std::condition_variable order_cv;
     esize_t next_to_submit = 0;
 
+    // The rows that hold ROI pixels, merged into ascending bands: the path
+    // copies and reads nothing else of a pattern, so the loaders read only
+    // these (unless they cover nearly all of it).
+    std::vector<std::pair<uint32_t, uint32_t>> bands;
+    {
+        std::vector<std::pair<uint32_t, uint32_t>> iv;
+        for (const auto &b : a.begins)
+            iv.push_back({(uint32_t)b.y, (uint32_t)std::min<size_t>(a.pic_size.y, b.y + a.slice_size.y)});
+        std::sort(iv.begin(), iv.end());
+        uint64_t covered = 0;
+        for (const auto &r : iv) {
+            if (!bands.empty() && r.first <= bands.back().first + bands.back().second) {
+                const uint32_t end = std::max(bands.back().first + bands.back().second, r.second);
+                bands.back().second = end - bands.back().first;
+            } else if (r.second > r.first) {
+                bands.push_back({r.first, r.second - r.first});
+            }
+        }
+        for (const auto &bd : bands) covered += bd.second;
+        if (covered * 10 >= (uint64_t)a.pic_size.y * 9) bands.clear();  // read whole patterns
+    }
     // loaders (src/process_files.hpp:98-133): batches are submitted in order
     auto loader = [&]() {
         esize_t bi;
@@ -395,8 +416,12 @@ int process(const params &a)
             bool ok = true;
             for (esize_t i = 0; i < files; ++i) {
                 std::string e;
-                if (!emida_cli::load_tiff(work[first + i].fname, buf + i * area, a.pic_size.x,
-                                          a.pic_size.y, e)) {
+                const bool got = bands.empty()
+                                     ? emida_cli::load_tiff(work[first + i].fname, buf + i * area, a.pic_size.x,
+                                                            a.pic_size.y, e)
+                                     : emida_cli::load_tiff_rows(work[first + i].fname, buf + i * area,
+                                                                 a.pic_size.x, a.pic_size.y, bands, e);
+                if (!got) {
                     std::cerr << e << "\n";
                     ok = false;
                 }

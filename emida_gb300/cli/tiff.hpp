@@ -4,6 +4,7 @@
 // pixels are swapped to host order.
 #pragma once
 
+#include <algorithm>
 #include <cstdint>
 #include <cstdio>
 #include <cstring>
@@ -150,6 +151,61 @@ public:
             for (uint64_t i = 0; i < total / 2; ++i) raster[i] = (uint16_t)((raster[i] >> 8) | (raster[i] << 8));
         return true;
     }
+
+    // Reads only the rows of `bands` ((first row, rows) pairs, ascending and
+    // disjoint) into raster (width*height uint16), with one read per run of
+    // strips that follow each other in the file; the other rows of raster are
+    // left as they are.
+    bool read_rows(const tiff_info &info, uint16_t *raster,
+                   const std::vector<std::pair<uint32_t, uint32_t>> &bands, std::string &err)
+    {
+        if (info.bits != 16 || info.samples != 1 || info.compression != 1) {
+            err = "only uncompressed 16-bit single-channel TIFF is supported";
+            return false;
+        }
+        if (info.orientation != 1) {
+            err = "only able to process row 0 TOP, col 0 LEFT orientation";
+            return false;
+        }
+        const size_t ns = info.strip_offsets.size();
+        if (ns != info.strip_bytes.size()) {
+            err = "inconsistent strip tables";
+            return false;
+        }
+        const uint64_t row = (uint64_t)info.width * 2, total = row * info.height;
+        std::vector<uint64_t> start(ns + 1, 0);  // raster byte of each strip
+        for (size_t s = 0; s < ns; ++s) start[s + 1] = start[s] + info.strip_bytes[s];
+        if (start[ns] < total) {
+            err = "strip data shorter than the image";
+            return false;
+        }
+        size_t s = 0;
+        for (const auto &bd : bands) {
+            uint64_t lo = (uint64_t)bd.first * row;
+            const uint64_t hi = std::min<uint64_t>(total, (uint64_t)(bd.first + bd.second) * row);
+            while (lo < hi) {
+                while (s < ns && start[s + 1] <= lo) ++s;  // the strip that holds byte lo
+                if (s == ns) {
+                    err = "truncated strip data";
+                    return false;
+                }
+                size_t e = s;
+                while (start[e + 1] < hi && e + 1 < ns &&
+                       info.strip_offsets[e + 1] == info.strip_offsets[e] + info.strip_bytes[e])
+                    ++e;
+                const uint64_t end = std::min(hi, start[e + 1]);
+                if (!rd(info.strip_offsets[s] + (lo - start[s]), (unsigned char *)raster + lo, (size_t)(end - lo))) {
+                    err = "truncated strip data";
+                    return false;
+                }
+                if (be_)
+                    for (uint64_t i = lo / 2; i < end / 2; ++i)
+                        raster[i] = (uint16_t)((raster[i] >> 8) | (raster[i] << 8));
+                lo = end;
+            }
+        }
+        return true;
+    }
 };
 
 // src/load_tiff.hpp:55-69 get_size
@@ -176,6 +232,22 @@ inline bool load_tiff(const std::string &name, uint16_t *raster, uint32_t w, uin
         return false;
     }
     return t.read(info, raster, err);
+}
+
+// load_tiff for the rows of `bands` only (ascending, disjoint (first, rows)
+// pairs): the rows that hold ROI pixels, which are all the path reads.
+inline bool load_tiff_rows(const std::string &name, uint16_t *raster, uint32_t w, uint32_t h,
+                           const std::vector<std::pair<uint32_t, uint32_t>> &bands, std::string &err)
+{
+    tiff_file t;
+    tiff_info info;
+    if (!t.open(name, info, err)) return false;
+    if (info.width != w || info.height != h) {
+        err = "The size of " + name + " is different than specified size " + std::to_string(w) +
+              "," + std::to_string(h);
+        return false;
+    }
+    return t.read_rows(info, raster, bands, err);
 }
 
 // Writes an uncompressed little-endian 16-bit grayscale TIFF with one strip.

@@ -74,3 +74,25 @@ def test_reader_rejects_a_truncated_fixture(driver, tmp_path):
     r = subprocess.run([driver, str(tif), str(tmp_path / "o.bin")], capture_output=True, text=True,
                        timeout=60)
     assert r.returncode == 1 and r.stderr.strip()
+
+
+def test_reader_reads_only_the_requested_row_bands(driver, tmp_path):
+    """load_tiff_rows, as the command line's loaders call it with the ROI row
+    bands: bands that start and end inside the 4-row strips and one that
+    reaches the last row; every other row is left untouched."""
+    raw = gzip.open(FIXTURE).read()
+    w, h, exp, _ = parse_tiff(raw)
+    tif = tmp_path / "INITIAL_x0y0.tif"
+    tif.write_bytes(raw)
+    out = tmp_path / "rows.bin"
+    bands = [(3, 10), (100, 37), (400, 1), (860, 13)]
+    r = subprocess.run([driver, str(tif), str(out)] + [f"{a}:{n}" for a, n in bands],
+                       capture_output=True, text=True, timeout=60)
+    assert r.returncode == 0, r.stderr
+    got = np.fromfile(out, dtype=np.uint8)
+    pixels = np.frombuffer(got[8:].tobytes(), dtype=np.uint16).reshape(h, w)
+    inside = np.zeros(h, dtype=bool)
+    for a, n in bands:
+        inside[a:a + n] = True
+    assert np.array_equal(pixels[inside], exp[inside])
+    assert (pixels[~inside] == 0xFFFF).all()
