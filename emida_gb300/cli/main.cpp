@@ -499,8 +499,8 @@ int process(const params &a)
         }
     };
     // a batch's text is formatted in up to TEXT_PARTS ranges of its patterns
-    // at once (three helper threads and this one), then written in order
-    constexpr esize_t TEXT_PARTS = 4;
+    // at once (seven helper threads and this one), then written in order
+    constexpr esize_t TEXT_PARTS = 8;
     std::thread fin([&]() {
         std::vector<std::string> parts(TEXT_PARTS);
         for (esize_t b = 0; b < n_batches; ++b) {
