@@ -123,3 +123,20 @@ def test_long_copied_row_equals_its_patterns_alone(world):
         sl = slice(30 * n * k, 30 * n * (k + 1))
         assert np.array_equal(offs[sl], alone_offs) and np.array_equal(coefs[sl], alone_coefs)
     s.close()
+
+
+def test_trace_records_every_row_in_order_of_its_stages(world):
+    """emida_gb_server_trace: one record per completed row with its pattern
+    count, and times from submission that do not decrease from admission to
+    first step launch, last step launch and completion."""
+    sizes, layouts, rows = world
+    s = make_server(sizes, layouts, budget_patterns=16, step=6)
+    ids = [s.submit(lid, pics) for lid, pics in rows]
+    for rid in ids:
+        s.wait(rid)
+    tr = s.trace()
+    s.close()
+    assert tr.shape == (len(rows), 5)
+    assert sorted(tr[:, 0].astype(int).tolist()) == sorted(len(p) for _, p in rows)
+    assert (tr[:, 1] >= 0).all()
+    assert (np.diff(tr[:, 1:], axis=1) >= 0).all()
