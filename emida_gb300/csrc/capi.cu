@@ -267,6 +267,8 @@ int emida_gb::host::run_fused(emida_gb_handle *h, const void *pics, uint32_t pat
     a.maxes = maxes;
     a.neigh = neigh;
     a.err = err ? err : h->d_err;
+    // the handle's own compute streams order their launches: a queue each
+    a.pair_queue = st == h->comp ? h->d_queues : (h->comp_alt && st == h->comp_alt) ? h->d_queues + 2 : nullptr;
     CUtensorMap map;
     std::memset(&map, 0, sizeof map);
     a.stage = STAGE_PLAIN;
@@ -701,6 +703,7 @@ int emida_gb::host::create_handle(const emida_gb_params *p, uint32_t fused_len, 
     const size_t sum_elem = h->in_f64 ? 8 : 4;
     TRY(h->alloc(&h->d_sums_ref, sum_elem * h->S));
     TRY(h->alloc((void **)&h->d_err, sizeof(uint32_t), true));
+    TRY(h->alloc((void **)&h->d_queues, 4 * sizeof(uint32_t), true));
     h->lstsq.resize(6 * (size_t)p->fitsize * p->fitsize);
     lstsq_matrix(p->fitsize, h->lstsq.data());
     TRY(h->alloc((void **)&h->d_lstsq, h->lstsq.size() * sizeof(double)));

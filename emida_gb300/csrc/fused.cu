@@ -298,7 +298,9 @@ template <int N, int G, typename T, int PPC_ = fused_pairs_per_cta<N, T>()> stru
     static constexpr size_t red_val = rsum + (size_t)(N / 2) * sizeof(C); // reference row sums
     static constexpr size_t red_idx = red_val + 32 * sizeof(T);
     static constexpr size_t red_sum = up(red_idx + 32 * sizeof(uint32_t), 8);
+    // the tile's mbarrier, then (first pair's block) the round the pair queue handed out
     static constexpr size_t barrier = red_sum + 32 * sizeof(double);
+    static constexpr size_t next_pair = barrier + 8;
     static constexpr size_t fit_vals = barrier + 16;
     static constexpr size_t fit_meta = up(fit_vals + 32 * 81 * sizeof(T), 4);
     static constexpr size_t fit_peak = up(fit_meta + 32 * 4 * sizeof(uint32_t), sizeof(T));
@@ -349,6 +351,8 @@ __global__ void __launch_bounds__(N * G / 4 * PPC_, fused_min_blocks(N, sizeof(T
     uint32_t *red_i = reinterpret_cast<uint32_t *>(base + L::red_idx);
     double *red_s = reinterpret_cast<double *>(base + L::red_sum);
     uint64_t *bar = reinterpret_cast<uint64_t *>(base + L::barrier);
+    // the round the pair queue handed out, in the first pair's block
+    uint32_t *next_s = reinterpret_cast<uint32_t *>((PPC == 1 ? base : smem) + L::next_pair);
     // neighbourhoods of up to 32 pairs wait here for one lane-per-pair fit
     T *fbuf = reinterpret_cast<T *>(base + L::fit_vals);            // [32][81]
     uint32_t *fmeta = reinterpret_cast<uint32_t *>(base + L::fit_meta);  // [32][4]
@@ -423,8 +427,12 @@ __global__ void __launch_bounds__(N * G / 4 * PPC_, fused_min_blocks(N, sizeof(T
         }
         cp_async_arrive(bar);
     };
-    // the CTA's pairs: PPC consecutive ones per round, rounds gridDim.x * PPC apart
+    // the CTA's pairs: PPC consecutive ones per round, rounds gridDim.x * PPC
+    // apart; with a pair queue, the first round blockIdx.x and then whichever
+    // round the queue hands out (the queue counts rounds of PPC pairs)
     const uint32_t stride = gridDim.x * PPC;
+    uint32_t *const queue = a.pair_queue;
+    const bool lead = sub == 0 && tid == 0;  // the CTA's thread 0: it talks to the queue
     const uint32_t first = blockIdx.x * PPC + sub;
     if (tma && tid == 0 && first < a.n_pairs) issue_tile(first);
     if (cpa && first < a.n_pairs) issue_chunks(first);
@@ -438,7 +446,10 @@ __global__ void __launch_bounds__(N * G / 4 * PPC_, fused_min_blocks(N, sizeof(T
     uint32_t iter = 0;
     // each pair's ROI corner is loaded during the pair before it
     uint2 beg_next = first < a.n_pairs ? a.begins[item(first).y] : make_uint2(0, 0);
-    for (uint32_t round0 = blockIdx.x * PPC; round0 < a.n_pairs; round0 += stride, ++iter) {
+    for (uint32_t round0 = blockIdx.x * PPC, nround = 0; round0 < a.n_pairs; round0 = nround, ++iter) {
+        // the queue's answer is needed after the row pass, which hides its latency
+        uint32_t fetched = 0;
+        if (queue && lead) fetched = (atomicAdd(queue, 1u) + gridDim.x) * PPC;
         // only the last round can leave some of the CTA's pairs without one:
         // they run it on a copy of the last pair and write nothing
         const uint32_t mine = round0 + sub;
@@ -460,7 +471,7 @@ __global__ void __launch_bounds__(N * G / 4 * PPC_, fused_min_blocks(N, sizeof(T
                 if constexpr (PPC > 1) stop = __syncthreads_or(stop);
                 if (stop) {
                     if (tid == 0) atomicOr(a.err, DEV_ERR_TMA_TIMEOUT);
-                    return;
+                    break;  // to the queue's count of CTAs done
                 }
             } else {
                 const uint16_t *src = reinterpret_cast<const uint16_t *>(pattern_base(pic)) +
@@ -563,11 +574,23 @@ __global__ void __launch_bounds__(N * G / 4 * PPC_, fused_min_blocks(N, sizeof(T
             rs[tid] = rsum.x;
             rs[N / 2 + tid] = rsum.y;
         }
+        if (queue && lead) *next_s = fetched;
         __syncthreads();
-        if (mine + stride < a.n_pairs) beg_next = a.begins[item(mine + stride).y];
+        // this CTA's next round, and this pair's successor in it (past n_pairs
+        // when there is none); the one-pair form keeps the expressions that
+        // compiled fastest for the 128-point kernel
+        uint32_t nxt;
+        if constexpr (PPC == 1) {
+            nxt = queue ? *next_s : mine + stride;
+            nround = queue ? nxt : round0 + stride;
+        } else {
+            nround = queue ? *next_s : round0 + stride;
+            nxt = nround + sub;
+        }
+        if (nxt < a.n_pairs) beg_next = a.begins[item(nxt).y];
         // the tile is free: fetch the next pair's ROI behind the remaining passes
-        if (tma && tid == 0 && mine + stride < a.n_pairs) issue_tile(mine + stride);
-        if (cpa && mine + stride < a.n_pairs) issue_chunks(mine + stride);
+        if (tma && tid == 0 && nxt < a.n_pairs) issue_tile(nxt);
+        if (cpa && nxt < a.n_pairs) issue_chunks(nxt);
 
         // ---- columns: forward FFT, conj product, inverse FFT --------------
         // Columns 1..N/2-1 by the groups (the last round leaves the last group
@@ -707,10 +730,10 @@ __global__ void __launch_bounds__(N * G / 4 * PPC_, fused_min_blocks(N, sizeof(T
                 fval[slot] = 2 * side != N ? pv * ((T)(4 * side * side) / (T)(N * N)) : pv;
             }
             __syncwarp();
-            const bool last = mine + stride >= a.n_pairs;
+            const bool last = nxt >= a.n_pairs;
             if (slot == 31 || last) fit_batch<T>(a, fbuf, fmeta, fval, (int)slot + 1, lane, N - 1);
         }
-        const bool ahead = sum_ahead && mine + stride < a.n_pairs;
+        const bool ahead = sum_ahead && nxt < a.n_pairs;
         if (ahead && warp != 0) {
             // the next tile was requested after this pair's row pass: wait for it
             // and sum it over the other warps' threads
@@ -726,6 +749,15 @@ __global__ void __launch_bounds__(N * G / 4 * PPC_, fused_min_blocks(N, sizeof(T
         }
         summed = ahead;
         __syncthreads();
+    }
+    if (queue && lead) {
+        // every CTA has taken its last round from the queue before it counts
+        // itself done, so the last one can zero the queue for the next launch
+        __threadfence();
+        if (atomicAdd(queue + 1, 1u) == gridDim.x - 1) {
+            atomicExch(queue, 0u);
+            atomicExch(queue + 1, 0u);
+        }
     }
 }
 
@@ -1142,11 +1174,12 @@ static cudaError_t launch_one(const fused_args &a, const CUtensorMap *tmap, int 
         e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k, threads, smem);
         if (e != cudaSuccess) return e;
         if (per_sm < 1) per_sm = 1;
-        // The FP32 128-point kernel holds 2 pairs per SM; three waves of CTAs
-        // (each with a third of the pairs) end more evenly than one when every
-        // CTA still gets 16 pairs or more (25,600 pairs: 1.206 against 1.225 ms).
-        // Launches that leave CTA slots free (grid < 0) keep one wave.
-        const int waves = grid == 0 && N == 128 && sizeof(T) == 4 &&
+        // The FP32 128-point kernel holds 2 pairs per SM; without a pair queue,
+        // three waves of CTAs (each with a third of the pairs) end more evenly
+        // than one when every CTA still gets 16 pairs or more (25,600 pairs:
+        // 1.206 against 1.225 ms).  With a queue one wave ends more evenly still
+        // (1.166 ms).  Launches that leave CTA slots free (grid < 0) keep one wave.
+        const int waves = grid == 0 && !a.pair_queue && N == 128 && sizeof(T) == 4 &&
                                   a.n_pairs >= 3u * 16u * (uint32_t)(per_sm * sms)
                               ? 3
                               : 1;

@@ -48,6 +48,14 @@ struct fused_args {
     // ROI pairs per CTA: 0 for the length's default; the FP32 96-point kernel
     // with uint16 input also takes 1 or 2 (its default is 4)
     uint32_t pairs_per_cta;
+    // Optional pair queue of the one-CTA kernels (every length but the
+    // cluster's): two device words, zero at launch (the next round of pairs
+    // past the first wave, the CTAs done).  CTA b starts on round b (pairs
+    // b PPC .. b PPC + PPC - 1) and takes each further round from the queue,
+    // so CTAs on faster SMs take more pairs and the launch ends evenly; its
+    // last CTA zeroes both words.  Launches that share a queue must be
+    // stream-ordered.  Null: CTA b walks rounds b, b + grid, b + 2 grid, ...
+    uint32_t *pair_queue;
 };
 
 // Offset of the s x s table inside lstsq_all (6*9, 6*25, 6*49, 6*81 doubles).

@@ -151,6 +151,10 @@ struct emida_gb_handle {
     double *d_offsets = nullptr, *d_coefs = nullptr, *d_lstsq = nullptr;
     void *d_tw_row = nullptr, *d_tw_col = nullptr;
     uint32_t *d_err = nullptr;
+    // The fused kernel's pair queues (two words each, zero between launches):
+    // one for launches on comp, one for comp_alt.  Launches on other streams
+    // walk their pairs statically, as two of them could overlap on one queue.
+    uint32_t *d_queues = nullptr;
     std::vector<double> lstsq;
     bool ref_set = false;
     // How submit brings pinned host batches to the kernels (EMIDA_GB_INGEST_*).

@@ -70,6 +70,9 @@ struct emida_gb_multi {
     std::vector<size_class> classes;
     double *d_lstsq_all = nullptr;
     uint32_t *d_err = nullptr;
+    // the fused kernels' pair queue (two words, zero between launches): every
+    // class launch runs on `stream`, so one queue serves them all
+    uint32_t *d_queue = nullptr;
     cudaStream_t stream = nullptr;
     // graph cache: the last captured run and what it was captured for
     cudaGraphExec_t gexec = nullptr;
@@ -305,6 +308,7 @@ int launch_plan(emida_gb_multi *m, const plan &pl, const work_set &ws, const voi
         a.items = ws.d_items[c];
         a.pattern_ptrs = table ? ws.d_ptrs : nullptr;
         a.pairs_per_cta = k.ppc;
+        a.pair_queue = m->d_queue;
         a.stage = STAGE_PLAIN;
         if (use_tma) {
             const uint32_t side = k.side;
@@ -474,6 +478,8 @@ int emida_gb_multi_create(uint32_t src_w, uint32_t src_h, int32_t precision, emi
     CK(cudaMemcpy(m->d_lstsq_all, all.data(), all.size() * sizeof(double), cudaMemcpyHostToDevice));
     CK(cudaMalloc((void **)&m->d_err, sizeof(uint32_t)));
     CK(cudaMemset(m->d_err, 0, sizeof(uint32_t)));
+    CK(cudaMalloc((void **)&m->d_queue, 2 * sizeof(uint32_t)));
+    CK(cudaMemset(m->d_queue, 0, 2 * sizeof(uint32_t)));
     *out = m.release();
     return EMIDA_GB_OK;
 }
@@ -790,6 +796,7 @@ void emida_gb_multi_destroy(emida_gb_multi *m)
     for (auto &L : m->layouts) emida_gb_destroy(L.h);
     if (m->d_lstsq_all) cudaFree(m->d_lstsq_all);
     if (m->d_err) cudaFree(m->d_err);
+    if (m->d_queue) cudaFree(m->d_queue);
     if (m->stream) cudaStreamDestroy(m->stream);
     delete m;
 }
