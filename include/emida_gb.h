@@ -130,7 +130,9 @@ int emida_gb_wait(emida_gb_handle *h, uint64_t ticket, double *offsets, double *
  * all on `stream`
  * (NULL: the handle's compute stream), no synchronisation.  Pageable host
  * memory is refused (EMIDA_GB_INVALID_ARGUMENT).  coefs, maxes, neigh may be
- * NULL. */
+ * NULL.  On the handle's compute stream the fused kernels hand out their
+ * pairs through a device queue (faster SMs take more); on another stream each
+ * CTA walks a fixed set of pairs.  The results are the same bits. */
 int emida_gb_run_device(emida_gb_handle *h, const void *dev_patterns, uint32_t patterns,
                         double *dev_offsets, double *dev_coefs, void *dev_maxes,
                         void *dev_neigh, void *stream);
