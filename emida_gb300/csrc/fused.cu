@@ -1242,9 +1242,12 @@ static cudaError_t launch_n(bool dbl, bool in_f64, const fused_args &a, const CU
                       : launch_one<N, G, double, uint16_t>(a, tmap, grid, st);
     if (in_f64) return launch_one<N, G, float, double>(a, tmap, grid, st);
     if constexpr (N == 96) {
-        // the autotuner's other tile shapes: 1 or 2 pairs per CTA
+        // 1, 2 or 4 pairs per CTA.  The default is 2 with a pair queue (two
+        // CTAs per SM; side 48: 33.0 against 32.4 M pairs/s with 4) and 4
+        // without one, where a single CTA per SM ends a fixed walk more evenly
         if (a.pairs_per_cta == 1) return launch_one<N, G, float, uint16_t, 1>(a, tmap, grid, st);
-        if (a.pairs_per_cta == 2) return launch_one<N, G, float, uint16_t, 2>(a, tmap, grid, st);
+        if (a.pairs_per_cta == 2 || (a.pairs_per_cta == 0 && a.pair_queue))
+            return launch_one<N, G, float, uint16_t, 2>(a, tmap, grid, st);
     }
     return launch_one<N, G, float, uint16_t>(a, tmap, grid, st);
 }

@@ -46,7 +46,7 @@ struct fused_args {
     // pattern_ptrs[pattern index] instead of pics + index * src_w * src_h.
     const void *const *pattern_ptrs;
     // ROI pairs per CTA: 0 for the length's default; the FP32 96-point kernel
-    // with uint16 input also takes 1 or 2 (its default is 4)
+    // with uint16 input takes 1, 2 or 4 (default: 2 with a pair queue, else 4)
     uint32_t pairs_per_cta;
     // Optional pair queue of the one-CTA kernels (every length but the
     // cluster's): two device words, zero at launch (the next round of pairs

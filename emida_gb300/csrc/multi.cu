@@ -711,9 +711,9 @@ int emida_gb_multi_autotune(emida_gb_multi *m, const void *dev_patterns, uint32_
             }
             if (st != EMIDA_GB_OK) break;
             // tile shapes of this length: pairs per CTA (the FP32 96-point
-            // kernel is built with 4, its default, 2 and 1)
+            // kernel is built with 4, 2 and 1)
             std::vector<uint32_t> ppcs = {0};
-            if (n == 96 && !m->dbl) ppcs = {0, 2, 1};
+            if (n == 96 && !m->dbl) ppcs = {4, 2, 1};
             for (uint32_t ppc : ppcs) {
                 k.ppc = ppc;
                 float nbest = 1e30f;
@@ -758,7 +758,8 @@ int emida_gb_multi_autotune(emida_gb_multi *m, const void *dev_patterns, uint32_
         k.grid = best_grid;
         k.ppc = best_ppc;
         char line[256];
-        const uint32_t shown_ppc = k.ppc ? k.ppc : (k.n == 96 && !m->dbl ? 4u : 1u);
+        // the default with the runner's pair queue: 2 at 96 points (FP32), else 1
+        const uint32_t shown_ppc = k.ppc ? k.ppc : (k.n == 96 && !m->dbl ? 2u : 1u);
         snprintf(line, sizeof line, "side %u (n=%u): %zu pairs, grid %d (%d per SM), %u pair%s per CTA, %.3f ms [%s]\n",
                  k.side, k.n, pl.items[c].size(), best_grid, best_grid / std::max(1, sms), shown_ppc,
                  shown_ppc == 1 ? "" : "s", best, tried.c_str());
