@@ -809,7 +809,7 @@ struct layout {
     static constexpr size_t psum = red_idx + 32 * 4;                    // partial sums [2]
     static constexpr size_t pbest_v = psum + 16;                        // CTA maxima [2]
     static constexpr size_t pbest_i = pbest_v + 16;
-    static constexpr size_t barrier = pbest_i + 16;
+    static constexpr size_t barrier = pbest_i + 16;                     // mbarrier, next pair
     static constexpr size_t fit_vals = barrier + 16;
     static constexpr size_t fit_meta = fit_vals + 32 * 81 * 4;
     static constexpr size_t fit_peak = fit_meta + 32 * 4 * 4;
@@ -853,6 +853,11 @@ __global__ void __cluster_dims__(2, 1, 1) __launch_bounds__(cl::THREADS, 1)
     T *pbest_v = reinterpret_cast<T *>(smem + L::pbest_v);
     uint32_t *pbest_i = reinterpret_cast<uint32_t *>(smem + L::pbest_i);
     uint64_t *bar = reinterpret_cast<uint64_t *>(smem + L::barrier);
+    // the pair queue: CTA 0's thread 0 takes the cluster's next pair and puts
+    // it in both CTAs' word after the mbarrier
+    uint32_t *const queue = a.pair_queue;
+    uint32_t *next_s = reinterpret_cast<uint32_t *>(smem + L::barrier + 8);
+    uint32_t *next_p = cluster.map_shared_rank(next_s, peer);
     T *fbuf = reinterpret_cast<T *>(smem + L::fit_vals);
     uint32_t *fmeta = reinterpret_cast<uint32_t *>(smem + L::fit_meta);
     T *fval = reinterpret_cast<T *>(smem + L::fit_peak);
@@ -910,7 +915,10 @@ __global__ void __cluster_dims__(2, 1, 1) __launch_bounds__(cl::THREADS, 1)
     if (tma && tid == 0 && cid < a.n_pairs) issue_tile(cid);
 
     uint32_t iter = 0;
-    for (uint32_t pair = cid; pair < a.n_pairs; pair += clusters, ++iter) {
+    for (uint32_t pair = cid, npair = 0; pair < a.n_pairs; pair = npair, ++iter) {
+        // the queue's answer is needed after the row pass, which hides its latency
+        uint32_t fetched = 0;
+        if (queue && rank == 0 && tid == 0) fetched = atomicAdd(queue, 1u) + clusters;
         const uint4 it = item(pair);
         const uint32_t pic = it.x, roi = it.y, out = it.z;
         const int s = (int)it.w, s2 = s * s;
@@ -995,9 +1003,17 @@ __global__ void __cluster_dims__(2, 1, 1) __launch_bounds__(cl::THREADS, 1)
             rs[tid] = rsum.x;
             rs[N / 2 + tid] = rsum.y;
         }
+        if (queue && rank == 0 && tid == 0) {
+            *next_s = fetched;
+            *next_p = fetched;
+        }
         __syncthreads();
-        if (tma && tid == 0 && pair + clusters < a.n_pairs) issue_tile(pair + clusters);
+        if (!queue && tma && tid == 0 && pair + clusters < a.n_pairs) issue_tile(pair + clusters);
         cluster.sync();  // B1: every spectrum row and both DC/Nyquist lines are complete
+        // the cluster's next pair (past n_pairs when there is none); with a
+        // queue, this CTA's half of its ROI is requested now
+        npair = queue ? *next_s : pair + clusters;
+        if (queue && tma && tid == 0 && npair < a.n_pairs) issue_tile(npair);
 
         // ---- columns: forward FFT, conj product, inverse FFT (local) -------
         // CTA 0's slot 0 packs the DC and Nyquist columns: it is the direct
@@ -1128,13 +1144,21 @@ __global__ void __cluster_dims__(2, 1, 1) __launch_bounds__(cl::THREADS, 1)
                 fval[slot] = 2 * side != N ? pv * scale : pv;
             }
             __syncwarp();
-            const bool last = pair + clusters >= a.n_pairs;
+            const bool last = npair >= a.n_pairs;
             if (slot == 31 || last) fit_batch<T>(a, fbuf, fmeta, fval, (int)slot + 1, lane, N - 1);
         }
         __syncthreads();
     }
     // the partner may still read this CTA's shared memory: leave together
     cluster.sync();
+    if (queue && rank == 0 && tid == 0) {
+        // every cluster has taken its last pair before it counts itself done
+        __threadfence();
+        if (atomicAdd(queue + 1, 1u) == clusters - 1) {
+            atomicExch(queue, 0u);
+            atomicExch(queue + 1, 0u);
+        }
+    }
 }
 
 static cudaError_t launch_cluster(const fused_args &a, const CUtensorMap *tmap, int grid, cudaStream_t st)

@@ -48,12 +48,12 @@ struct fused_args {
     // ROI pairs per CTA: 0 for the length's default; the FP32 96-point kernel
     // with uint16 input takes 1, 2 or 4 (default: 2 with a pair queue, else 4)
     uint32_t pairs_per_cta;
-    // Optional pair queue of the one-CTA kernels (every length but the
-    // cluster's): two device words, zero at launch (the next round of pairs
-    // past the first wave, the CTAs done).  CTA b starts on round b (pairs
-    // b PPC .. b PPC + PPC - 1) and takes each further round from the queue,
-    // so CTAs on faster SMs take more pairs and the launch ends evenly; its
-    // last CTA zeroes both words.  Launches that share a queue must be
+    // Optional pair queue: two device words, zero at launch (the next round of
+    // pairs past the first wave, the CTAs or clusters done).  CTA b starts on
+    // round b (pairs b PPC .. b PPC + PPC - 1; cluster b of the 256-point
+    // kernel on pair b) and takes each further round from the queue, so CTAs
+    // on faster SMs take more pairs and the launch ends evenly; the last to
+    // finish zeroes both words.  Launches that share a queue must be
     // stream-ordered.  Null: CTA b walks rounds b, b + grid, b + 2 grid, ...
     uint32_t *pair_queue;
 };

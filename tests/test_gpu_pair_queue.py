@@ -24,13 +24,14 @@ def _scene(size, side, n):
 
 
 @pytest.mark.parametrize("side,precision", [(64, "float"), (48, "float"), (32, "float"),
-                                            (96, "float"), (64, "double")])
+                                            (96, "float"), (128, "float"), (64, "double")])
 def test_queue_and_static_walk_give_the_same_bits(side, precision):
+    # side 128: the 256-point kernel on clusters of two CTAs
     import torch
     from emida_gb300 import DeviceBuffer, GpuOffset, _lib
-    size = 512
+    size = 1024 if side == 128 else 512
     ref, uniq, begins = _scene(size, side, 4)
-    n_max = 600
+    n_max = 200 if side == 128 else 600
     pics = np.ascontiguousarray(np.resize(uniq, (n_max, size, size)))
     d_pics = DeviceBuffer.from_array(pics)
     g = GpuOffset((size, size), begins, (side, side), (2 * side - 1, 2 * side - 1), 32, "fft", 5, 1,
