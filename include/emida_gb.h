@@ -171,7 +171,10 @@ enum {
 };
 int emida_gb_set_ingest(emida_gb_handle *h, int mode);
 int emida_gb_ingest(const emida_gb_handle *h);
-/* The handle's compute stream (a cudaStream_t). */
+/* The handle's compute stream (a cudaStream_t).  The fused kernels launched on
+ * it share one pair queue, which stream order keeps to one launch at a time:
+ * work captured from this stream into a graph must not run while other work
+ * of the handle runs. */
 void *emida_gb_stream(emida_gb_handle *h);
 /* The public in_stream and out_stream members of gpu_offset
  * (src/gpu_offset.hpp:96-97): the streams of transfer_async's copies and of
@@ -249,7 +252,9 @@ int emida_gb_multi_run_slots(emida_gb_multi *m, const void *dev_patterns, uint32
 int emida_gb_multi_run_table(emida_gb_multi *m, const void *const *patterns, uint32_t n,
                              const uint32_t *layout_of, double *dev_offsets, double *dev_coefs,
                              void *dev_maxes);
-/* The planner's stream (a cudaStream_t) and a wait for its work. */
+/* The planner's stream (a cudaStream_t) and a wait for its work.  Every run of
+ * the planner launches on this stream, whose order keeps the fused kernels'
+ * shared pair queue to one launch at a time. */
 void *emida_gb_multi_stream(emida_gb_multi *m);
 int emida_gb_multi_synchronize(emida_gb_multi *m);
 /* Per ROI size class with a fused kernel, times on these patterns each
