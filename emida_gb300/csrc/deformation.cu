@@ -110,11 +110,24 @@ __global__ void __launch_bounds__(32)
                 const double x = lane < NC ? B[p * NC + lane] : 0.0;
                 const double y = lane < NC ? B[r * NC + lane] : 0.0;
                 const double al = warp_sum(x * x), be = warp_sum(y * y), ga = warp_sum(x * y);
-                if (al == 0.0 || be == 0.0 || fabs(ga) <= 1e-15 * sqrt(al * be)) continue;
+                // |ga| <= 1e-15 sqrt(al be), squared (NaN columns fail it and rotate)
+                if (al == 0.0 || be == 0.0 || ga * ga <= 1e-30 * (al * be)) continue;
                 rotated = true;
-                const double zeta = (be - al) / (2.0 * ga);
-                const double t = copysign(1.0, zeta) / (fabs(zeta) + sqrt(1.0 + zeta * zeta));
-                const double c = 1.0 / sqrt(1.0 + t * t), s = c * t;
+                // The angle only steers the sweep: t = tan of the Jacobi angle from
+                // zeta in FP32 (zeta itself in FP64, whatever the column norms;
+                // an infinite zeta gives t = 0, an underflowed one t = 1, the
+                // limits of t).  The rotation applied must be orthonormal to FP64
+                // rounding, so c = 1 / sqrt(1 + t^2) is refined from an FP32 seed
+                // by two Newton-Raphson steps for the inverse square root,
+                // c <- c (3 - u c^2) / 2, which double the correct bits each.
+                const float zf = (float)((be - al) / (2.0 * ga));
+                const float az = fabsf(zf);
+                const float tf = az > 1e18f ? 0.5f / zf : copysignf(1.0f, zf) / (az + sqrtf(1.0f + zf * zf));
+                const double t = (double)tf, u = 1.0 + t * t;
+                double c = (double)rsqrtf((float)u);
+                c = c * (1.5 - 0.5 * u * c * c);
+                c = c * (1.5 - 0.5 * u * c * c);
+                const double s = c * t;
                 if (lane < NC) {
                     B[p * NC + lane] = c * x - s * y;
                     B[r * NC + lane] = s * x + c * y;
