@@ -5,7 +5,7 @@
 // vector minimising |A x|: the right singular vector of the smallest singular
 // value, reshaped to 3 x 3 and divided by its [2][2] entry.
 //
-// One warp per pattern, FP64.  The system sits in shared memory column by
+// One warp per two patterns, FP64.  Each system sits in shared memory column by
 // column; a Householder QR reduces it to a 9 x 9 triangle R with the same right
 // singular vectors, and a one-sided (Hestenes) Jacobi SVD orthogonalises R's
 // nine columns by plane rotations: the accumulated rotations are the right
@@ -31,147 +31,195 @@ __device__ __forceinline__ double warp_sum(double v)
     return v;
 }
 
+// 16-lane sum: each half-warp reduces its own values
+__device__ __forceinline__ double half_sum(double v)
+{
+#pragma unroll
+    for (int o = 8; o; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
+    return v;
+}
+
+// Patterns per warp (PPW = 2): the warp builds and QR-reduces each pattern's
+// system in turn, then each half-warp runs one pattern's 9 x 9 Jacobi SVD, so
+// the FP64 instructions of the rotations (nine active lanes of sixteen) serve
+// two patterns at once.  PPW = 1 where two systems do not fit shared memory:
+// both halves then run the same pattern's SVD and the lower one writes it.
+template <int PPW>
 __global__ void __launch_bounds__(32)
     k_homography(const double *__restrict__ mids, const double *__restrict__ offsets, uint32_t n_rois,
-                 double cx, double cy, double cz, const double *__restrict__ coefs, double min_det,
-                 double *__restrict__ out)
+                 uint32_t patterns, double cx, double cy, double cz, const double *__restrict__ coefs,
+                 double min_det, double *__restrict__ out)
 {
     extern __shared__ double sm[];
     const uint32_t rows = 2 * n_rois;
-    double *A = sm;                  // column j: A[j * rows + i]
-    double *V = sm + NC * rows;      // V[r * NC + c], starts as the identity
-    double *B = V + NC * NC;         // R of A = QR, column-major, B[c * NC + r]
+    const size_t set = (size_t)NC * rows + 2 * NC * NC;  // one pattern's A, V and B
     const int lane = threadIdx.x;
-    const uint32_t pat = blockIdx.x;
-    const double *off = offsets + (size_t)pat * n_rois * 2;
-    const double *q = coefs ? coefs + (size_t)pat * n_rois * 6 : nullptr;
+    uint32_t kept0 = 0, kept1 = 0;
 
-    // the system of process_offsets.py:85-99, masked rows left at zero
-    uint32_t kept = 0;
-    for (uint32_t r = lane; r < n_rois; r += 32) {
-        bool keep = true;
-        if (q) {
-            const double a = -q[6 * r + 3], b = -q[6 * r + 4] / 2, c = -q[6 * r + 5];
-            keep = a * c - b * b > min_det;
-        }
-        kept += keep;
-        const double a = mids[2 * r] - cx, b = mids[2 * r + 1] - cy, z = cz;
-        const double c = a + off[2 * r], d = b + off[2 * r + 1];
-        const double e0[NC] = {-a * z, -b * z, -z * z, 0, 0, 0, a * c, b * c, z * c};
-        const double e1[NC] = {0, 0, 0, -a * z, -b * z, -z * z, a * d, b * d, z * d};
-#pragma unroll
-        for (int j = 0; j < NC; ++j) {
-            A[j * rows + 2 * r] = keep ? e0[j] : 0.0;
-            A[j * rows + 2 * r + 1] = keep ? e1[j] : 0.0;
-        }
-    }
-    for (int i = lane; i < NC * NC; i += 32) V[i] = (i / NC == i % NC) ? 1.0 : 0.0;
-#pragma unroll
-    for (int o = 16; o; o >>= 1) kept += __shfl_xor_sync(0xffffffffu, kept, o);
-    __syncwarp();
+#pragma unroll 1
+    for (int hp = 0; hp < PPW; ++hp) {
+        // a missing last pattern (odd count) runs on a copy of the last and is not written
+        const uint32_t pat = min(blockIdx.x * PPW + hp, patterns - 1);
+        double *A = sm + hp * set;       // column j: A[j * rows + i]
+        double *V = A + NC * rows;       // V[r * NC + c], starts as the identity
+        double *B = V + NC * NC;         // R of A = QR, column-major, B[c * NC + r]
+        const double *off = offsets + (size_t)pat * n_rois * 2;
+        const double *q = coefs ? coefs + (size_t)pat * n_rois * 6 : nullptr;
 
-    // Householder QR, A = QR: the right singular vectors of A are those of the
-    // 9 x 9 triangle R, so the iterative part below works on nine rows only
-    for (int k = 0; k < NC; ++k) {
-        double *ak = A + k * rows;
-        double n2 = 0;
-        for (uint32_t i = k + lane; i < rows; i += 32) n2 += ak[i] * ak[i];
-        n2 = warp_sum(n2);
-        const double x0 = ak[k];
+        // the system of process_offsets.py:85-99, masked rows left at zero
+        uint32_t kept = 0;
+        for (uint32_t r = lane; r < n_rois; r += 32) {
+            bool keep = true;
+            if (q) {
+                const double a = -q[6 * r + 3], b = -q[6 * r + 4] / 2, c = -q[6 * r + 5];
+                keep = a * c - b * b > min_det;
+            }
+            kept += keep;
+            const double a = mids[2 * r] - cx, b = mids[2 * r + 1] - cy, z = cz;
+            const double c = a + off[2 * r], d = b + off[2 * r + 1];
+            const double e0[NC] = {-a * z, -b * z, -z * z, 0, 0, 0, a * c, b * c, z * c};
+            const double e1[NC] = {0, 0, 0, -a * z, -b * z, -z * z, a * d, b * d, z * d};
+#pragma unroll
+            for (int j = 0; j < NC; ++j) {
+                A[j * rows + 2 * r] = keep ? e0[j] : 0.0;
+                A[j * rows + 2 * r + 1] = keep ? e1[j] : 0.0;
+            }
+        }
+        for (int i = lane; i < NC * NC; i += 32) V[i] = (i / NC == i % NC) ? 1.0 : 0.0;
+#pragma unroll
+        for (int o = 16; o; o >>= 1) kept += __shfl_xor_sync(0xffffffffu, kept, o);
+        if (hp == 0)
+            kept0 = kept;
+        else
+            kept1 = kept;
         __syncwarp();
-        if (n2 == 0.0) continue;  // the column is zero from row k down: R[k][k] = 0
-        const double alpha = x0 >= 0 ? -sqrt(n2) : sqrt(n2);
-        const double vtv = 2.0 * (n2 - alpha * x0);  // |x - alpha e_k|^2
-        if (lane == 0) ak[k] = x0 - alpha;          // the reflector v, in place
-        __syncwarp();
-        for (int j = k + 1; j < NC; ++j) {
-            double *aj = A + j * rows;
-            double w = 0;
-            for (uint32_t i = k + lane; i < rows; i += 32) w += ak[i] * aj[i];
-            w = warp_sum(w);
-            const double f = 2.0 * w / vtv;
-            for (uint32_t i = k + lane; i < rows; i += 32) aj[i] -= f * ak[i];
+
+        // Householder QR, A = QR: the right singular vectors of A are those of
+        // the 9 x 9 triangle R, so the iterative part below works on nine rows only
+        for (int k = 0; k < NC; ++k) {
+            double *ak = A + k * rows;
+            double n2 = 0;
+            for (uint32_t i = k + lane; i < rows; i += 32) n2 += ak[i] * ak[i];
+            n2 = warp_sum(n2);
+            const double x0 = ak[k];
+            __syncwarp();
+            if (n2 == 0.0) continue;  // the column is zero from row k down: R[k][k] = 0
+            const double alpha = x0 >= 0 ? -sqrt(n2) : sqrt(n2);
+            const double vtv = 2.0 * (n2 - alpha * x0);  // |x - alpha e_k|^2
+            if (lane == 0) ak[k] = x0 - alpha;          // the reflector v, in place
+            __syncwarp();
+            for (int j = k + 1; j < NC; ++j) {
+                double *aj = A + j * rows;
+                double w = 0;
+                for (uint32_t i = k + lane; i < rows; i += 32) w += ak[i] * aj[i];
+                w = warp_sum(w);
+                const double f = 2.0 * w / vtv;
+                for (uint32_t i = k + lane; i < rows; i += 32) aj[i] -= f * ak[i];
+                __syncwarp();
+            }
+            if (lane == 0) ak[k] = alpha;
             __syncwarp();
         }
-        if (lane == 0) ak[k] = alpha;
+        for (int i = lane; i < NC * NC; i += 32) {
+            const int c = i / NC, r = i % NC;
+            B[i] = r <= c ? A[c * rows + r] : 0.0;
+        }
         __syncwarp();
     }
-    for (int i = lane; i < NC * NC; i += 32) {
-        const int c = i / NC, r = i % NC;
-        B[i] = r <= c ? A[c * rows + r] : 0.0;
-    }
-    __syncwarp();
 
-    // cyclic one-sided Jacobi sweeps on R: lane r < 9 holds row r
+    // cyclic one-sided Jacobi sweeps on each pattern's R: half-warp hp holds
+    // pattern hp, its lane r < 9 row r.  Each half rotates by its own tests; a
+    // sweep without a rotation in either half ends the iteration.
+    const int hp = PPW == 2 ? lane >> 4 : 0, r = lane & 15;
+    const bool writer = PPW == 2 || lane < 16;
+    double *V = sm + hp * set + NC * rows;
+    double *B = V + NC * NC;
     for (int sweep = 0; sweep < MAX_SWEEPS; ++sweep) {
         bool rotated = false;
         for (int p = 0; p < NC - 1; ++p) {
-            for (int r = p + 1; r < NC; ++r) {
-                const double x = lane < NC ? B[p * NC + lane] : 0.0;
-                const double y = lane < NC ? B[r * NC + lane] : 0.0;
-                const double al = warp_sum(x * x), be = warp_sum(y * y), ga = warp_sum(x * y);
+            for (int k = p + 1; k < NC; ++k) {
+                const double x = r < NC ? B[p * NC + r] : 0.0;
+                const double y = r < NC ? B[k * NC + r] : 0.0;
+                const double al = half_sum(x * x), be = half_sum(y * y), ga = half_sum(x * y);
                 // |ga| <= 1e-15 sqrt(al be), squared (NaN columns fail it and rotate)
-                if (al == 0.0 || be == 0.0 || ga * ga <= 1e-30 * (al * be)) continue;
-                rotated = true;
-                // The angle only steers the sweep: t = tan of the Jacobi angle from
-                // zeta in FP32 (zeta itself in FP64, whatever the column norms;
-                // an infinite zeta gives t = 0, an underflowed one t = 1, the
-                // limits of t).  The rotation applied must be orthonormal to FP64
-                // rounding, so c = 1 / sqrt(1 + t^2) is refined from an FP32 seed
-                // by two Newton-Raphson steps for the inverse square root,
-                // c <- c (3 - u c^2) / 2, which double the correct bits each.
-                const float zf = (float)((be - al) / (2.0 * ga));
-                const float az = fabsf(zf);
-                const float tf = az > 1e18f ? 0.5f / zf : copysignf(1.0f, zf) / (az + sqrtf(1.0f + zf * zf));
-                const double t = (double)tf, u = 1.0 + t * t;
-                double c = (double)rsqrtf((float)u);
-                c = c * (1.5 - 0.5 * u * c * c);
-                c = c * (1.5 - 0.5 * u * c * c);
-                const double s = c * t;
-                if (lane < NC) {
-                    B[p * NC + lane] = c * x - s * y;
-                    B[r * NC + lane] = s * x + c * y;
-                    const double vx = V[lane * NC + p], vy = V[lane * NC + r];
-                    V[lane * NC + p] = c * vx - s * vy;
-                    V[lane * NC + r] = s * vx + c * vy;
+                const bool rot = !(al == 0.0 || be == 0.0 || ga * ga <= 1e-30 * (al * be));
+                if (rot) {
+                    rotated = true;
+                    // The angle only steers the sweep: t = tan of the Jacobi angle
+                    // from zeta in FP32 (zeta itself in FP64, whatever the column
+                    // norms; an infinite zeta gives t = 0, an underflowed one t = 1,
+                    // the limits of t).  The rotation applied must be orthonormal to
+                    // FP64 rounding, so c = 1 / sqrt(1 + t^2) is refined from an FP32
+                    // seed by two Newton-Raphson steps for the inverse square root,
+                    // c <- c (3 - u c^2) / 2, which double the correct bits each.
+                    const float zf = (float)((be - al) / (2.0 * ga));
+                    const float az = fabsf(zf);
+                    const float tf = az > 1e18f ? 0.5f / zf : copysignf(1.0f, zf) / (az + sqrtf(1.0f + zf * zf));
+                    const double t = (double)tf, u = 1.0 + t * t;
+                    double c = (double)rsqrtf((float)u);
+                    c = c * (1.5 - 0.5 * u * c * c);
+                    c = c * (1.5 - 0.5 * u * c * c);
+                    const double s = c * t;
+                    if (r < NC && writer) {
+                        B[p * NC + r] = c * x - s * y;
+                        B[k * NC + r] = s * x + c * y;
+                        const double vx = V[r * NC + p], vy = V[r * NC + k];
+                        V[r * NC + p] = c * vx - s * vy;
+                        V[r * NC + k] = s * vx + c * vy;
+                    }
                 }
                 __syncwarp();
             }
         }
-        if (!rotated) break;
+        if (!__any_sync(0xffffffffu, rotated)) break;
     }
 
     // the smallest singular value's column of V
     int jmin = 0;
     double smin = INFINITY;
     for (int j = 0; j < NC; ++j) {
-        const double x = lane < NC ? B[j * NC + lane] : 0.0;
-        const double n2 = warp_sum(x * x);
+        const double x = r < NC ? B[j * NC + r] : 0.0;
+        const double n2 = half_sum(x * x);
         if (n2 < smin) {
             smin = n2;
             jmin = j;
         }
     }
-    if (lane < NC) {
+    const uint32_t pat = blockIdx.x * PPW + hp;
+    if (r < NC && writer && pat < patterns) {
+        const uint32_t kept = hp ? kept1 : kept0;
         const bool enough = !coefs || kept > 10;
-        const double v = V[lane * NC + jmin], v22 = V[8 * NC + jmin];
-        out[(size_t)pat * NC + lane] = enough ? v / v22 : NAN;
+        const double v = V[r * NC + jmin], v22 = V[8 * NC + jmin];
+        out[(size_t)pat * NC + r] = enough ? v / v22 : NAN;
     }
 }
 
 }  // namespace
 
-size_t homography_smem(uint32_t n_rois) { return (size_t)(NC * 2 * n_rois + 2 * NC * NC) * sizeof(double); }
+// one pattern's system, V and R
+static size_t homography_set_bytes(uint32_t n_rois) { return (size_t)(NC * 2 * n_rois + 2 * NC * NC) * sizeof(double); }
+static bool homography_two_per_warp(uint32_t n_rois) { return 2 * homography_set_bytes(n_rois) <= 227 * 1024; }
+
 
 cudaError_t launch_homography(const double *mids, const double *offsets, uint32_t n_rois,
                               uint32_t patterns, double cx, double cy, double cz, const double *coefs,
                               double min_det, double *out, cudaStream_t st)
 {
     if (patterns == 0) return cudaSuccess;
-    const size_t smem = homography_smem(n_rois);
-    cudaError_t e = cudaFuncSetAttribute(k_homography, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+    // two patterns per warp once they leave no SM without a warp (at 256
+    // patterns on 152 SMs one per warp is 3 % faster; at 2048, two are 2.2x)
+    int dev = 0, sms = 0;
+    cudaError_t e = cudaGetDevice(&dev);
+    if (e == cudaSuccess) e = cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
     if (e != cudaSuccess) return e;
-    k_homography<<<patterns, 32, smem, st>>>(mids, offsets, n_rois, cx, cy, cz, coefs, min_det, out);
+    const bool two = homography_two_per_warp(n_rois) && patterns >= 2u * (uint32_t)sms;
+    const size_t smem = (two ? 2 : 1) * homography_set_bytes(n_rois);
+    auto k = two ? k_homography<2> : k_homography<1>;
+    e = cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+    if (e != cudaSuccess) return e;
+    const uint32_t ppw = two ? 2 : 1;
+    k<<<(patterns + ppw - 1) / ppw, 32, smem, st>>>(mids, offsets, n_rois, patterns, cx, cy, cz, coefs, min_det,
+                                                    out);
     return cudaGetLastError();
 }
 

@@ -11,8 +11,6 @@ namespace emida_gb {
 constexpr uint32_t HOMOGRAPHY_MAX_ROIS = 1600;
 constexpr uint32_t HOMOGRAPHY_MIN_ROIS = 5;
 
-size_t homography_smem(uint32_t n_rois);
-
 // mids [n_rois][2] ROI centres (x, y); offsets [patterns][n_rois][2]; coefs
 // [patterns][n_rois][6] or null (no mask); out [patterns][9] row-major 3x3.
 cudaError_t launch_homography(const double *mids, const double *offsets, uint32_t n_rois,
