@@ -1034,7 +1034,8 @@ def main():
     deformation = {"patterns_per_s": P / (fit_ms.value / 10 / 1000.0), "ms_per_step": fit_ms.value / 10,
                    "what": "per pattern a 3x3 projective map from its 100 ROI offsets "
                            "(FP64 Householder QR of the 200 x 9 system and a one-sided Jacobi SVD of "
-                           "its 9 x 9 triangle, one warp per pattern)"}
+                           "its 9 x 9 triangle; a warp per pattern, or a half-warp per pattern in the SVD "
+                           "from two patterns per SM on)"}
 
     # plain form on the same data for the fused-vs-plain ratio
     plain = None
