@@ -146,13 +146,21 @@ __global__ void __launch_bounds__(32)
                 if (rot) {
                     rotated = true;
                     // The angle only steers the sweep: t = tan of the Jacobi angle
-                    // from zeta in FP32 (zeta itself in FP64, whatever the column
-                    // norms; an infinite zeta gives t = 0, an underflowed one t = 1,
-                    // the limits of t).  The rotation applied must be orthonormal to
-                    // FP64 rounding, so c = 1 / sqrt(1 + t^2) is refined from an FP32
-                    // seed by two Newton-Raphson steps for the inverse square root,
+                    // from zeta in FP32.  zeta = (be - al) / (2 ga) is divided in FP32
+                    // where both operands' exponents are within 100 of 0 (their
+                    // exponent fields read by integer instructions), else in FP64;
+                    // an infinite zeta gives t = 0, an underflowed one t = 1, the
+                    // limits of t.  The rotation applied must be orthonormal to FP64
+                    // rounding, so c = 1 / sqrt(1 + t^2) is refined from an FP32 seed
+                    // by two Newton-Raphson steps for the inverse square root,
                     // c <- c (3 - u c^2) / 2, which double the correct bits each.
-                    const float zf = (float)((be - al) / (2.0 * ga));
+                    const double dn = be - al, dd = 2.0 * ga;
+                    const int en = (__double2hiint(dn) >> 20) & 0x7ff, ed = (__double2hiint(dd) >> 20) & 0x7ff;
+                    float zf;
+                    if (en > 1023 - 100 && en < 1023 + 100 && ed > 1023 - 100 && ed < 1023 + 100)
+                        zf = (float)dn / (float)dd;
+                    else
+                        zf = (float)(dn / dd);
                     const float az = fabsf(zf);
                     const float tf = az > 1e18f ? 0.5f / zf : copysignf(1.0f, zf) / (az + sqrtf(1.0f + zf * zf));
                     const double t = (double)tf, u = 1.0 + t * t;
