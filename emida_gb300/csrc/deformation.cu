@@ -134,13 +134,23 @@ __global__ void __launch_bounds__(32)
     const bool writer = PPW == 2 || lane < 16;
     double *V = sm + hp * set + NC * rows;
     double *B = V + NC * NC;
+    // the columns' squared norms, summed again only when a rotation changed the
+    // column (the same sums over the same values: nothing but the work changes)
+    double nrm[NC];
+#pragma unroll
+    for (int j = 0; j < NC; ++j) {
+        const double x = r < NC ? B[j * NC + r] : 0.0;
+        nrm[j] = half_sum(x * x);
+    }
     for (int sweep = 0; sweep < MAX_SWEEPS; ++sweep) {
         bool rotated = false;
+#pragma unroll
         for (int p = 0; p < NC - 1; ++p) {
+#pragma unroll
             for (int k = p + 1; k < NC; ++k) {
                 const double x = r < NC ? B[p * NC + r] : 0.0;
                 const double y = r < NC ? B[k * NC + r] : 0.0;
-                const double al = half_sum(x * x), be = half_sum(y * y), ga = half_sum(x * y);
+                const double al = nrm[p], be = nrm[k], ga = half_sum(x * y);
                 // |ga| <= 1e-15 sqrt(al be), squared (NaN columns fail it and rotate)
                 const bool rot = !(al == 0.0 || be == 0.0 || ga * ga <= 1e-30 * (al * be));
                 if (rot) {
@@ -177,6 +187,14 @@ __global__ void __launch_bounds__(32)
                     }
                 }
                 __syncwarp();
+                if (__any_sync(0xffffffffu, rot)) {
+                    // both halves take part in the sums; an unrotated half sums its
+                    // unchanged columns again
+                    const double xn = r < NC ? B[p * NC + r] : 0.0;
+                    const double yn = r < NC ? B[k * NC + r] : 0.0;
+                    nrm[p] = half_sum(xn * xn);
+                    nrm[k] = half_sum(yn * yn);
+                }
             }
         }
         if (!__any_sync(0xffffffffu, rotated)) break;
