@@ -97,3 +97,18 @@ def test_on_offsets_of_the_path():
         assert keep[k].sum() > 10
         exp = eo.homography_fit(mids[keep[k]], offs.reshape(3, S, 2)[k][keep[k]], centre)
         assert np.allclose(got[k], exp, rtol=1e-9, atol=1e-13)
+
+
+@pytest.mark.parametrize("scale_exp", [30, -40])
+def test_extreme_scales_match_oracle(scale_exp):
+    """Coordinates scaled by 2^30 and 2^-40 (exact in FP64): the system's entries scale by
+    the square, its column norms leave FP32's range (exponents past +-100), and the
+    rotations' zeta is divided in FP64 instead of FP32.  Every entry scales alike, so the
+    fitted map is the unscaled one's: both must match the oracle on the unscaled inputs."""
+    from emida_gb300 import fit_homography
+    from oracle import oracle as eo
+    mids, offs, centre = synth(71, 12)
+    f = 2.0 ** scale_exp
+    got = fit_homography(mids * f, offs * f, centre * f)
+    for k in range(len(offs)):
+        assert np.allclose(got[k], eo.homography_fit(mids, offs[k], centre), rtol=1e-9, atol=1e-13)
