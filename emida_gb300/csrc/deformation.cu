@@ -5,15 +5,16 @@
 // vector minimising |A x|: the right singular vector of the smallest singular
 // value, reshaped to 3 x 3 and divided by its [2][2] entry.
 //
-// One warp per two patterns, FP64.  Each system sits in shared memory column by
-// column; a Householder QR reduces it to a 9 x 9 triangle R with the same right
-// singular vectors, and a one-sided (Hestenes) Jacobi SVD orthogonalises R's
-// nine columns by plane rotations: the accumulated rotations are the right
+// FP64, a warp per pattern, or per two patterns where the batch has two a SM
+// and both systems fit shared memory.  Each system sits in shared memory column
+// by column; a Householder QR reduces it to a 9 x 9 triangle R with the same
+// right singular vectors, and a one-sided (Hestenes) Jacobi SVD orthogonalises
+// R's nine columns by plane rotations: the accumulated rotations are the right
 // singular vectors and the column norms the singular values.  The QR costs
-// about a tenth of the FP64 work of running the rotations over all 2S rows.  Optionally a quality mask drops
-// ROIs whose fitted peak is not a clear maximum, as jove/analyze.py:44-56 does
-// (det of the negated quadratic's Hessian <= min_det), and a pattern with ten
-// or fewer good ROIs yields NaN.
+// about a tenth of the FP64 work of running the rotations over all 2S rows.
+// Optionally a quality mask drops ROIs whose fitted peak is not a clear
+// maximum, as jove/analyze.py:44-56 does (det of the negated quadratic's
+// Hessian <= min_det), and a pattern with ten or fewer good ROIs yields NaN.
 #include <cmath>
 
 #include "deformation.cuh"
