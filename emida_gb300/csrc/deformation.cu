@@ -5,8 +5,8 @@
 // vector minimising |A x|: the right singular vector of the smallest singular
 // value, reshaped to 3 x 3 and divided by its [2][2] entry.
 //
-// FP64, a warp per pattern, or per two patterns where the batch has two a SM
-// and both systems fit shared memory.  Each system sits in shared memory column
+// FP64, a warp per pattern, or per two patterns where the batch has two
+// patterns per SM and both systems fit shared memory.  Each system sits in shared memory column
 // by column; a Householder QR reduces it to a 9 x 9 triangle R with the same
 // right singular vectors, and a one-sided (Hestenes) Jacobi SVD orthogonalises
 // R's nine columns by plane rotations: the accumulated rotations are the right
